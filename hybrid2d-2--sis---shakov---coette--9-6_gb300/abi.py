@@ -1,0 +1,177 @@
+"""ctypes binding of libhyb_gb300.so (the C ABI in include/hyb_dvm.h).
+
+The library is the only compute path: if it is missing or cannot be loaded
+every call raises; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import hyb_types as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhyb_gb300.so")
+
+# every symbol declared in include/hyb_dvm.h
+EXPORTS = [
+    "hyb_create", "hyb_destroy", "hyb_last_error", "hyb_version",
+    "hyb_init_maxwellian", "hyb_upload_f", "hyb_download_f", "hyb_download_moments",
+    "hyb_download_hot", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
+    "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
+    "hyb_launch_count", "hyb_last_step_ms", "hyb_stream",
+]
+
+_lib = None
+
+
+class HybError(RuntimeError):
+    def __init__(self, rc, msg):
+        super().__init__(f"hyb error {rc}: {msg}")
+        self.rc = rc
+
+
+def load(path=None):
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} not built: run __graft_entry__.build() first")
+    L = C.CDLL(path)
+    vp, ip, dp = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+    L.hyb_create.argtypes = [vp, vp, vp, C.POINTER(vp)]
+    L.hyb_destroy.argtypes = [vp]
+    L.hyb_last_error.argtypes = [vp]
+    L.hyb_last_error.restype = C.c_char_p
+    L.hyb_version.restype = C.c_char_p
+    L.hyb_init_maxwellian.argtypes = [vp] + [C.c_double] * 4
+    L.hyb_upload_f.argtypes = [vp, dp]
+    L.hyb_download_f.argtypes = [vp, dp]
+    L.hyb_download_moments.argtypes = [vp, dp, dp]
+    L.hyb_download_hot.argtypes = [vp, dp, dp, dp, dp]
+    L.hyb_step.argtypes = [vp, ip, vp]
+    for fn in ("hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp", "hyb_convert_ns"):
+        getattr(L, fn).argtypes = [vp]
+    L.hyb_detfp_res.argtypes = [vp, vp]
+    L.hyb_gsis_configure.argtypes = [vp, vp]
+    L.hyb_gsis_last_inner.argtypes = [vp, C.POINTER(ip)]
+    L.hyb_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.hyb_last_step_ms.argtypes = [vp, dp]
+    L.hyb_stream.argtypes = [vp, C.POINTER(vp)]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Solver:
+    """One device context for a cases.Case; methods follow the reference's
+    subroutines (GKUA_Phy_boundary, Hybrid_GKUA_Comput_Block, DETFP,
+    Convert_NS, DETFP_res, Hybrid_Time_advance_LU_SGS)."""
+
+    def __init__(self, case, precision=None, device=0):
+        self.L = load()
+        self.case = case
+        m, g, p, keep = case.c_structs()
+        if precision is not None:
+            p.precision = precision
+        p.device = device
+        self._keep = (m, g, p, keep)
+        h = C.c_void_p()
+        rc = self.L.hyb_create(C.byref(m), C.byref(g), C.byref(p), C.byref(h))
+        if rc != 0:
+            raise HybError(rc, "hyb_create failed")
+        self.h = h
+        self.nx, self.ny, self.nv = case.nx, case.ny, case.nv
+        self.P = (self.nx + 7) * (self.ny + 7)
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = self.L.hyb_last_error(self.h).decode() if self.h else ""
+            raise HybError(rc, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hyb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- the iteration -------------------------------------------------------
+    def init_maxwellian(self, rho=1.0, u=0.0, v=0.0, t=1.0):
+        self._ck(self.L.hyb_init_maxwellian(self.h, rho, u, v, t), "init_maxwellian")
+
+    def step(self, n=1, residual=True):
+        r = T.HybResidual()
+        self._ck(self.L.hyb_step(self.h, n, C.byref(r) if residual else None), "step")
+        return r.as_dict() if residual else None
+
+    def phy_boundary(self):
+        self._ck(self.L.hyb_phy_boundary(self.h), "phy_boundary")
+
+    def kinetic_step(self):
+        self._ck(self.L.hyb_kinetic_step(self.h), "kinetic_step")
+
+    def detfp(self):
+        self._ck(self.L.hyb_detfp(self.h), "detfp")
+
+    def convert_ns(self):
+        self._ck(self.L.hyb_convert_ns(self.h), "convert_ns")
+
+    def residual(self):
+        r = T.HybResidual()
+        self._ck(self.L.hyb_detfp_res(self.h, C.byref(r)), "detfp_res")
+        return r.as_dict()
+
+    def gsis(self, **kw):
+        gp = T.HybGsisParams()
+        gp.enable = kw.get("enable", 1)
+        gp.max_inner = kw.get("max_inner", 2000)
+        gp.inner_tol = kw.get("inner_tol", 1e-6)
+        gp.cfl = kw.get("cfl", 20.0)
+        gp.dtmax = kw.get("dtmax", 10.0)
+        gp.dtmin = kw.get("dtmin", 1e-7)
+        gp.flux = kw.get("flux", 5)
+        gp.ns_scheme = kw.get("ns_scheme", 1)
+        gp.use_mlp = kw.get("use_mlp", 0)
+        self._ck(self.L.hyb_gsis_configure(self.h, C.byref(gp)), "gsis_configure")
+
+    # ---- state ---------------------------------------------------------------
+    def download_f(self):
+        a = np.zeros(2 * self.P * self.nv)
+        self._ck(self.L.hyb_download_f(self.h, _dp(a)), "download_f")
+        return a
+
+    def upload_f(self, frd):
+        frd = np.ascontiguousarray(frd, dtype=np.float64)
+        self._ck(self.L.hyb_upload_f(self.h, _dp(frd)), "upload_f")
+
+    def moments(self):
+        s = np.zeros(11 * self.P)
+        cf = np.zeros((self.nx + 3) * (self.ny + 3))
+        self._ck(self.L.hyb_download_moments(self.h, _dp(s), _dp(cf)), "download_moments")
+        return s, cf
+
+    def hot(self):
+        nc = (self.nx + 3) * (self.ny + 3)
+        ti, qi, tj, qj = np.zeros(4 * nc), np.zeros(2 * nc), np.zeros(4 * nc), np.zeros(2 * nc)
+        self._ck(self.L.hyb_download_hot(self.h, _dp(ti), _dp(qi), _dp(tj), _dp(qj)), "download_hot")
+        return ti, qi, tj, qj
+
+    def launches(self):
+        n = C.c_longlong()
+        self._ck(self.L.hyb_launch_count(self.h, C.byref(n)), "launch_count")
+        return n.value
+
+    def last_ms(self):
+        x = C.c_double()
+        self._ck(self.L.hyb_last_step_ms(self.h, C.byref(x)), "last_step_ms")
+        return x.value

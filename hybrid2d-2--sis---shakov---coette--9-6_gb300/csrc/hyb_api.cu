@@ -1,0 +1,613 @@
+// hyb_api.cu -- the C ABI of include/hyb_dvm.h.
+//
+// Owns the context: geometry derived from the node coordinates (Creat_Mesh,
+// sub_init.f90:178-208; Update_coordinate_buffer_onemesh, :719-823), device
+// buffers, the reference-layout <-> device-layout transfers, and the outer
+// iteration Hybrid_Time_advance_LU_SGS (Hybrid_Sub.f90:4-160).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "hyb_common.cuh"
+
+namespace hyb {
+size_t hot_doubles(int nx, int ny);
+}
+
+#define VERSION_STRING "hyb_gb300 1.0 (sm_103a)"
+
+namespace {
+
+inline size_t XN(int nx, int i, int j) { return (size_t)(i + 1) + (size_t)(nx + 4) * (size_t)(j + 1); }
+inline size_t MI(int nx, int i, int j) { return (size_t)(i - 1) + (size_t)nx * (size_t)(j - 1); }
+
+// Creat_Mesh metrics and ghost nodes / cell centres; periodic faces take the
+// partner face's nodes shifted by the period vector.
+void build_geometry(hyb_ctx *c, const double *x, const double *y) {
+    const int nx = c->nx, ny = c->ny;
+    c->xn.assign((size_t)(nx + 4) * (ny + 4), 0.0);
+    c->yn.assign((size_t)(nx + 4) * (ny + 4), 0.0);
+    size_t nm = (size_t)nx * ny;
+    c->vol.assign(nm, 0.0); c->si.assign(nm, 0.0); c->sj.assign(nm, 0.0);
+    c->ni1.assign(nm, 0.0); c->ni2.assign(nm, 0.0); c->nj1.assign(nm, 0.0); c->nj2.assign(nm, 0.0);
+    auto &X = c->xn;
+    auto &Y = c->yn;
+    for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++) {
+            X[XN(nx, i, j)] = x[MI(nx, i, j)];
+            Y[XN(nx, i, j)] = y[MI(nx, i, j)];
+        }
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++)
+            c->vol[MI(nx, i, j)] = fabs((X[XN(nx, i, j)] - X[XN(nx, i + 1, j + 1)]) *
+                                            (Y[XN(nx, i + 1, j)] - Y[XN(nx, i, j + 1)]) -
+                                        (X[XN(nx, i + 1, j)] - X[XN(nx, i, j + 1)]) *
+                                            (Y[XN(nx, i, j)] - Y[XN(nx, i + 1, j + 1)])) * 0.5;
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx; i++) {
+            double dx = X[XN(nx, i, j + 1)] - X[XN(nx, i, j)], dy = Y[XN(nx, i, j + 1)] - Y[XN(nx, i, j)];
+            double s = sqrt(dx * dx + dy * dy);
+            c->si[MI(nx, i, j)] = s;
+            c->ni1[MI(nx, i, j)] = dy / s;
+            c->ni2[MI(nx, i, j)] = -dx / s;
+        }
+    for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+            double dx = X[XN(nx, i + 1, j)] - X[XN(nx, i, j)], dy = Y[XN(nx, i + 1, j)] - Y[XN(nx, i, j)];
+            double s = sqrt(dx * dx + dy * dy);
+            c->sj[MI(nx, i, j)] = s;
+            c->nj1[MI(nx, i, j)] = -dy / s;
+            c->nj2[MI(nx, i, j)] = dx / s;
+        }
+    for (int l = 1; l <= HYB_LAP; l++) {
+        for (int j = 1; j <= ny; j++) {
+            double px = X[XN(nx, nx, j)] - X[XN(nx, 1, j)], py = Y[XN(nx, nx, j)] - Y[XN(nx, 1, j)];
+            if (c->bc[0] == HYB_BC_PERIODIC) {
+                X[XN(nx, 1 - l, j)] = X[XN(nx, nx - l, j)] - px;
+                Y[XN(nx, 1 - l, j)] = Y[XN(nx, nx - l, j)] - py;
+                X[XN(nx, nx + l, j)] = X[XN(nx, 1 + l, j)] + px;
+                Y[XN(nx, nx + l, j)] = Y[XN(nx, 1 + l, j)] + py;
+            } else {
+                X[XN(nx, 1 - l, j)] = 2.0 * X[XN(nx, 1, j)] - X[XN(nx, 1 + l, j)];
+                Y[XN(nx, 1 - l, j)] = 2.0 * Y[XN(nx, 1, j)] - Y[XN(nx, 1 + l, j)];
+                X[XN(nx, nx + l, j)] = 2.0 * X[XN(nx, nx, j)] - X[XN(nx, nx - l, j)];
+                Y[XN(nx, nx + l, j)] = 2.0 * Y[XN(nx, nx, j)] - Y[XN(nx, nx - l, j)];
+            }
+        }
+        for (int i = 1; i <= nx; i++) {
+            double px = X[XN(nx, i, ny)] - X[XN(nx, i, 1)], py = Y[XN(nx, i, ny)] - Y[XN(nx, i, 1)];
+            if (c->bc[1] == HYB_BC_PERIODIC) {
+                X[XN(nx, i, 1 - l)] = X[XN(nx, i, ny - l)] - px;
+                Y[XN(nx, i, 1 - l)] = Y[XN(nx, i, ny - l)] - py;
+                X[XN(nx, i, ny + l)] = X[XN(nx, i, 1 + l)] + px;
+                Y[XN(nx, i, ny + l)] = Y[XN(nx, i, 1 + l)] + py;
+            } else {
+                X[XN(nx, i, 1 - l)] = 2.0 * X[XN(nx, i, 1)] - X[XN(nx, i, 1 + l)];
+                Y[XN(nx, i, 1 - l)] = 2.0 * Y[XN(nx, i, 1)] - Y[XN(nx, i, 1 + l)];
+                X[XN(nx, i, ny + l)] = 2.0 * X[XN(nx, i, ny)] - X[XN(nx, i, ny - l)];
+                Y[XN(nx, i, ny + l)] = 2.0 * Y[XN(nx, i, ny)] - Y[XN(nx, i, ny - l)];
+            }
+        }
+    }
+    for (int j = 1; j <= HYB_LAP; j++)
+        for (int i = 1; i <= HYB_LAP; i++) {
+            int i1 = 1 - i, j1 = 1 - j, i2 = nx + i, j2 = ny + j;
+            X[XN(nx, i1, j1)] = X[XN(nx, i1, 1)] + X[XN(nx, 1, j1)] - X[XN(nx, 1, 1)];
+            Y[XN(nx, i1, j1)] = Y[XN(nx, i1, 1)] + Y[XN(nx, 1, j1)] - Y[XN(nx, 1, 1)];
+            X[XN(nx, i2, j2)] = X[XN(nx, i2, ny)] + X[XN(nx, nx, j2)] - X[XN(nx, nx, ny)];
+            Y[XN(nx, i2, j2)] = Y[XN(nx, i2, ny)] + Y[XN(nx, nx, j2)] - Y[XN(nx, nx, ny)];
+            X[XN(nx, i1, j2)] = X[XN(nx, i1, ny)] + X[XN(nx, 1, j2)] - X[XN(nx, 1, ny)];
+            Y[XN(nx, i1, j2)] = Y[XN(nx, i1, ny)] + Y[XN(nx, 1, j2)] - Y[XN(nx, 1, ny)];
+            X[XN(nx, i2, j1)] = X[XN(nx, i2, 1)] + X[XN(nx, nx, j1)] - X[XN(nx, nx, 1)];
+            Y[XN(nx, i2, j1)] = Y[XN(nx, i2, 1)] + Y[XN(nx, nx, j1)] - Y[XN(nx, nx, 1)];
+        }
+    size_t nc = (size_t)(nx + 3) * (ny + 3);
+    c->x1.assign(nc, 0.0);
+    c->y1.assign(nc, 0.0);
+    for (int j = 1 - HYB_LAP; j <= ny + HYB_LAP - 1; j++)
+        for (int i = 1 - HYB_LAP; i <= nx + HYB_LAP - 1; i++) {
+            c->x1[hyb_c2(nx, i, j)] = (X[XN(nx, i, j)] + X[XN(nx, i + 1, j)] + X[XN(nx, i, j + 1)] +
+                                       X[XN(nx, i + 1, j + 1)]) * 0.25;
+            c->y1[hyb_c2(nx, i, j)] = (Y[XN(nx, i, j)] + Y[XN(nx, i + 1, j)] + Y[XN(nx, i, j + 1)] +
+                                       Y[XN(nx, i + 1, j + 1)]) * 0.25;
+        }
+}
+
+template <typename T>
+int dalloc(hyb_ctx *ctx, T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return HYB_ERR_NOMEM;
+    }
+    cudaMemsetAsync(*p, 0, n * sizeof(T), ctx->stream);
+    return HYB_OK;
+}
+
+// upload a host double array converted to the context's real type
+int upload_real(hyb_ctx *ctx, void *dst, const std::vector<double> &src) {
+    if (ctx->precision == HYB_PREC_FP64) {
+        HYB_CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> tmp(src.size());
+        for (size_t k = 0; k < src.size(); k++) tmp[k] = (float)src[k];
+        HYB_CK(cudaMemcpy(dst, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return HYB_OK;
+}
+
+void free_all(hyb_ctx *c) {
+    auto F = [](void *p) {
+        if (p) cudaFree(p);
+    };
+    F(c->d_f); F(c->d_rhs);
+    for (int k = 0; k < 4; k++) F(c->d_fw[k]);
+    F(c->d_eqp); F(c->d_vol); F(c->d_gA1); F(c->d_gA2); F(c->d_gB1); F(c->d_gB2);
+    F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_S0); F(c->d_CF); F(c->d_wall);
+    F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err);
+    if (c->h_resid) cudaFreeHost(c->h_resid);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+// cell (i,j) -> device cell index in the (a,b) layout
+inline size_t dev_cell(const hyb_ctx *c, int i, int j) {
+    int a = c->scan_is_j ? j : i, b = c->scan_is_j ? i : j;
+    return (size_t)(b - 1) * c->PA + (a - 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hyb_version(void) { return VERSION_STRING; }
+
+const char *hyb_last_error(const hyb_ctx *ctx) {
+    if (!ctx) return "null context";
+    return ctx->last_error.c_str();
+}
+
+int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_ctx **out) {
+    if (!m || !vg || !p || !out || !m->x || !m->y) return HYB_ERR_INVALID;
+    *out = nullptr;
+    if (m->nx < 3 || m->ny < 3 || vg->nvi < 1 || vg->nvj < 1) return HYB_ERR_INVALID;
+    if (!vg->vi || !vg->vj || !vg->wi || !vg->wj) return HYB_ERR_INVALID;
+    if (p->precision != HYB_PREC_FP64 && p->precision != HYB_PREC_MIXED) return HYB_ERR_INVALID;
+    if (p->scheme != HYB_SCHEME_UP1 && p->scheme != HYB_SCHEME_NND && p->scheme != HYB_SCHEME_WENO3)
+        return HYB_ERR_INVALID;
+    if (!(p->dt > 0.0) || !(p->cfc > 0.0)) return HYB_ERR_INVALID;
+    for (int f = 0; f < 4; f++) {
+        if (m->bc[f] != HYB_BC_WALL && m->bc[f] != HYB_BC_PERIODIC) return HYB_ERR_UNSUPPORTED;
+        if (m->bc[f] == HYB_BC_WALL && (!m->wall_u[f] || !m->wall_v[f] || !m->wall_t[f])) return HYB_ERR_INVALID;
+    }
+    if ((m->bc[0] == HYB_BC_PERIODIC) != (m->bc[2] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
+    if ((m->bc[1] == HYB_BC_PERIODIC) != (m->bc[3] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYB_ERR_NODEVICE;
+    if (p->device < 0 || p->device >= ndev) return HYB_ERR_INVALID;
+
+    hyb_ctx *c = new (std::nothrow) hyb_ctx();
+    if (!c) return HYB_ERR_NOMEM;
+    c->dev = p->device;
+    c->prm = *p;
+    c->precision = p->precision;
+    c->real_size = p->precision == HYB_PREC_FP64 ? sizeof(double) : sizeof(float);
+    c->nx = m->nx; c->ny = m->ny; c->ncx = m->nx - 1; c->ncy = m->ny - 1;
+    c->nvi = vg->nvi; c->nvj = vg->nvj; c->nv = vg->nvi * vg->nvj;
+    for (int f = 0; f < 4; f++) c->bc[f] = m->bc[f];
+    // the scan axis is the longer one that fits one CTA row (<= 1024 cells)
+    int ncx = c->ncx, ncy = c->ncy;
+    if (ncy >= ncx && ncy <= 1024) c->scan_is_j = 1;
+    else if (ncx <= 1024) c->scan_is_j = 0;
+    else { delete c; return HYB_ERR_UNSUPPORTED; }
+    c->Na = c->scan_is_j ? ncy : ncx;
+    c->Nb = c->scan_is_j ? ncx : ncy;
+    c->PA = (c->Na + 31) / 32 * 32;
+    // wall stencils need at least three cells along the wall-normal axis,
+    // a periodic march axis at least two
+    for (int f = 0; f < 4; f++)
+        if (m->bc[f] == HYB_BC_WALL && ((f == 0 || f == 2) ? ncx : ncy) < 4) { delete c; return HYB_ERR_UNSUPPORTED; }
+    if (c->Nb < 2) { delete c; return HYB_ERR_UNSUPPORTED; }
+
+    if (cudaSetDevice(c->dev) != cudaSuccess) { delete c; return HYB_ERR_CUDA; }
+    cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+
+    c->vi.assign(vg->vi, vg->vi + vg->nvi);
+    c->vj.assign(vg->vj, vg->vj + vg->nvj);
+    c->wi.assign(vg->wi, vg->wi + vg->nvi);
+    c->wj.assign(vg->wj, vg->wj + vg->nvj);
+    for (int f = 0; f < 4; f++) {
+        if (m->bc[f] != HYB_BC_WALL) continue;
+        int n = (f == 0 || f == 2) ? ncy : ncx;
+        c->wall_u[f].assign(m->wall_u[f], m->wall_u[f] + n);
+        c->wall_v[f].assign(m->wall_v[f], m->wall_v[f] + n);
+        c->wall_t[f].assign(m->wall_t[f], m->wall_t[f] + n);
+        for (int k = 0; k < n; k++)
+            if (!(c->wall_t[f][k] > 0.0)) { free_all(c); delete c; return HYB_ERR_INVALID; }
+    }
+    build_geometry(c, m->x, m->y);
+
+    int rc = HYB_OK;
+    const size_t ncell = (size_t)c->Nb * c->PA;
+    const size_t fsz = (size_t)c->nv * 2 * ncell;
+    const size_t rs = c->real_size;
+#define ALLOC(ptr, bytes)                                           \
+    do {                                                            \
+        if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess) {  \
+            c->last_error = "cudaMalloc failed for " #ptr;          \
+            rc = HYB_ERR_NOMEM;                                     \
+        } else                                                      \
+            cudaMemsetAsync((ptr), 0, (bytes), c->stream);          \
+    } while (0)
+    ALLOC(c->d_f, fsz * rs);
+    if (rc == HYB_OK) ALLOC(c->d_rhs, fsz * rs);
+    for (int f = 0; f < 4 && rc == HYB_OK; f++) {
+        if (m->bc[f] != HYB_BC_WALL) continue;
+        int on_scan = c->scan_is_j ? (f == 1 || f == 3) : (f == 0 || f == 2);
+        size_t n = on_scan ? c->Nb : c->PA;
+        ALLOC(c->d_fw[f], (size_t)c->nv * 2 * n * rs);
+    }
+    if (rc == HYB_OK) ALLOC(c->d_eqp, 8 * ncell * rs);
+    if (rc == HYB_OK) ALLOC(c->d_vol, ncell * rs);
+    if (rc == HYB_OK) ALLOC(c->d_gA1, (size_t)c->Nb * (c->PA + 1) * rs);
+    if (rc == HYB_OK) ALLOC(c->d_gA2, (size_t)c->Nb * (c->PA + 1) * rs);
+    if (rc == HYB_OK) ALLOC(c->d_gB1, (size_t)(c->Nb + 1) * c->PA * rs);
+    if (rc == HYB_OK) ALLOC(c->d_gB2, (size_t)(c->Nb + 1) * c->PA * rs);
+    if (rc == HYB_OK) ALLOC(c->d_vx, c->nvi * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_vy, c->nvj * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_w, c->nv * sizeof(double));
+    const size_t nc2 = (size_t)(c->nx + 3) * (c->ny + 3);
+    if (rc == HYB_OK) ALLOC(c->d_S, HYB_NSUM * nc2 * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_S0, HYB_NSUM * nc2 * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_CF, nc2 * sizeof(double));
+    const int maxfc = std::max(ncx, ncy);
+    if (rc == HYB_OK) ALLOC(c->d_wall, (size_t)4 * 6 * 4096 * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_x1, nc2 * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_y1, nc2 * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_hot, hyb::hot_doubles(c->nx, c->ny) * sizeof(double));
+    size_t nblk = (size_t)((c->Na + 31) / 32) * c->Nb;
+    if (rc == HYB_OK) ALLOC(c->d_resid, (16 + 8 * nblk) * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_err, sizeof(int));
+#undef ALLOC
+    if (rc == HYB_OK && cudaMallocHost((void **)&c->h_resid, 16 * sizeof(double)) != cudaSuccess) rc = HYB_ERR_NOMEM;
+    if (rc == HYB_OK && maxfc > 4096) { rc = HYB_ERR_UNSUPPORTED; c->last_error = "wall longer than 4096 cells"; }
+    if (rc != HYB_OK) {
+        free_all(c);
+        delete c;
+        return rc;
+    }
+    // geometry in the (a,b) layout
+    std::vector<double> vol(ncell, 1.0), gA1((size_t)c->Nb * (c->PA + 1), 0.0), gA2(gA1.size(), 0.0);
+    std::vector<double> gB1((size_t)(c->Nb + 1) * c->PA, 0.0), gB2(gB1.size(), 0.0);
+    const int nx = c->nx;
+    for (int b = 1; b <= c->Nb; b++)
+        for (int a = 1; a <= c->Na; a++) {
+            int i = c->scan_is_j ? b : a, j = c->scan_is_j ? a : b;
+            vol[(size_t)(b - 1) * c->PA + (a - 1)] = c->vol[MI(nx, i, j)];
+        }
+    for (int b = 1; b <= c->Nb; b++)
+        for (int q = 1; q <= c->Na + 1; q++) {
+            size_t k = (size_t)(b - 1) * (c->PA + 1) + (q - 1);
+            if (c->scan_is_j) {   // j-face (i=b, j=q)
+                gA1[k] = c->nj1[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
+                gA2[k] = c->nj2[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
+            } else {              // i-face (i=q, j=b)
+                gA1[k] = c->ni1[MI(nx, q, b)] * c->si[MI(nx, q, b)];
+                gA2[k] = c->ni2[MI(nx, q, b)] * c->si[MI(nx, q, b)];
+            }
+        }
+    for (int q = 1; q <= c->Nb + 1; q++)
+        for (int a = 1; a <= c->Na; a++) {
+            size_t k = (size_t)(q - 1) * c->PA + (a - 1);
+            if (c->scan_is_j) {   // i-face (i=q, j=a)
+                gB1[k] = c->ni1[MI(nx, q, a)] * c->si[MI(nx, q, a)];
+                gB2[k] = c->ni2[MI(nx, q, a)] * c->si[MI(nx, q, a)];
+            } else {              // j-face (i=a, j=q)
+                gB1[k] = c->nj1[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
+                gB2[k] = c->nj2[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
+            }
+        }
+    int r2 = upload_real(c, c->d_vol, vol);
+    if (!r2) r2 = upload_real(c, c->d_gA1, gA1);
+    if (!r2) r2 = upload_real(c, c->d_gA2, gA2);
+    if (!r2) r2 = upload_real(c, c->d_gB1, gB1);
+    if (!r2) r2 = upload_real(c, c->d_gB2, gB2);
+    std::vector<double> w((size_t)c->nv);
+    for (int jv = 0; jv < c->nvj; jv++)
+        for (int iv = 0; iv < c->nvi; iv++) w[(size_t)iv + (size_t)c->nvi * jv] = c->wi[iv] * c->wj[jv];
+    // wall data per face: u, v, t, normal (x, y) and orientation of the
+    // reference (GKUA_wall_functions.f90:34-42)
+    std::vector<double> wall((size_t)4 * 6 * 4096, 0.0);
+    for (int f = 0; f < 4; f++) {
+        if (m->bc[f] != HYB_BC_WALL) continue;
+        int n = (f == 0 || f == 2) ? ncy : ncx;
+        for (int k = 0; k < n; k++) {
+            double *d = &wall[((size_t)f * 4096 + k) * 6];
+            d[0] = c->wall_u[f][k];
+            d[1] = c->wall_v[f][k];
+            d[2] = c->wall_t[f][k];
+            if (f == 0) { d[3] = c->ni1[MI(nx, 1, k + 1)]; d[4] = c->ni2[MI(nx, 1, k + 1)]; d[5] = 1.0; }
+            if (f == 1) { d[3] = c->nj1[MI(nx, k + 1, 1)]; d[4] = c->nj2[MI(nx, k + 1, 1)]; d[5] = 1.0; }
+            if (f == 2) { d[3] = c->ni1[MI(nx, c->nx, k + 1)]; d[4] = c->ni2[MI(nx, c->nx, k + 1)]; d[5] = -1.0; }
+            if (f == 3) { d[3] = c->nj1[MI(nx, k + 1, c->ny)]; d[4] = c->nj2[MI(nx, k + 1, c->ny)]; d[5] = -1.0; }
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!r2) {
+        e = cudaMemcpy(c->d_vx, c->vi.data(), c->nvi * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c->d_vy, c->vj.data(), c->nvj * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c->d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c->d_wall, wall.data(), wall.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c->d_x1, c->x1.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c->d_y1, c->y1.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { c->last_error = cudaGetErrorString(e); r2 = HYB_ERR_CUDA; }
+    }
+    if (!r2 && cudaStreamSynchronize(c->stream) != cudaSuccess) r2 = HYB_ERR_CUDA;
+    if (r2) {
+        free_all(c);
+        delete c;
+        return r2;
+    }
+    c->gsis.enable = 0;
+    *out = c;
+    return HYB_OK;
+}
+
+int hyb_destroy(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    cudaStreamSynchronize(ctx->stream);
+    hyb::ns_destroy(ctx);
+    free_all(ctx);
+    delete ctx;
+    return HYB_OK;
+}
+
+static int check_err_word(hyb_ctx *ctx) {
+    int h = 0;
+    HYB_CK(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    if (h != 0) {
+        ctx->last_error = "device error word set (bounded wait expired)";
+        cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream);
+        return h;
+    }
+    return HYB_OK;
+}
+
+// DETFP + GKUA_DET_wall + periodic S exchange
+int hyb_detfp(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    int rc = hyb::launch_moments(ctx);
+    if (!rc) rc = hyb::launch_sghost(ctx);
+    return rc;
+}
+
+int hyb_phy_boundary(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    return hyb::launch_wall(ctx);
+}
+
+int hyb_kinetic_step(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    int rc = hyb::launch_sweep(ctx, 1);
+    if (!rc) ctx->rhs_valid = 1;
+    return rc;
+}
+
+int hyb_convert_ns(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    return hyb::launch_convert_ns(ctx);
+}
+
+int hyb_detfp_res(hyb_ctx *ctx, hyb_residual *out) {
+    if (!ctx || !out) return HYB_ERR_INVALID;
+    if (!ctx->rhs_valid) {
+        ctx->last_error = "no RHS stored yet";
+        return HYB_ERR_INVALID;
+    }
+    int rc = hyb::launch_residual(ctx, out);
+    if (rc) return rc;
+    for (int k = 0; k < 4; k++)
+        if (!isfinite(out->res_rms[k]) || !isfinite(out->res_max[k])) return HYB_ERR_NONFINITE;
+    return HYB_OK;
+}
+
+int hyb_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t) {
+    if (!ctx) return HYB_ERR_INVALID;
+    if (!(rho > 0) || !(t > 0)) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    int rc = hyb::launch_init_maxwellian(ctx, rho, u, v, t);
+    // CF of the uniform state before the first DETFP (init_flow_zero)
+    if (!rc) rc = hyb_phy_boundary(ctx);
+    if (!rc) rc = hyb_detfp(ctx);
+    if (!rc) rc = hyb_convert_ns(ctx);
+    if (!rc) {
+        HYB_CK(cudaStreamSynchronize(ctx->stream));
+        ctx->rhs_valid = 0;
+    }
+    return rc;
+}
+
+int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
+    if (!ctx || n_iter < 1) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const size_t nc2 = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
+    HYB_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    for (int it = 0; it < n_iter; it++) {
+        const bool last = (it == n_iter - 1);
+        if (ctx->gsis.enable)
+            HYB_CK(cudaMemcpyAsync(ctx->d_S0, ctx->d_S, HYB_NSUM * nc2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+        int rc = hyb::launch_wall(ctx);
+        if (!rc) rc = hyb::launch_sweep(ctx, last ? 1 : 0);
+        if (!rc) rc = hyb::launch_moments(ctx);
+        if (!rc) rc = hyb::launch_sghost(ctx);
+        if (!rc) rc = hyb::launch_convert_ns(ctx);
+        if (!rc && ctx->gsis.enable) rc = hyb::gsis_solve(ctx);
+        if (rc) return rc;
+    }
+    ctx->rhs_valid = 1;
+    HYB_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (out) {
+        int rc = hyb::launch_residual(ctx, out);
+        if (rc) return rc;
+    }
+    HYB_CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->last_ms = ms;
+    int rc = check_err_word(ctx);
+    if (rc) return rc;
+    if (out)
+        for (int k = 0; k < 4; k++)
+            if (!isfinite(out->res_rms[k])) return HYB_ERR_NONFINITE;
+    return HYB_OK;
+}
+
+// ---- transfers -------------------------------------------------------------
+int hyb_upload_f(hyb_ctx *ctx, const double *frd) {
+    if (!ctx || !frd) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const int nx = ctx->nx, ny = ctx->ny, pw = nx + 7;
+    const size_t P = (size_t)(nx + 7) * (ny + 7), ncell = (size_t)ctx->Nb * ctx->PA;
+    std::vector<double> buf((size_t)ctx->nv * 2 * ncell, 0.0);
+    for (int v = 0; v < ctx->nv; v++)
+        for (int j = 1; j <= ny - 1; j++)
+            for (int i = 1; i <= nx - 1; i++) {
+                size_t src = ((size_t)v * P + (size_t)(i + 3) + (size_t)pw * (j + 3)) * 2;
+                size_t dc = dev_cell(ctx, i, j);
+                buf[(size_t)v * 2 * ncell + dc] = frd[src + 0];
+                buf[(size_t)v * 2 * ncell + ncell + dc] = frd[src + 1];
+            }
+    int rc = upload_real(ctx, ctx->d_f, buf);
+    if (rc) return rc;
+    rc = hyb_phy_boundary(ctx);
+    if (!rc) rc = hyb_detfp(ctx);
+    if (!rc) rc = hyb_convert_ns(ctx);
+    if (!rc) HYB_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->rhs_valid = 0;
+    return rc;
+}
+
+int hyb_download_f(hyb_ctx *ctx, double *frd) {
+    if (!ctx || !frd) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const int nx = ctx->nx, ny = ctx->ny, pw = nx + 7;
+    const size_t P = (size_t)(nx + 7) * (ny + 7), ncell = (size_t)ctx->Nb * ctx->PA;
+    const size_t n = (size_t)ctx->nv * 2 * ncell;
+    std::vector<double> buf(n);
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->precision == HYB_PREC_FP64) {
+        HYB_CK(cudaMemcpy(buf.data(), ctx->d_f, n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> tmp(n);
+        HYB_CK(cudaMemcpy(tmp.data(), ctx->d_f, n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < n; k++) buf[k] = tmp[k];
+    }
+    for (int v = 0; v < ctx->nv; v++)
+        for (int j = 1; j <= ny - 1; j++)
+            for (int i = 1; i <= nx - 1; i++) {
+                size_t dst = ((size_t)v * P + (size_t)(i + 3) + (size_t)pw * (j + 3)) * 2;
+                size_t dc = dev_cell(ctx, i, j);
+                frd[dst + 0] = buf[(size_t)v * 2 * ncell + dc];
+                frd[dst + 1] = buf[(size_t)v * 2 * ncell + ncell + dc];
+            }
+    return HYB_OK;
+}
+
+int hyb_download_moments(hyb_ctx *ctx, double *s_gkua, double *cf) {
+    if (!ctx || (!s_gkua && !cf)) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const int nx = ctx->nx, ny = ctx->ny, pw = nx + 7;
+    const size_t nc2 = (size_t)(nx + 3) * (ny + 3);
+    std::vector<double> S(HYB_NSUM * nc2), C(nc2);
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    HYB_CK(cudaMemcpy(S.data(), ctx->d_S, S.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    HYB_CK(cudaMemcpy(C.data(), ctx->d_CF, C.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int j = -1; j <= ny + 1; j++)
+        for (int i = -1; i <= nx + 1; i++) {
+            size_t c2 = hyb_c2(nx, i, j);
+            size_t ix = (size_t)(i + 3) + (size_t)pw * (j + 3);
+            if (s_gkua)
+                for (int k = 0; k < HYB_NSUM; k++) s_gkua[ix * HYB_NSUM + k] = S[(size_t)k * nc2 + c2];
+            if (cf) cf[c2] = C[c2];
+        }
+    return HYB_OK;
+}
+
+int hyb_download_hot(hyb_ctx *ctx, double *tao_i, double *q_i, double *tao_j, double *q_j) {
+    if (!ctx) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const size_t nc2 = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
+    std::vector<double> H(hyb::hot_doubles(ctx->nx, ctx->ny));
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    HYB_CK(cudaMemcpy(H.data(), ctx->d_hot, H.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    // d_hot: U[4] d uu vv T amu tin_i[4] qin_i[2] tin_j[4] qin_j[2] tg_i[4] qg_i[2] tg_j[4] qg_j[2]
+    const double *tg_i = H.data() + 21 * nc2, *qg_i = tg_i + 4 * nc2, *tg_j = qg_i + 2 * nc2, *qg_j = tg_j + 4 * nc2;
+    for (size_t c = 0; c < nc2; c++) {
+        if (tao_i) for (int k = 0; k < 4; k++) tao_i[c * 4 + k] = tg_i[k * nc2 + c];
+        if (q_i) for (int k = 0; k < 2; k++) q_i[c * 2 + k] = qg_i[k * nc2 + c];
+        if (tao_j) for (int k = 0; k < 4; k++) tao_j[c * 4 + k] = tg_j[k * nc2 + c];
+        if (q_j) for (int k = 0; k < 2; k++) q_j[c * 2 + k] = qg_j[k * nc2 + c];
+    }
+    return HYB_OK;
+}
+
+// ---- GSIS ------------------------------------------------------------------
+int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp) {
+    if (!ctx || !gp) return HYB_ERR_INVALID;
+    ctx->gsis = *gp;
+    if (gp->enable) return hyb::ns_create(ctx);
+    return HYB_OK;
+}
+
+int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner) {
+    if (!ctx || !n_inner) return HYB_ERR_INVALID;
+    *n_inner = ctx->gsis_last_inner;
+    return HYB_OK;
+}
+
+// ---- introspection -----------------------------------------------------------
+int hyb_launch_count(const hyb_ctx *ctx, long long *count) {
+    if (!ctx || !count) return HYB_ERR_INVALID;
+    *count = ctx->launches;
+    return HYB_OK;
+}
+
+int hyb_last_step_ms(const hyb_ctx *ctx, double *ms) {
+    if (!ctx || !ms) return HYB_ERR_INVALID;
+    *ms = ctx->last_ms;
+    return HYB_OK;
+}
+
+int hyb_stream(const hyb_ctx *ctx, void **stream) {
+    if (!ctx || !stream) return HYB_ERR_INVALID;
+    *stream = (void *)ctx->stream;
+    return HYB_OK;
+}
+
+}  // extern "C"
+
+// GSIS solver entry points; the synthetic solve lives in hyb_gsis.cu
+namespace hyb {
+__attribute__((weak)) int ns_create(hyb_ctx *ctx) {
+    ctx->last_error = "GSIS synthetic solve not built";
+    return HYB_ERR_UNSUPPORTED;
+}
+__attribute__((weak)) void ns_destroy(hyb_ctx *) {}
+__attribute__((weak)) int gsis_solve(hyb_ctx *ctx) {
+    ctx->last_error = "GSIS synthetic solve not built";
+    return HYB_ERR_UNSUPPORTED;
+}
+}  // namespace hyb

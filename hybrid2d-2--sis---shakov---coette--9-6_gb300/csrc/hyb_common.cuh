@@ -1,0 +1,136 @@
+// hyb_common.cuh -- shared device/host definitions of the GB300 kinetic solver.
+//
+// Device layout (one structured block, Couette-type boundaries):
+//   The two mesh directions are renamed by their role in the fused LU-SGS
+//   kernel: the SCAN axis "a" (contiguous in memory, the forward recurrence
+//   along it is evaluated as a parallel affine scan) and the MARCH axis "b"
+//   (walked sequentially by each CTA).  Which reference direction (i or j)
+//   plays which role is chosen per context (scan_is_j).
+//   f      : real[Nv][NRD][Nb][PA]      interior cells only, PA = Na rounded up
+//                                        to a multiple of 32 (128-B rows)
+//   fw_*   : real[Nv][NRD][n]           wall slot values (the reference's
+//                                        ghost index -3 / n+3)
+//   eqp    : real4[2][Nb*PA]            Shakhov parameters per cell
+//   S      : double[NSUM][(nx+3)(ny+3)] moments on the reference extents
+//                                        (1-LAP:n+LAP-1), i fastest
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/hyb_dvm.h"
+
+#define HYB_LAP 2
+#define HYB_PI 3.1415926535897932
+
+// REAL(4) literals of the reference widened to double
+#define HYB_FLOOR_D ((double)1.0e-30f)
+#define HYB_EPSWENO_D ((double)1.0e-15f)
+#define HYB_CWENO1_D ((double)(1.0f / 3.0f))
+#define HYB_CWENO2_D ((double)(2.0f / 3.0f))
+
+namespace hyb {
+
+// boundary kind of one end of an axis
+enum AxisBC : int { AX_PERIODIC = 0, AX_WALL = 1 };
+
+// geometry of the scan / march axes for the fused kernel
+struct AxisGeom {
+    int n;          // cells along the axis
+    int bc_lo, bc_hi;  // AX_*
+};
+
+template <typename real>
+struct KinArgs {
+    real *f;              // [Nv][2][Nb][PA]
+    real *rhs;            // optional RHS store (same layout) or nullptr
+    const real *fw_alo, *fw_ahi;   // wall slots at the scan-axis ends [Nv][2][Nb]
+    const real *fw_blo, *fw_bhi;   // wall slots at the march-axis ends [Nv][2][PA]
+    const real *eqp;      // [8][Nb*PA]: crt, u, v, invT, hT, cqx, cqy, cf
+    const real *vol;      // [Nb*PA] cell volume
+    // face normal * length, per face: scan faces [Nb][PA+1] (2 comps), march
+    // faces [Nb+1][PA] (2 comps)
+    const real *gA1, *gA2, *gB1, *gB2;
+    const double *vx, *vy; // velocity nodes per v (v = iv + nvi*jv)
+    int nvi, nv;
+    int Na, Nb, PA;
+    int bca_lo, bca_hi, bcb_lo, bcb_hi;
+    int scheme;
+    int scan_is_j;         // 1: scan axis = reference j
+    real dt;
+    int *err;              // device error word
+};
+
+}  // namespace hyb
+
+// ---- host-side context -------------------------------------------------------
+struct hyb_ctx {
+    int dev;
+    cudaStream_t stream;
+    cudaEvent_t ev0, ev1;
+    int precision;
+    int nx, ny, ncx, ncy, nvi, nvj, nv;
+    int scan_is_j, Na, Nb, PA;
+    int bc[4];
+    hyb_params prm;
+    std::string last_error;
+    long long launches;
+    double last_ms;
+    size_t real_size;
+
+    // host copies of inputs
+    std::vector<double> vi, vj, wi, wj;
+    std::vector<double> wall_u[4], wall_v[4], wall_t[4];
+    std::vector<double> xn, yn;            // nodes with ghosts (1-LAP:n+LAP)
+    std::vector<double> vol, si, sj, ni1, ni2, nj1, nj2;  // (nx,ny)
+    std::vector<double> x1, y1;            // (1-LAP:n+LAP-1)
+    int uniform;                           // Cartesian uniform spacing
+
+    // device buffers
+    void *d_f, *d_rhs, *d_fw[4], *d_eqp, *d_vol, *d_gA1, *d_gA2, *d_gB1, *d_gB2;
+    double *d_vx, *d_vy, *d_w;             // per-velocity nodes and weights
+    double *d_S;                           // [NSUM][(nx+3)(ny+3)]
+    double *d_S0;
+    double *d_CF;                          // [(nx+3)(ny+3)]
+    double *d_wall;                        // per wall face: u, v, t, normal
+    double *d_x1, *d_y1;
+    double *d_hot;                         // HoT + NSF arrays (see hyb_ns.cu)
+    double *d_resid;                       // residual partials / result
+    int *d_err;
+    double *h_resid;                       // pinned
+    int rhs_valid;
+    // GSIS
+    hyb_gsis_params gsis;
+    int gsis_last_inner;
+    void *ns;                              // NS solver state (hyb_ns.cu)
+};
+
+#define HYB_CK(call)                                                              \
+    do {                                                                          \
+        cudaError_t _e = (call);                                                  \
+        if (_e != cudaSuccess) {                                                  \
+            ctx->last_error = std::string(#call) + ": " + cudaGetErrorString(_e); \
+            return HYB_ERR_CUDA;                                                  \
+        }                                                                         \
+    } while (0)
+
+// C2 index on the (1-LAP:n+LAP-1) extents
+__host__ __device__ inline size_t hyb_c2(int nx, int i, int j) {
+    return (size_t)(i + 1) + (size_t)(nx + 3) * (size_t)(j + 1);
+}
+
+// launch helpers implemented in the .cu files
+namespace hyb {
+int launch_wall(hyb_ctx *ctx);
+int launch_sweep(hyb_ctx *ctx, int store_rhs);
+int launch_moments(hyb_ctx *ctx);
+int launch_sghost(hyb_ctx *ctx);
+int launch_residual(hyb_ctx *ctx, hyb_residual *out);
+int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);
+int launch_convert_ns(hyb_ctx *ctx);
+int ns_create(hyb_ctx *ctx);
+void ns_destroy(hyb_ctx *ctx);
+int gsis_solve(hyb_ctx *ctx);
+}  // namespace hyb

@@ -1,0 +1,41 @@
+"""One tiny kinetic iteration on cuda:0 checked against the CPU oracle."""
+import sys
+import time
+
+import numpy as np
+
+from . import abi, cases
+
+
+def run():
+    from oracle import oracle as O   # the checker only
+    c = cases.couette_small(ncy=32, nvx=16, nvy=16, dt=0.05)
+    t0 = time.time()
+    g = abi.Solver(c, precision=0)
+    g.init_maxwellian()
+    rg = g.step(2)
+    o = O.Oracle(c, threads=0)
+    o.init_maxwellian()
+    ro = o.step(2)
+    P = (c.nx + 7) * (c.ny + 7)
+    fg = g.download_f().reshape(c.nv, c.ny + 7, c.nx + 7, 2)[:, 4:4 + c.ny - 1, 4:4 + c.nx - 1]
+    fo = o.frd().reshape(c.nv, c.ny + 7, c.nx + 7, 2)[:, 4:4 + c.ny - 1, 4:4 + c.nx - 1]
+    err = float(np.abs(fg - fo).max() / np.abs(fo).max())
+    rerr = abs(rg["max_rms"] - ro["max_rms"]) / ro["max_rms"]
+    launches = g.launches()
+    g.close()
+    print(f"smoke: {c.name} fp64 2 steps on cuda:0: max rel f err {err:.2e}, residual rel err {rerr:.2e}, "
+          f"{launches} kernel launches, {time.time() - t0:.1f}s")
+    if not (err < 1e-11 and rerr < 1e-9):
+        raise AssertionError(f"GPU result differs from the oracle: f {err:.3e} residual {rerr:.3e}")
+    # mixed precision path as well
+    g = abi.Solver(c, precision=1)
+    g.init_maxwellian()
+    rm = g.step(2)
+    g.close()
+    if not (abs(rm["max_rms"] - ro["max_rms"]) < 1e-3 * ro["max_rms"]):
+        raise AssertionError("mixed-precision residual far from the FP64 oracle")
+
+
+if __name__ == "__main__":
+    sys.exit(run())

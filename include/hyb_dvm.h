@@ -1,0 +1,194 @@
+/*
+ * hyb_dvm.h -- C ABI of the GB300 discrete-velocity Shakhov solver.
+ *
+ * This is the drop-in boundary for the kinetic hot path of Hybrid2D.  In the
+ * reference every routine on that path is an argument-less Fortran subroutine
+ * that reads and writes module globals (Global_Var, Com_ctrl in
+ * Hybrid2D/src/COMMONDATA.f90:28-170).  Here the same state lives in an opaque
+ * context that owns all device memory; the Fortran host keeps its mesh, input
+ * and restart handling and passes plain arrays (Fortran column-major, the
+ * reference's own extents) through these entry points.  A Fortran
+ * ISO_C_BINDING interface module for every function is in hyb_dvm.f90.
+ *
+ * Conventions
+ *   - every call returns an int status: HYB_OK (0) or a negative HYB_ERR_*;
+ *     nothing aborts the process (the reference uses STOP / MPI_FINALIZE);
+ *   - host arrays stay owned by the caller; the context owns device buffers;
+ *   - one host thread per context; contexts are independent;
+ *   - device waits are bounded and surface as HYB_ERR_TIMEOUT.
+ *
+ * Index conventions follow the reference: a block has nx*ny mesh NODES, cells
+ * are i=1..nx-1, j=1..ny-1, i-faces i=1..nx, j-faces j=1..ny.  The block faces
+ * are numbered like Bc%face in Hybrid2D/src/sub_init.f90:269-277:
+ * 1 = i-min, 2 = j-min, 3 = i-max, 4 = j-max.
+ */
+#ifndef HYB_DVM_H
+#define HYB_DVM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define HYB_OK                 0
+#define HYB_ERR_INVALID       -1   /* bad argument / size / null pointer      */
+#define HYB_ERR_NOMEM         -2   /* device or host allocation failed        */
+#define HYB_ERR_CUDA          -3   /* CUDA runtime error                      */
+#define HYB_ERR_NONFINITE     -4   /* NaN/Inf detected in a residual          */
+#define HYB_ERR_TIMEOUT       -5   /* a bounded device wait ran out           */
+#define HYB_ERR_UNSUPPORTED   -6   /* configuration outside the built scope   */
+#define HYB_ERR_TEMPERATURE   -7   /* NS temperature below 0.1 (reference
+                                      sub_NS_singlegrid.f90:148-151 STOPs)    */
+#define HYB_ERR_NODEVICE      -8   /* no CUDA device / extension not usable   */
+
+/* ---- boundary kinds (values follow const_var, COMMONDATA.f90:14) -------- */
+#define HYB_BC_WALL        (-2)    /* diffuse wall, GKUA_boundary.f90:49-100  */
+#define HYB_BC_PERIODIC      1     /* face connected to the opposite face of
+                                      the same block (inner boundary with
+                                      neighb = own block, GKUA_boundary.f90:
+                                      400-633 exchange semantics)            */
+
+/* ---- kinetic spatial schemes (GKUA_Scheme_*, COMMONDATA.f90:18) -------- */
+#define HYB_SCHEME_UP1     0
+#define HYB_SCHEME_NND     1
+#define HYB_SCHEME_WENO3   3
+
+/* ---- precision modes ---------------------------------------------------- */
+#define HYB_PREC_FP64      0       /* f, fluxes, sweeps, moments in FP64      */
+#define HYB_PREC_MIXED     1       /* f, fluxes, sweeps in FP32; moments,
+                                      residual, synthetic solve in FP64      */
+
+/* ---- moment vector length (Nsum, COMMONDATA.f90:4) ---------------------- */
+#define HYB_NSUM          11
+#define HYB_NRD            2       /* reduced distributions G and H          */
+
+/* Mesh of one structured block.  Node coordinates are (nx, ny) Fortran
+ * column-major, exactly B%x / B%y as read by Creat_Mesh
+ * (Hybrid2D/src/sub_init.f90:178-180).  The library derives vol, si, sj,
+ * ni1, ni2, nj1, nj2 (sub_init.f90:183-208) and the ghost-node / cell-centre
+ * coordinates (sub_init.f90:719-823) itself. */
+typedef struct hyb_mesh {
+    int nx, ny;                 /* nodes; nx >= 3, ny >= 5                    */
+    const double *x, *y;        /* node coordinates, nx*ny each               */
+    int bc[4];                  /* HYB_BC_* for faces 1..4                    */
+    /* Diffuse-wall data per wall face, one value per face cell in face order
+     * (faces 2/4: i=1..nx-1, faces 1/3: j=1..ny-1).  NULL for non-wall faces.
+     * The reference hard-codes wall_u=wall_v=0 (GKUA_boundary.f90:66-67) and
+     * one global Twall; here every face cell carries its own values. */
+    const double *wall_u[4], *wall_v[4], *wall_t[4];
+} hyb_mesh;
+
+/* Discrete velocity grid (GKUA_lisansudu.f90).  w_i / w_j are the complete
+ * one-dimensional moment weights: FBAV*w for Gauss-Legendre
+ * (GKUA_DETFP.f90:314), w*exp(v^2) for half-range Gauss-Hermite
+ * (GKUA_DETFP.f90:200-202), the Newton-Cotes rule for uniform grids. */
+typedef struct hyb_vgrid {
+    int nvi, nvj;
+    const double *vi, *vj;      /* nodes                                      */
+    const double *wi, *wj;      /* full 1-D weights                           */
+} hyb_vgrid;
+
+/* Solver parameters (control.in / Com_ctrl equivalents). */
+typedef struct hyb_params {
+    double dt;          /* dt_global_GKUA (GKUA_Residual.f90:27)              */
+    double cfc;         /* collision coefficient delta (sub_init.f90:65)      */
+    double cpr;         /* Shakhov coefficient (1-Pr)/(5/2) (sub_init.f90:66) */
+    double x1s;         /* 1 - viscosity exponent omega (sub_init.f90:14)    */
+    double r00, t00;    /* positivity fall-backs of DETFP (GKUA_DETFP.f90:63,72) */
+    int    scheme;      /* HYB_SCHEME_*                                       */
+    int    precision;   /* HYB_PREC_*                                         */
+    /* macroscopic (NS / GSIS) scaling, sub_init.f90:16-66 */
+    double gamma, ma, pr, re;   /* Re = cfc * Ma * sqrt(2 gamma)             */
+    double omega_ns;            /* NS viscosity exponent; the reference's
+                                   get_viscous hard-codes 0.81
+                                   (sub_Residual.f90:563)                    */
+    int    device;              /* CUDA device ordinal                       */
+    int    reserved[7];
+} hyb_params;
+
+/* Residual of the kinetic iteration: moments 1..4 of the last RHS,
+ * DETFP_res (GKUA_DETFP_RES.f90:4-60). */
+typedef struct hyb_residual {
+    double res_max[4];
+    double res_rms[4];
+    double max_rms;             /* max over the four rms values               */
+} hyb_residual;
+
+/* Parameters of the GSIS synthetic macroscopic solve (the commented coupling
+ * of Hybrid_Sub.f90:45-153 plus the NS solver of sub_NS_singlegrid.f90). */
+typedef struct hyb_gsis_params {
+    int    enable;          /* 0: plain kinetic iteration                    */
+    int    max_inner;       /* cap on NS inner iterations per outer step     */
+    double inner_tol;       /* reference: res_iter > 1e-6 (Hybrid_Sub.f90:99) */
+    double cfl, dtmax, dtmin;   /* local time step (sub_NS_singlegrid.f90:160-183) */
+    int    flux;            /* NS flux splitting, Flux_* (COMMONDATA.f90:12) */
+    int    ns_scheme;       /* NS reconstruction scheme, Scheme_* (:11)      */
+    int    use_mlp;         /* use the learned closure as warm start         */
+    int    reserved[5];
+} hyb_gsis_params;
+
+typedef struct hyb_ctx hyb_ctx;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* Replaces init / Alloc_GKUA_FRD (sub_init.f90:6-79, 329-386). */
+int hyb_create(const hyb_mesh *mesh, const hyb_vgrid *vgrid,
+               const hyb_params *params, hyb_ctx **out);
+int hyb_destroy(hyb_ctx *ctx);
+/* Human-readable text of the last error on this context (never NULL). */
+const char *hyb_last_error(const hyb_ctx *ctx);
+/* Library version / build string. */
+const char *hyb_version(void);
+
+/* ---- state transfer ----------------------------------------------------- */
+/* Uniform Maxwellian initial state and first moments: init_flow_zero +
+ * GKUA_sudufenbu (sub_init.f90:390-463, GKUA_sudufenbu.f90:22-53). */
+int hyb_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);
+/* f in the reference layout FRD(NRD,-3:nx+3,-3:ny+3,NVIT,NVJT), column-major
+ * (COMMONDATA.f90:49, sub_init.f90:344).  Interior cells are transferred;
+ * upload recomputes the moments (backup_Mesco_read + DETFP,
+ * Backup_write_read.f90:93-108). */
+int hyb_upload_f(hyb_ctx *ctx, const double *frd);
+int hyb_download_f(hyb_ctx *ctx, double *frd);
+/* S_GKUA(Nsum,-3:nx+3,-3:ny+3) (sub_init.f90:351) after DETFP: rho, u, v, T,
+ * Pxx, Pyy, Pxy, qx, qy, Pzz, 0; CF(-1:nx+1,-1:ny+1) may be NULL. */
+int hyb_download_moments(hyb_ctx *ctx, double *s_gkua, double *cf);
+/* Higher-order terms of Convert_NS (Hybrid_Sub.f90:191-461):
+ * TaoNSi_G(4,-1:nx+1,-1:ny+1), Qi_G(2,...), TaoNSj_G(4,...), Qj_G(2,...).
+ * Any pointer may be NULL. */
+int hyb_download_hot(hyb_ctx *ctx, double *tao_i, double *q_i,
+                     double *tao_j, double *q_j);
+
+/* ---- the iteration (Hybrid_Time_advance_LU_SGS, Hybrid_Sub.f90:4-160) --- */
+/* n_iter outer iterations; each runs the boundary conditions, the kinetic
+ * LU-SGS step, the moments, the wall moments, Convert_NS and (when enabled)
+ * the GSIS synthetic solve.  If out != NULL the residual of the last
+ * iteration (DETFP_res) is written to it. */
+int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out);
+/* The same stages one at a time, named after the reference subroutines. */
+int hyb_phy_boundary(hyb_ctx *ctx);          /* GKUA_Phy_boundary          */
+int hyb_kinetic_step(hyb_ctx *ctx);          /* Hybrid_GKUA_Comput_Block   */
+int hyb_detfp(hyb_ctx *ctx);                 /* DETFP + GKUA_DET_wall      */
+int hyb_convert_ns(hyb_ctx *ctx);            /* Convert_NS                 */
+int hyb_detfp_res(hyb_ctx *ctx, hyb_residual *out);   /* DETFP_res         */
+
+/* ---- GSIS synthetic solve ---------------------------------------------- */
+int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp);
+/* Inner NS iterations used by the last outer iteration (Mesh%iter). */
+int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner);
+
+/* ---- timing / introspection -------------------------------------------- */
+/* Number of kernel launches issued by this context since creation. */
+int hyb_launch_count(const hyb_ctx *ctx, long long *count);
+/* Milliseconds of the last hyb_step measured with CUDA events on the
+ * context's stream. */
+int hyb_last_step_ms(const hyb_ctx *ctx, double *ms);
+/* Raw CUDA stream handle (cudaStream_t) the context launches on. */
+int hyb_stream(const hyb_ctx *ctx, void **stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYB_DVM_H */

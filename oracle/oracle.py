@@ -1,0 +1,173 @@
+"""ctypes driver of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module, as the checker.  It is never imported by the product package.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhyb_oracle.so")
+
+_lib = None
+
+
+def build(force=False):
+    if force or not os.path.exists(LIB_PATH) or \
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "hyb_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+        L.orc_create.argtypes = [vp, vp, vp, C.POINTER(vp)]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_set_threads.argtypes = [ip]
+        L.orc_init_maxwellian.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+        for fn in ("orc_exchange_f", "orc_phy_boundary", "orc_kinetic_step", "orc_detfp", "orc_convert_ns"):
+            getattr(L, fn).argtypes = [vp]
+        L.orc_detfp_res.argtypes = [vp, vp]
+        L.orc_step.argtypes = [vp, ip, vp]
+        for fn in ("orc_frd", "orc_frd00", "orc_s", "orc_cf"):
+            getattr(L, fn).argtypes = [vp]
+            getattr(L, fn).restype = dp
+        L.orc_upload_f.argtypes = [vp, dp]
+        L.orc_hot.argtypes = [vp, dp, dp, dp, dp]
+        L.orc_nsf_in.argtypes = [vp, dp, dp, dp, dp]
+        L.orc_err.argtypes = [vp]
+        L.orc_err.restype = C.c_double
+        L.orc_geometry.argtypes = [vp] + [dp] * 9
+        L.orc_grid_gl.argtypes = [C.c_double, ip, C.c_double, ip, ip, dp, dp]
+        L.orc_grid_nc.argtypes = [ip, C.c_double, C.c_double, ip, dp, dp]
+        L.orc_cfc_vhs.argtypes = [C.c_double] * 10 + [dp]
+        L.orc_cfc_vhs.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """One oracle instance for a cases.Case."""
+
+    def __init__(self, case, threads=0):
+        from_types = case.c_structs()
+        self.case = case
+        self._m, self._g, self._p, self._keep = from_types
+        self.L = lib()
+        if threads:
+            self.L.orc_set_threads(threads)
+        h = C.c_void_p()
+        rc = self.L.orc_create(C.byref(self._m), C.byref(self._g), C.byref(self._p), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"orc_create failed: {rc}")
+        self.h = h
+        self.nx, self.ny, self.nv = case.nx, case.ny, case.nv
+        self.P = (self.nx + 7) * (self.ny + 7)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.orc_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    # ---- stages ------------------------------------------------------------
+    def init_maxwellian(self, rho=1.0, u=0.0, v=0.0, t=1.0):
+        return self.L.orc_init_maxwellian(self.h, rho, u, v, t)
+
+    def exchange_f(self):
+        return self.L.orc_exchange_f(self.h)
+
+    def phy_boundary(self):
+        return self.L.orc_phy_boundary(self.h)
+
+    def kinetic_step(self):
+        return self.L.orc_kinetic_step(self.h)
+
+    def detfp(self):
+        return self.L.orc_detfp(self.h)
+
+    def convert_ns(self):
+        return self.L.orc_convert_ns(self.h)
+
+    def residual(self):
+        from importlib import import_module
+        T = _types()
+        r = T.HybResidual()
+        self.L.orc_detfp_res(self.h, C.byref(r))
+        return r.as_dict()
+
+    def step(self, n=1):
+        T = _types()
+        r = T.HybResidual()
+        rc = self.L.orc_step(self.h, n, C.byref(r))
+        if rc != 0:
+            raise RuntimeError(f"orc_step failed: {rc}")
+        return r.as_dict()
+
+    # ---- state -------------------------------------------------------------
+    def frd(self):
+        """FRD(NRD,-3:nx+3,-3:ny+3,NVI,NVJ) as a Fortran-ordered array view copy."""
+        n = 2 * self.P * self.nv
+        a = np.ctypeslib.as_array(self.L.orc_frd(self.h), shape=(n,)).copy()
+        return a
+
+    def frd00(self):
+        n = 2 * self.P * self.nv
+        return np.ctypeslib.as_array(self.L.orc_frd00(self.h), shape=(n,)).copy()
+
+    def s_gkua(self):
+        n = 11 * self.P
+        return np.ctypeslib.as_array(self.L.orc_s(self.h), shape=(n,)).copy()
+
+    def cf(self):
+        return np.ctypeslib.as_array(self.L.orc_cf(self.h), shape=(self.P,)).copy()
+
+    def upload_f(self, frd):
+        frd = np.ascontiguousarray(frd, dtype=np.float64)
+        return self.L.orc_upload_f(self.h, _dp(frd))
+
+    def hot(self):
+        nc = (self.nx + 3) * (self.ny + 3)
+        ti, qi, tj, qj = np.zeros(4 * nc), np.zeros(2 * nc), np.zeros(4 * nc), np.zeros(2 * nc)
+        self.L.orc_hot(self.h, _dp(ti), _dp(qi), _dp(tj), _dp(qj))
+        return ti, qi, tj, qj
+
+    def err(self):
+        return self.L.orc_err(self.h)
+
+
+def _types():
+    import sys
+    return sys.modules["hyb_gb300.hyb_types"]
+
+
+def grid_gl(dv, n, vdown, kgln, single_literals=1):
+    m = n * kgln
+    v, w = np.zeros(m), np.zeros(m)
+    lib().orc_grid_gl(dv, n, vdown, kgln, single_literals, _dp(v), _dp(w))
+    return v, w
+
+
+def grid_nc(n, vdown, vup, rule=0):
+    v, w = np.zeros(n), np.zeros(n)
+    lib().orc_grid_nc(n, vdown, vup, rule, _dp(v), _dp(w))
+    return v, w
+
+
+def cfc_vhs(mole_mass, gamma, alp, omg, vis_ref, tref, ma, nd_inf, t_inf, lref):
+    re = C.c_double()
+    c = lib().orc_cfc_vhs(mole_mass, gamma, alp, omg, vis_ref, tref, ma, nd_inf, t_inf, lref, C.byref(re))
+    return c, re.value

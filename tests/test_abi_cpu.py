@@ -1,0 +1,92 @@
+"""C-ABI checks that need no GPU: exports, struct layout, argument errors."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hyb_dvm.h")
+
+
+def _declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+char\s*\*|int)\s*(hyb_\w+)\s*\(", txt, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    from hyb_gb300 import build, abi
+    build.build_all()
+    return abi.load()
+
+
+def test_header_and_binding_agree(pkg):
+    from hyb_gb300 import abi
+    assert _declared() == sorted(abi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in _declared():
+        assert hasattr(lib, name), name
+
+
+def test_version_string(lib):
+    assert b"sm_103a" in lib.hyb_version()
+
+
+def test_struct_layout_matches_c(pkg):
+    from hyb_gb300 import hyb_types as T
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "hyb_dvm.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu\n", sizeof(hyb_mesh), sizeof(hyb_vgrid), sizeof(hyb_params),
+         sizeof(hyb_residual), sizeof(hyb_gsis_params));
+  printf("%zu %zu %zu %zu\n", offsetof(hyb_mesh, wall_t), offsetof(hyb_params, omega_ns),
+         offsetof(hyb_params, device), offsetof(hyb_gsis_params, use_mlp));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        cfile, exe = os.path.join(d, "p.c"), os.path.join(d, "p")
+        open(cfile, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), cfile, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    sizes = [C.sizeof(T.HybMesh), C.sizeof(T.HybVgrid), C.sizeof(T.HybParams), C.sizeof(T.HybResidual),
+             C.sizeof(T.HybGsisParams)]
+    offs = [T.HybMesh.wall_t.offset, T.HybParams.omega_ns.offset, T.HybParams.device.offset,
+            T.HybGsisParams.use_mlp.offset]
+    assert [int(x) for x in out] == sizes + offs
+
+
+def test_invalid_arguments_are_rejected_without_a_device(lib, pkg):
+    from hyb_gb300 import cases, hyb_types as T
+    c = cases.couette_small(ncy=16, nvx=8, nvy=8)
+    m, g, p, keep = c.c_structs()
+    h = C.c_void_p()
+    assert lib.hyb_create(None, C.byref(g), C.byref(p), C.byref(h)) == T.HYB_ERR_INVALID
+    bad = T.HybParams.from_buffer_copy(p)
+    bad.dt = -1.0
+    assert lib.hyb_create(C.byref(m), C.byref(g), C.byref(bad), C.byref(h)) == T.HYB_ERR_INVALID
+    bad = T.HybParams.from_buffer_copy(p)
+    bad.precision = 7
+    assert lib.hyb_create(C.byref(m), C.byref(g), C.byref(bad), C.byref(h)) == T.HYB_ERR_INVALID
+    mm = T.HybMesh.from_buffer_copy(m)
+    mm.bc[0] = 99
+    assert lib.hyb_create(C.byref(mm), C.byref(g), C.byref(p), C.byref(h)) == T.HYB_ERR_UNSUPPORTED
+    mm = T.HybMesh.from_buffer_copy(m)
+    mm.bc[2] = T.HYB_BC_WALL       # periodic face without its partner
+    assert lib.hyb_create(C.byref(mm), C.byref(g), C.byref(p), C.byref(h)) == T.HYB_ERR_INVALID
+    # a valid request either needs a device or succeeds on one
+    rc = lib.hyb_create(C.byref(m), C.byref(g), C.byref(p), C.byref(h))
+    assert rc in (T.HYB_OK, T.HYB_ERR_NODEVICE)
+    if rc == T.HYB_OK:
+        lib.hyb_destroy(h)
+    # null context calls fail cleanly
+    assert lib.hyb_step(None, 1, None) == T.HYB_ERR_INVALID
+    assert lib.hyb_destroy(None) == T.HYB_ERR_INVALID
+    assert lib.hyb_last_error(None) == b"null context"
