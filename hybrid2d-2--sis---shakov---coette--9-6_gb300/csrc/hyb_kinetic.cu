@@ -63,9 +63,12 @@ __device__ __forceinline__ void fence_async_shared() {
 }
 
 // bounded wait: returns false when the spin limit ran out
-#define HYB_SPIN_LIMIT (1u << 26)
+// (about two seconds of SM clock; the normal wait is well under a microsecond)
+#define HYB_SPIN_CYCLES 4000000000LL
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (uint32_t it = 0; it < HYB_SPIN_LIMIT; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (clock64() - t0 < HYB_SPIN_CYCLES)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -224,7 +227,9 @@ __global__ void __launch_bounds__(1024) k_sweep(KinArgs<real> A) {
     }
     __syncthreads();
     if (producer) {
-        for (int bp = -1; bp <= RING - 2; bp++) issue_row(bp);
+        // rows -1 .. RING-3 fill slots 0 .. RING-2; step b refills the slot of
+        // row b-3 with row b+RING-3 (slot RING-1 is first filled at step 1)
+        for (int bp = -1; bp <= RING - 3; bp++) issue_row(bp);
         if (perB) {   // rows Nb+1, Nb+2 are the old rows 1, 2
             for (int w = 0; w < 2; w++) {
                 mbar_arrive_expect_tx(&bars[RING + w], 2 * row_bytes);
@@ -448,16 +453,8 @@ __global__ void __launch_bounds__(1024) k_sweep(KinArgs<real> A) {
         A.f[vrow0 + c1] = fg;
         A.f[vrow0 + rstride + c1] = fh;
     }
-    // drain: wait for the look-ahead copies still in flight before exiting
-    if (vok) {
-        for (int bp = Nb + 1; bp <= Nb + RING - 3; bp++) {
-            if (bp > Nb) {
-                int s = (bp + 1) % RING;
-                uint32_t par = (uint32_t)(((bp + 1) / RING) & 1);
-                mbar_wait_bounded(&bars[s], par);
-            }
-        }
-    }
+    // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
+    // for above, so no copy is in flight when the CTA exits
 }
 
 // ---------------------------------------------------------------------------
