@@ -19,8 +19,10 @@ EXPORTS = [
     "hyb_init_maxwellian", "hyb_upload_f", "hyb_download_f", "hyb_download_moments",
     "hyb_download_hot", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
     "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
-    "hyb_launch_count", "hyb_last_step_ms", "hyb_stream",
+    "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
+    "hyb_profile_enable", "hyb_profile_read",
 ]
+STAGES = ["wall", "sweep", "moments", "sghost", "convert_ns", "gsis", "residual"]
 
 _lib = None
 
@@ -60,6 +62,9 @@ def load(path=None):
     L.hyb_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.hyb_last_step_ms.argtypes = [vp, dp]
     L.hyb_stream.argtypes = [vp, C.POINTER(vp)]
+    L.hyb_set_walls.argtypes = [vp, ip, dp, dp, dp]
+    L.hyb_profile_enable.argtypes = [vp, ip]
+    L.hyb_profile_read.argtypes = [vp, dp, C.POINTER(C.c_longlong), ip]
     _lib = L
     return L
 
@@ -170,6 +175,20 @@ class Solver:
         n = C.c_longlong()
         self._ck(self.L.hyb_launch_count(self.h, C.byref(n)), "launch_count")
         return n.value
+
+    def set_walls(self, face, u, v, t):
+        u, v, t = (np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, t))
+        self._ck(self.L.hyb_set_walls(self.h, face, _dp(u), _dp(v), _dp(t)), "set_walls")
+
+    def profile(self, enable=True):
+        self._ck(self.L.hyb_profile_enable(self.h, 1 if enable else 0), "profile_enable")
+
+    def profile_read(self):
+        n = len(STAGES)
+        ms = np.zeros(n)
+        ln = (C.c_longlong * n)()
+        self._ck(self.L.hyb_profile_read(self.h, _dp(ms), ln, n), "profile_read")
+        return {s: (float(ms[k]), int(ln[k])) for k, s in enumerate(STAGES)}
 
     def last_ms(self):
         x = C.c_double()

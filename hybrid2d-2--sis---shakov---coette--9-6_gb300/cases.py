@@ -86,6 +86,7 @@ class Case:
     pr: float = 2.0 / 3.0
     gamma: float = 5.0 / 3.0
     nc_rule: int = 1         # the reference NewtonCotes pattern (GKUA_DETFP.f90:419-444)
+    stretch: float = 0.0     # >0: tanh clustering of the y nodes towards both plates
     extra: dict = field(default_factory=dict)
 
     # ---- derived arrays -------------------------------------------------
@@ -107,7 +108,11 @@ class Case:
 
     def nodes(self):
         xs = np.linspace(0.0, self.lx, self.nx)
-        ys = np.linspace(0.0, self.ly, self.ny)
+        eta = np.linspace(0.0, 1.0, self.ny)
+        if self.stretch > 0.0:
+            ys = self.ly * 0.5 * (1.0 + np.tanh(self.stretch * (2.0 * eta - 1.0)) / np.tanh(self.stretch))
+        else:
+            ys = self.ly * eta
         X, Y = np.meshgrid(xs, ys, indexing="ij")      # (nx, ny)
         return np.asfortranarray(X), np.asfortranarray(Y)
 

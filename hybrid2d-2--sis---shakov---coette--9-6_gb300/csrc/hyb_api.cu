@@ -6,6 +6,8 @@
 // iteration Hybrid_Time_advance_LU_SGS (Hybrid_Sub.f90:4-160).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -151,8 +153,10 @@ void free_all(hyb_ctx *c) {
     for (int k = 0; k < 4; k++) F(c->d_fw[k]);
     F(c->d_eqp); F(c->d_vol); F(c->d_gA1); F(c->d_gA2); F(c->d_gB1); F(c->d_gB2);
     F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_S0); F(c->d_CF); F(c->d_wall);
-    F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err);
+    F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err); F(c->d_mpart);
     if (c->h_resid) cudaFreeHost(c->h_resid);
+    if (c->h_wall) cudaFreeHost(c->h_wall);
+    for (auto ev : c->prof_ev) cudaEventDestroy(ev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -210,7 +214,9 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     else { delete c; return HYB_ERR_UNSUPPORTED; }
     c->Na = c->scan_is_j ? ncy : ncx;
     c->Nb = c->scan_is_j ? ncx : ncy;
-    c->PA = (c->Na + 31) / 32 * 32;
+    // cells per sweep thread: chunks must tile the scan axis exactly
+    c->cpt = (c->Na % 4 == 0 && c->Na >= 128) ? 4 : ((c->Na % 2 == 0 && c->Na >= 64) ? 2 : 1);
+    c->PA = (c->Na + 32 * c->cpt - 1) / (32 * c->cpt) * (32 * c->cpt);
     // wall stencils need at least three cells along the wall-normal axis,
     // a periodic march axis at least two
     for (int f = 0; f < 4; f++)
@@ -278,6 +284,7 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     size_t nblk = (size_t)((c->Na + 31) / 32) * c->Nb;
     if (rc == HYB_OK) ALLOC(c->d_resid, (16 + 8 * nblk) * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_err, sizeof(int));
+    if (rc == HYB_OK) ALLOC(c->d_mpart, (size_t)hyb::moments_slices(c) * 10 * ncell * sizeof(double));
 #undef ALLOC
     if (rc == HYB_OK && cudaMallocHost((void **)&c->h_resid, 16 * sizeof(double)) != cudaSuccess) rc = HYB_ERR_NOMEM;
     if (rc == HYB_OK && maxfc > 4096) { rc = HYB_ERR_UNSUPPORTED; c->last_error = "wall longer than 4096 cells"; }
@@ -317,6 +324,25 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
                 gB2[k] = c->nj2[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
             }
         }
+    // uniform Cartesian spacing: one face speed per axis and one volume
+    {
+        auto same = [](const std::vector<double> &x, size_t n0, size_t n, size_t stride, size_t len) {
+            (void)n0;
+            double ref = x[0];
+            for (size_t r = 0; r < n; r++)
+                for (size_t k = 0; k < len; k++) {
+                    double y = x[r * stride + k];
+                    if (fabs(y - ref) > 1e-12 * (fabs(ref) + 1e-300) && !(ref == 0.0 && y == 0.0)) return false;
+                }
+            return true;
+        };
+        bool u = same(vol, 0, c->Nb, c->PA, c->Na) && same(gA1, 0, c->Nb, c->PA + 1, c->Na + 1) &&
+                 same(gA2, 0, c->Nb, c->PA + 1, c->Na + 1) && same(gB1, 0, c->Nb + 1, c->PA, c->Na) &&
+                 same(gB2, 0, c->Nb + 1, c->PA, c->Na);
+        // a zero normal component must be exactly zero everywhere
+        for (size_t k = 0; u && k < gA2.size(); k++) (void)0;
+        c->uniform = u ? 1 : 0;
+    }
     int r2 = upload_real(c, c->d_vol, vol);
     if (!r2) r2 = upload_real(c, c->d_gA1, gA1);
     if (!r2) r2 = upload_real(c, c->d_gA2, gA2);
@@ -342,6 +368,8 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
             if (f == 3) { d[3] = c->nj1[MI(nx, k + 1, c->ny)]; d[4] = c->nj2[MI(nx, k + 1, c->ny)]; d[5] = -1.0; }
         }
     }
+    c->wall_host = wall;
+    if (!r2 && cudaMallocHost((void **)&c->h_wall, (size_t)6 * 4096 * sizeof(double)) != cudaSuccess) r2 = HYB_ERR_NOMEM;
     cudaError_t e = cudaSuccess;
     if (!r2) {
         e = cudaMemcpy(c->d_vx, c->vi.data(), c->nvi * sizeof(double), cudaMemcpyHostToDevice);
@@ -359,6 +387,15 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         return r2;
     }
     c->gsis.enable = 0;
+    // launch-shape override, "cpt,vpb,minb"
+    if (const char *e = getenv("HYB_SWEEP_SHAPE")) {
+        int a = 0, b = 0, d = 0;
+        if (sscanf(e, "%d,%d,%d", &a, &b, &d) == 3 && (a == 1 || a == 2 || a == 4) && c->cpt % a == 0) {
+            c->sw_cpt = a;
+            c->sw_vpb = b;
+            c->sw_minb = d;
+        }
+    }
     *out = c;
     return HYB_OK;
 }
@@ -439,39 +476,127 @@ int hyb_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t) 
     return rc;
 }
 
+}  // extern "C"
+
+namespace {
+enum Stage { ST_WALL = 0, ST_SWEEP, ST_MOM, ST_SGHOST, ST_CNS, ST_GSIS, ST_RESID, ST_COUNT };
+
+// run one stage, bracketed by events when profiling is on
+template <typename F>
+int staged(hyb_ctx *ctx, int stage, size_t *evi, F &&fn) {
+    if (!ctx->prof_on) return fn();
+    if (*evi + 2 > ctx->prof_ev.size()) {
+        for (int k = 0; k < 64; k++) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return HYB_ERR_CUDA;
+            ctx->prof_ev.push_back(e);
+        }
+    }
+    long long l0 = ctx->launches;
+    cudaEventRecord(ctx->prof_ev[*evi], ctx->stream);
+    int rc = fn();
+    cudaEventRecord(ctx->prof_ev[*evi + 1], ctx->stream);
+    ctx->prof_stage.push_back(stage);
+    ctx->prof_launch[stage] += ctx->launches - l0;
+    *evi += 2;
+    return rc;
+}
+
+int collect_profile(hyb_ctx *ctx, size_t nev) {
+    if (!ctx->prof_on || nev == 0) return HYB_OK;
+    HYB_CK(cudaEventSynchronize(ctx->prof_ev[nev - 1]));
+    for (size_t k = 0; k + 1 < nev; k += 2) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->prof_ev[k], ctx->prof_ev[k + 1]);
+        ctx->prof_ms[ctx->prof_stage[k / 2]] += ms;
+    }
+    ctx->prof_stage.clear();
+    return HYB_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
     if (!ctx || n_iter < 1) return HYB_ERR_INVALID;
     cudaSetDevice(ctx->dev);
     const size_t nc2 = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
+    size_t evi = 0;
+    ctx->prof_stage.clear();
     HYB_CK(cudaEventRecord(ctx->ev0, ctx->stream));
     for (int it = 0; it < n_iter; it++) {
         const bool last = (it == n_iter - 1);
         if (ctx->gsis.enable)
             HYB_CK(cudaMemcpyAsync(ctx->d_S0, ctx->d_S, HYB_NSUM * nc2 * sizeof(double), cudaMemcpyDeviceToDevice,
                                    ctx->stream));
-        int rc = hyb::launch_wall(ctx);
-        if (!rc) rc = hyb::launch_sweep(ctx, last ? 1 : 0);
-        if (!rc) rc = hyb::launch_moments(ctx);
-        if (!rc) rc = hyb::launch_sghost(ctx);
-        if (!rc) rc = hyb::launch_convert_ns(ctx);
-        if (!rc && ctx->gsis.enable) rc = hyb::gsis_solve(ctx);
+        int rc = staged(ctx, ST_WALL, &evi, [&] { return hyb::launch_wall(ctx); });
+        if (!rc) rc = staged(ctx, ST_SWEEP, &evi, [&] { return hyb::launch_sweep(ctx, last ? 1 : 0); });
+        if (!rc) rc = staged(ctx, ST_MOM, &evi, [&] { return hyb::launch_moments(ctx); });
+        if (!rc) rc = staged(ctx, ST_SGHOST, &evi, [&] { return hyb::launch_sghost(ctx); });
+        if (!rc) rc = staged(ctx, ST_CNS, &evi, [&] { return hyb::launch_convert_ns(ctx); });
+        if (!rc && ctx->gsis.enable) rc = staged(ctx, ST_GSIS, &evi, [&] { return hyb::gsis_solve(ctx); });
         if (rc) return rc;
     }
     ctx->rhs_valid = 1;
     HYB_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (out) {
-        int rc = hyb::launch_residual(ctx, out);
+        int rc = staged(ctx, ST_RESID, &evi, [&] { return hyb::launch_residual(ctx, out); });
         if (rc) return rc;
     }
     HYB_CK(cudaEventSynchronize(ctx->ev1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     ctx->last_ms = ms;
-    int rc = check_err_word(ctx);
+    int rc = collect_profile(ctx, evi);
+    if (rc) return rc;
+    rc = check_err_word(ctx);
     if (rc) return rc;
     if (out)
         for (int k = 0; k < 4; k++)
             if (!isfinite(out->res_rms[k])) return HYB_ERR_NONFINITE;
+    return HYB_OK;
+}
+
+int hyb_set_walls(hyb_ctx *ctx, int face, const double *wall_u, const double *wall_v, const double *wall_t) {
+    if (!ctx || face < 1 || face > 4 || !wall_u || !wall_v || !wall_t) return HYB_ERR_INVALID;
+    if (ctx->bc[face - 1] != HYB_BC_WALL) return HYB_ERR_INVALID;
+    const int n = (face == 1 || face == 3) ? ctx->ncy : ctx->ncx;
+    for (int k = 0; k < n; k++)
+        if (!(wall_t[k] > 0.0)) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    // the staging buffer may still feed a previous copy
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    double *tab = &ctx->wall_host[(size_t)(face - 1) * 4096 * 6];
+    for (int k = 0; k < n; k++) {
+        tab[k * 6 + 0] = wall_u[k];
+        tab[k * 6 + 1] = wall_v[k];
+        tab[k * 6 + 2] = wall_t[k];
+        ctx->wall_u[face - 1][k] = wall_u[k];
+        ctx->wall_v[face - 1][k] = wall_v[k];
+        ctx->wall_t[face - 1][k] = wall_t[k];
+    }
+    memcpy(ctx->h_wall, tab, (size_t)n * 6 * sizeof(double));
+    HYB_CK(cudaMemcpyAsync(ctx->d_wall + (size_t)(face - 1) * 4096 * 6, ctx->h_wall, (size_t)n * 6 * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    return HYB_OK;
+}
+
+int hyb_profile_enable(hyb_ctx *ctx, int enable) {
+    if (!ctx) return HYB_ERR_INVALID;
+    ctx->prof_on = enable ? 1 : 0;
+    for (int k = 0; k < 8; k++) {
+        ctx->prof_ms[k] = 0.0;
+        ctx->prof_launch[k] = 0;
+    }
+    return HYB_OK;
+}
+
+int hyb_profile_read(hyb_ctx *ctx, double *ms, long long *launches, int n) {
+    if (!ctx || n < 0) return HYB_ERR_INVALID;
+    for (int k = 0; k < n && k < ST_COUNT; k++) {
+        if (ms) ms[k] = ctx->prof_ms[k];
+        if (launches) launches[k] = ctx->prof_launch[k];
+    }
     return HYB_OK;
 }
 

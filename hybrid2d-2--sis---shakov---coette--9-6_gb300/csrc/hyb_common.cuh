@@ -72,7 +72,8 @@ struct hyb_ctx {
     cudaEvent_t ev0, ev1;
     int precision;
     int nx, ny, ncx, ncy, nvi, nvj, nv;
-    int scan_is_j, Na, Nb, PA;
+    int scan_is_j, Na, Nb, PA, cpt;         // cpt: largest scan cells per sweep thread
+    int sw_cpt, sw_vpb, sw_minb;             // chosen sweep launch shape (0: default)
     int bc[4];
     hyb_params prm;
     std::string last_error;
@@ -98,9 +99,18 @@ struct hyb_ctx {
     double *d_x1, *d_y1;
     double *d_hot;                         // HoT + NSF arrays (see hyb_ns.cu)
     double *d_resid;                       // residual partials / result
+    double *d_mpart;                       // moment partial sums [VS][10][Nb*PA]
     int *d_err;
     double *h_resid;                       // pinned
     int rhs_valid;
+    // per-stage profiling (hyb_profile_enable)
+    int prof_on;
+    std::vector<cudaEvent_t> prof_ev;      // event pool, pairs per stage
+    std::vector<int> prof_stage;           // stage of each recorded pair
+    double prof_ms[8];
+    long long prof_launch[8];
+    double *h_wall;                        // pinned staging of wall data
+    std::vector<double> wall_host;         // full wall table (u,v,t,normal)
     // GSIS
     hyb_gsis_params gsis;
     int gsis_last_inner;
@@ -125,7 +135,9 @@ __host__ __device__ inline size_t hyb_c2(int nx, int i, int j) {
 namespace hyb {
 int launch_wall(hyb_ctx *ctx);
 int launch_sweep(hyb_ctx *ctx, int store_rhs);
+size_t sweep_smem_bytes(const hyb_ctx *ctx);
 int launch_moments(hyb_ctx *ctx);
+int moments_slices(const hyb_ctx *ctx);
 int launch_sghost(hyb_ctx *ctx);
 int launch_residual(hyb_ctx *ctx, hyb_residual *out);
 int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);

@@ -179,7 +179,20 @@ int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp);
 /* Inner NS iterations used by the last outer iteration (Mesh%iter). */
 int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner);
 
+/* Replace the diffuse-wall data of one wall face (1..4), one value per face
+ * cell as in hyb_mesh.  The reference passes the wall velocity on every call
+ * of GKUA_wall_boundary(nm, nn, wall_u, wall_v) (GKUA_wall_functions.f90:1)
+ * and reads Twall from a global; this is that per-call input. */
+int hyb_set_walls(hyb_ctx *ctx, int face, const double *wall_u,
+                  const double *wall_v, const double *wall_t);
+
 /* ---- timing / introspection -------------------------------------------- */
+/* Per-stage device timing with CUDA events on the context's stream.  While
+ * enabled, hyb_step brackets every stage (wall, sweep, moments, sghost,
+ * convert_ns, gsis, residual) with events and accumulates milliseconds and
+ * launch counts; hyb_profile_read returns them in that order (7 entries). */
+int hyb_profile_enable(hyb_ctx *ctx, int enable);
+int hyb_profile_read(hyb_ctx *ctx, double *ms, long long *launches, int n);
 /* Number of kernel launches issued by this context since creation. */
 int hyb_launch_count(const hyb_ctx *ctx, long long *count);
 /* Milliseconds of the last hyb_step measured with CUDA events on the

@@ -103,6 +103,15 @@ def test_fp64_transposed_orientation(cases_mod):
     _cmp_state(c, g, o, 1e-11)
 
 
+def test_fp64_stretched_mesh(cases_mod):
+    """Non-uniform spacing takes the per-face geometry path of the sweep."""
+    c = cases_mod.couette_small(ncy=32, nvx=12, nvy=12, dt=0.02, stretch=1.5)
+    g, o = _pair(c, 0)
+    g.step(3)
+    o.step(3)
+    _cmp_state(c, g, o, 1e-11)
+
+
 def test_mixed_precision_error_is_bounded(cases_mod):
     c = cases_mod.couette_small(ncy=32, nvx=16, nvy=16, dt=0.05)
     g, o = _pair(c, 1)
