@@ -136,22 +136,24 @@ template <> struct KahanAcc<float> {
 };
 
 template <typename real, int MC>
-__global__ void __launch_bounds__(256) k_moments_part(MomArgs M) {
+__global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int PA = M.PA, t = threadIdx.x, TPV = blockDim.x;
     const int b = blockIdx.x + 1, slice = blockIdx.y;
     const int a0 = t * MC + 1;
     const bool act = a0 <= M.Na;
-    const int nvj = M.nv / M.nvi;
+    const int nvi = M.nvi, nvj = M.nv / M.nvi;
     const int jv0 = (int)((long long)nvj * slice / M.vs), jv1 = (int)((long long)nvj * (slice + 1) / M.vs);
-    const int v0 = jv0 * M.nvi, v1 = jv1 * M.nvi, nloc = v1 - v0;
+    const int v0 = jv0 * nvi, nloc = (jv1 - jv0) * nvi;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
     uint64_t *empty = full + MOM_NST;
-    real *stage = reinterpret_cast<real *>(smem_raw + 256);
+    real *svx = reinterpret_cast<real *>(smem_raw + 256);          // nvi nodes
+    real *stage = reinterpret_cast<real *>(smem_raw + 256 + ((nvi * sizeof(real) + 127) / 128) * 128);
     const size_t rs = (size_t)M.Nb * PA;
     const real *f = (const real *)M.f;
     const uint32_t row_bytes = (uint32_t)(PA * sizeof(real));
     const int nwarp = TPV >> 5, lane = t & 31;
+    for (int k = t; k < nvi; k += TPV) svx[k] = (real)M.vx[k];
     if (t == 0) {
         for (int k = 0; k < MOM_NST; k++) {
             mbar_init(&full[k], 1);
@@ -169,57 +171,52 @@ __global__ void __launch_bounds__(256) k_moments_part(MomArgs M) {
     };
     if (t == 0)
         for (int n = 0; n < MOM_NST - 1 && n < nloc; n++) issue(n);
-    double acc[10][MC];
-#pragma unroll
-    for (int q = 0; q < 10; q++)
-#pragma unroll
-        for (int c = 0; c < MC; c++) acc[q][c] = 0.0;
     KahanAcc<real> ks[10][MC];
 #pragma unroll
     for (int q = 0; q < 10; q++)
 #pragma unroll
         for (int c = 0; c < MC; c++) ks[q][c].zero();
     bool ok = true;
-    for (int n = 0; n < nloc && ok; n++) {
-        const int k = n % MOM_NST;
-        // refill the slot freed by velocity n-1 with velocity n+NST-1
-        if (t == 0 && n + MOM_NST - 1 < nloc) {
-            if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
-                ok = false;
-            else
-                issue(n + MOM_NST - 1);
-        }
-        if (!mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
-        const int v = v0 + n;
-        const int iv = v % M.nvi, jv = v / M.nvi;
-        if (act && ok) {
-            const real vx = (real)M.vx[iv], vy = (real)M.vy[jv], wv = (real)M.w[v];
-            const real *g = stage + (size_t)k * 2 * PA + (a0 - 1), *h = g + PA;
-#pragma unroll
-            for (int c = 0; c < MC; c++) {
-                const real gg = g[c], hh = h[c];
-                const real vxg = vx * gg, vyg = vy * gg, vx2g = vx * vxg, vy2g = vy * vyg;
-                const real b4 = hh + vx2g + vy2g;
-                ks[0][c].add(wv * gg);
-                ks[1][c].add(wv * vxg);
-                ks[2][c].add(wv * vyg);
-                ks[3][c].add(wv * b4);
-                ks[4][c].add(wv * vx2g);
-                ks[5][c].add(wv * vy2g);
-                ks[6][c].add(wv * (vx * vy * gg));
-                ks[7][c].add(wv * (vx * b4));
-                ks[8][c].add(wv * (vy * b4));
-                ks[9][c].add(wv * hh);
+    int n = 0;
+    for (int jv = jv0; jv < jv1 && ok; jv++) {
+        const real vy = (real)M.vy[jv];
+        const double *wrow = M.w + (size_t)jv * nvi;
+        for (int iv = 0; iv < nvi && ok; iv++, n++) {
+            const int k = n % MOM_NST;
+            // refill the slot freed by velocity n-1 with velocity n+NST-1
+            if (t == 0 && n + MOM_NST - 1 < nloc) {
+                if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
+                    ok = false;
+                else
+                    issue(n + MOM_NST - 1);
             }
-            if (iv == M.nvi - 1) {   // end of a velocity row: fold into FP64
+            if (!mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
+            if (act && ok) {
+                const real vx = svx[iv], wv = (real)__ldg(wrow + iv);
+                const real *g = stage + (size_t)k * 2 * PA + (a0 - 1);
+                real gg[MC], hh[MC];
 #pragma unroll
-                for (int q = 0; q < 10; q++)
+                for (int c = 0; c < MC; c++) { gg[c] = g[c]; hh[c] = g[PA + c]; }
+                const real wx = wv * vx, wy = wv * vy, wxy = wx * vy;
 #pragma unroll
-                    for (int c = 0; c < MC; c++) acc[q][c] += ks[q][c].fold();
+                for (int c = 0; c < MC; c++) {
+                    const real wg = wv * gg[c];
+                    const real b4 = hh[c] + (vx * vx + vy * vy) * gg[c];
+                    ks[0][c].add(wg);
+                    ks[1][c].add(wx * gg[c]);
+                    ks[2][c].add(wy * gg[c]);
+                    ks[3][c].add(wv * b4);
+                    ks[4][c].add(wx * (vx * gg[c]));
+                    ks[5][c].add(wy * (vy * gg[c]));
+                    ks[6][c].add(wxy * gg[c]);
+                    ks[7][c].add(wx * b4);
+                    ks[8][c].add(wy * b4);
+                    ks[9][c].add(wv * hh[c]);
+                }
             }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[k]);
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[k]);
     }
     if (__syncthreads_or(!ok)) {
         if (t == 0) atomicExch(M.err, HYB_ERR_TIMEOUT);
@@ -231,7 +228,7 @@ __global__ void __launch_bounds__(256) k_moments_part(MomArgs M) {
 #pragma unroll
     for (int q = 0; q < 10; q++)
 #pragma unroll
-        for (int c = 0; c < MC; c++) M.part[((size_t)slice * 10 + q) * ncell + cell0 + c] = acc[q][c];
+        for (int c = 0; c < MC; c++) M.part[((size_t)slice * 10 + q) * ncell + cell0 + c] = ks[q][c].fold();
 }
 
 template <typename real>
@@ -462,6 +459,16 @@ int moments_slices(const hyb_ctx *ctx) {
     return vs;
 }
 
+template <typename real, int MC>
+static void launch_mom(hyb_ctx *ctx, const MomArgs &M, dim3 grd, int tpv, size_t smem) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_moments_part<real, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    k_moments_part<real, MC><<<grd, tpv, smem, ctx->stream>>>(M);
+}
+
 int launch_moments(hyb_ctx *ctx) {
     MomArgs M;
     M.f = ctx->d_f;
@@ -487,27 +494,21 @@ int launch_moments(hyb_ctx *ctx) {
     M.x1s = ctx->prm.x1s;
     M.r00 = ctx->prm.r00;
     M.t00 = ctx->prm.t00;
-    const int mc = ctx->cpt >= 2 ? 2 : 1;
+    // cells per thread: FP64 sums need one register pair per moment, the
+    // compensated FP32 sums two floats; both stay below 128 registers
+    const int mc = (ctx->precision == HYB_PREC_FP64 && ctx->cpt >= 4) ? 4 : (ctx->cpt >= 2 ? 2 : 1);
     const int tpv = ctx->PA / mc;
-    const size_t smem = 256 + (size_t)MOM_NST * 2 * ctx->PA * ctx->real_size;
+    const size_t smem = 256 + ((ctx->nvi * ctx->real_size + 127) / 128) * 128 +
+                        (size_t)MOM_NST * 2 * ctx->PA * ctx->real_size;
     dim3 grd(ctx->Nb, M.vs);
-    static bool attr[4] = {false, false, false, false};
     if (ctx->precision == HYB_PREC_FP64) {
-        if (mc == 2) {
-            if (!attr[0]) { cudaFuncSetAttribute(k_moments_part<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); attr[0] = true; }
-            k_moments_part<double, 2><<<grd, tpv, smem, ctx->stream>>>(M);
-        } else {
-            if (!attr[1]) { cudaFuncSetAttribute(k_moments_part<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); attr[1] = true; }
-            k_moments_part<double, 1><<<grd, tpv, smem, ctx->stream>>>(M);
-        }
+        if (mc == 4) launch_mom<double, 4>(ctx, M, grd, tpv, smem);
+        else if (mc == 2) launch_mom<double, 2>(ctx, M, grd, tpv, smem);
+        else launch_mom<double, 1>(ctx, M, grd, tpv, smem);
     } else {
-        if (mc == 2) {
-            if (!attr[2]) { cudaFuncSetAttribute(k_moments_part<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); attr[2] = true; }
-            k_moments_part<float, 2><<<grd, tpv, smem, ctx->stream>>>(M);
-        } else {
-            if (!attr[3]) { cudaFuncSetAttribute(k_moments_part<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); attr[3] = true; }
-            k_moments_part<float, 1><<<grd, tpv, smem, ctx->stream>>>(M);
-        }
+        if (mc == 4) launch_mom<float, 4>(ctx, M, grd, tpv, smem);
+        else if (mc == 2) launch_mom<float, 2>(ctx, M, grd, tpv, smem);
+        else launch_mom<float, 1>(ctx, M, grd, tpv, smem);
     }
     ctx->launches++;
     int rc = check_err(ctx, "k_moments_part");

@@ -1,523 +1,43 @@
-// hyb_sweep.cu -- the fused kinetic step of one outer iteration:
-// Get_Feq + RHSFDVsub + LU-SGS forward sweep + backward step + update + floor
-// (GKUA_Residual.f90:4-469), for every velocity node.
-//
-// Work decomposition.  One thread group per velocity node walks the MARCH
-// axis b row by row; a row of the SCAN axis a is split over the group's
-// threads, CPT consecutive cells per thread.  Rows of f are staged into a
-// shared-memory ring by cp.async.bulk copies that complete on mbarriers,
-// RING-5 = 3 rows ahead of use.
-//
-// The forward recurrence dF(a,b) = c(a,b) + p(a) dF(a-1,b), with
-// c = (vol RHS + pos(B) dF(a,b-1)) / alpha and p = pos(A) / alpha, is linear in
-// dF(a-1,b): each thread composes the affine maps of its CPT cells, the group
-// scans the composed maps (warp shuffles, then one shared-memory pass across
-// warps) and each thread replays its cells from the incoming value.  The
-// recurrence along b is carried in registers.  The reference's backward step
-// reads only forward values of the downstream neighbours
-// (GKUA_Residual.f90:64-90), so it is evaluated one row behind the forward
-// sweep and neither dF nor the RHS is written to memory (the RHS only when a
-// residual is requested).  The seam of a periodic face is explicit in both
-// sweeps, as the reference's zero FRD00 ghosts make every block face.
+// hyb_sweep.cu -- launch-shape selection and dispatch of the fused kinetic
+// sweep (kernel in hyb_sweep.cuh, instantiated per precision in
+// hyb_sweep_f32.cu / hyb_sweep_f64.cu).
 #include <cuda_runtime.h>
-#include <math.h>
 
 #include "hyb_common.cuh"
-#include "hyb_device.cuh"
 
 namespace hyb {
 
-constexpr int RING = 8;   // staged rows per velocity
+int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb);
+int sweep_launch_f64(hyb_ctx *ctx, const KinArgs<double> &A, int cpt, int vpb);
+size_t sweep_group_bytes_f32(int PA, int tpv);
+size_t sweep_group_bytes_f64(int PA, int tpv);
 
-template <typename real>
-__host__ __device__ inline size_t sweep_group_bytes(int PA, int TPV) {
-    size_t nw = (size_t)TPV / 32;
-    size_t b = 128;                                    // RING+2 mbarriers
-    b += (size_t)RING * 2 * PA * sizeof(real);         // staged rows
-    b += (size_t)2 * 2 * PA * sizeof(real);            // rows Nb+1, Nb+2 (periodic)
-    b += (size_t)2 * 2 * TPV * sizeof(real);           // first-cell dF per thread
-    b += (size_t)2 * nw * 3 * sizeof(real);            // warp aggregates
-    return (b + 127) / 128 * 128;
-}
-
-// CPT consecutive values from (shared or global) memory / to global memory
-template <typename real, int CPT> struct Vec;
-template <> struct Vec<float, 4> {
-    static __device__ __forceinline__ void ld(const float *p, float *o) {
-        float4 x = *reinterpret_cast<const float4 *>(p);
-        o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w;
-    }
-    static __device__ __forceinline__ void st(float *p, const float *o) {
-        *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
-    }
-};
-template <> struct Vec<float, 2> {
-    static __device__ __forceinline__ void ld(const float *p, float *o) {
-        float2 x = *reinterpret_cast<const float2 *>(p);
-        o[0] = x.x; o[1] = x.y;
-    }
-    static __device__ __forceinline__ void st(float *p, const float *o) {
-        *reinterpret_cast<float2 *>(p) = make_float2(o[0], o[1]);
-    }
-};
-template <> struct Vec<double, 4> {
-    static __device__ __forceinline__ void ld(const double *p, double *o) {
-        double2 x = *reinterpret_cast<const double2 *>(p), y = *reinterpret_cast<const double2 *>(p + 2);
-        o[0] = x.x; o[1] = x.y; o[2] = y.x; o[3] = y.y;
-    }
-    static __device__ __forceinline__ void st(double *p, const double *o) {
-        *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
-        *reinterpret_cast<double2 *>(p + 2) = make_double2(o[2], o[3]);
-    }
-};
-template <> struct Vec<double, 2> {
-    static __device__ __forceinline__ void ld(const double *p, double *o) {
-        double2 x = *reinterpret_cast<const double2 *>(p);
-        o[0] = x.x; o[1] = x.y;
-    }
-    static __device__ __forceinline__ void st(double *p, const double *o) {
-        *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
-    }
-};
-template <typename real> struct Vec<real, 1> {
-    static __device__ __forceinline__ void ld(const real *p, real *o) { o[0] = *p; }
-    static __device__ __forceinline__ void st(real *p, const real *o) { *p = o[0]; }
-};
-
-template <typename real, int CPT, bool UNI, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_sweep(KinArgs<real> A) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int PA = A.PA, Na = A.Na, Nb = A.Nb;
-    const int TPV = PA / CPT;
-    const int g = threadIdx.y, t = threadIdx.x;
-    const int a0 = t * CPT + 1;                  // first cell of this thread
-    const int lane = t & 31, warp = t >> 5;
-    const int v = blockIdx.x * blockDim.y + g;
-    const bool vok = v < A.nv;
-    const bool act = vok && (a0 <= Na);          // chunks are all-in or all-out
-    const bool producer = (t == 0) && vok;
-    const int scheme = A.scheme;
-
-    unsigned char *base = smem_raw + (size_t)g * sweep_group_bytes<real>(PA, TPV);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base);
-    real *ring = reinterpret_cast<real *>(base + 128);
-    real *wrap = ring + (size_t)RING * 2 * PA;
-    real *dlf = wrap + (size_t)2 * 2 * PA;       // [2][2][TPV]
-    real *agg = dlf + (size_t)2 * 2 * TPV;       // [2][nw][3]
-    const int nw = TPV >> 5;
-
-    const bool perB = (A.bcb_lo == AX_PERIODIC);
-    const bool perA = (A.bca_lo == AX_PERIODIC);
-    const size_t vrow0 = vok ? (size_t)v * 2 * Nb * PA : 0;
-    const size_t rstride = (size_t)Nb * PA;
-    const uint32_t row_bytes = (uint32_t)(PA * sizeof(real));
-
-    auto phys_row = [&](int bp) -> int {
-        if (bp >= 1 && bp <= Nb) return bp;
-        if (perB && bp <= 0) return bp + Nb;
-        return 0;
-    };
-    auto issue_row = [&](int bp) {
-        int s = (bp + 1) % RING;
-        int pr = phys_row(bp);
-        if (pr > 0 && bp <= Nb) {
-            mbar_arrive_expect_tx(&bars[s], 2 * row_bytes);
-            const real *src = A.f + vrow0 + (size_t)(pr - 1) * PA;
-            bulk_g2s(ring + (size_t)s * 2 * PA, src, row_bytes, &bars[s]);
-            bulk_g2s(ring + (size_t)s * 2 * PA + PA, src + rstride, row_bytes, &bars[s]);
-        } else {
-            mbar_arrive(&bars[s]);                // keeps the slot's phase count
-        }
-    };
-    if (producer) {
-        for (int s = 0; s < RING + 2; s++) mbar_init(&bars[s], 1);
-        fence_async_shared();
-    }
-    __syncthreads();
-    if (producer) {
-        // rows -1 .. RING-3 fill slots 0 .. RING-2; step b refills the slot of
-        // row b-3 with row b+RING-3
-        for (int bp = -1; bp <= RING - 3; bp++) issue_row(bp);
-        if (perB) {
-            for (int w = 0; w < 2; w++) {
-                mbar_arrive_expect_tx(&bars[RING + w], 2 * row_bytes);
-                const real *src = A.f + vrow0 + (size_t)w * PA;
-                bulk_g2s(wrap + (size_t)w * 2 * PA, src, row_bytes, &bars[RING + w]);
-                bulk_g2s(wrap + (size_t)w * 2 * PA + PA, src + rstride, row_bytes, &bars[RING + w]);
-            }
-        }
-    }
-    auto rowp = [&](int bp, int r) -> const real * {
-        if (bp > Nb) return wrap + (size_t)(bp - Nb - 1) * 2 * PA + (size_t)r * PA;
-        return ring + (size_t)((bp + 1) % RING) * 2 * PA + (size_t)r * PA;
-    };
-    bool timeout = false;
-    auto wait_row = [&](int bp) {
-        if (!vok) return;
-        if (bp > Nb) {
-            if (perB && !mbar_wait_bounded(&bars[RING + (bp - Nb - 1)], 0)) timeout = true;
-            return;
-        }
-        if (phys_row(bp) == 0) return;
-        if (!mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1))) timeout = true;
-    };
-    // scan-axis cell c (1-based, may be outside 1..Na) of a staged row
-    auto cellA = [&](const real *row, int c) -> real {
-        if (perA) c = ((c - 1 + 2 * Na) % Na) + 1;
-        else c = c < 1 ? 1 : (c > Na ? Na : c);
-        return row[c - 1];
-    };
-
-    // ---- velocity and geometry ----------------------------------------------
-    const int iv = vok ? v % A.nvi : 0, jv = vok ? v / A.nvi : 0;
-    const real vx = vok ? (real)A.vx[iv] : real(0), vy = vok ? (real)A.vy[jv] : real(0);
-    const real dt = A.dt;
-    const int PA1 = PA + 1;
-    real sA_u = 0, sB_u = 0, vol_u = 1, ivol_u = 1, abase_u = 0;
-    if (UNI) {
-        sA_u = vx * A.gA1[0] + vy * A.gA2[0];
-        sB_u = vx * A.gB1[0] + vy * A.gB2[0];
-        vol_u = A.vol[0];
-        ivol_u = real(1) / vol_u;
-        abase_u = vol_u / dt + (posp(sA_u) - negp(sA_u) + posp(sB_u) - negp(sB_u));
-    }
-    auto speedA = [&](int q, int b) -> real {       // scan face q at row b
-        if (UNI) return sA_u;
-        size_t k = (size_t)(b - 1) * PA1 + (q - 1);
-        return vx * A.gA1[k] + vy * A.gA2[k];
-    };
-    auto speedB = [&](int q, int a) -> real {       // march face q at cell a
-        if (UNI) return sB_u;
-        size_t k = (size_t)(q - 1) * PA + (a - 1);
-        return vx * A.gB1[k] + vy * A.gB2[k];
-    };
-    // march-axis face flux at face q for cell a (component r)
-    auto fluxB = [&](int q, int a, int r, real sp) -> real {
-        if (!perB) {
-            if (q == 1) return sp * A.fw_blo[((size_t)v * 2 + r) * PA + (a - 1)];
-            if (q == Nb + 1) return sp * A.fw_bhi[((size_t)v * 2 + r) * PA + (a - 1)];
-            if (q == 2) return face_flux_wall_lo_s(scheme, sp, rowp(1, r)[a - 1], rowp(2, r)[a - 1], rowp(3, r)[a - 1]);
-            if (q == Nb)
-                return face_flux_wall_hi_s(scheme, sp, rowp(Nb, r)[a - 1], rowp(Nb - 1, r)[a - 1],
-                                           rowp(Nb - 2, r)[a - 1]);
-        }
-        return face_flux_s(scheme, sp, rowp(q - 2, r)[a - 1], rowp(q - 1, r)[a - 1], rowp(q, r)[a - 1],
-                           rowp(q + 1, r)[a - 1]);
-    };
-
-    // ---- carried state per cell ------------------------------------------------
-    real dG[CPT], dH[CPT];                 // forward values of the previous row
-    real iap[CPT];                         // 1/alpha of the previous row
-    real sAhp[CPT];                        // scan speed of face a+1, previous row
-    real sBl[CPT];                         // march speed of face b (low face)
-    real FBl_G[CPT], FBl_H[CPT];           // march flux through face b
-#pragma unroll
-    for (int k = 0; k < CPT; k++) {
-        dG[k] = dH[k] = real(0);
-        iap[k] = real(1);
-        sAhp[k] = sBl[k] = FBl_G[k] = FBl_H[k] = real(0);
-    }
-    const real fl = Consts<real>::floor_();
-    const real *ep = A.eqp;
-    const size_t ncell = (size_t)Nb * PA;
-
-    for (int bp = -1; bp <= 2; bp++) wait_row(bp);
-    if (act) {
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            sBl[k] = speedB(1, a0 + k);
-            FBl_G[k] = fluxB(1, a0 + k, 0, sBl[k]);
-            FBl_H[k] = fluxB(1, a0 + k, 1, sBl[k]);
-        }
-    }
-
-    for (int b = 1; b <= Nb; b++) {
-        wait_row(b + 2);
-        if (__syncthreads_or(timeout)) {
-            if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
-            return;
-        }
-        real pc[CPT], cG[CPT], cH[CPT], ia[CPT], sAh[CPT], sBh[CPT], FBh_G[CPT], FBh_H[CPT];
-        real fo0[CPT], fo1[CPT];           // f of row b-1 (for the backward update)
-        real P = real(1), CGt = real(0), CHt = real(0);
-        if (act) {
-            const real *r0 = rowp(b, 0), *r1 = rowp(b, 1);
-            real f0[CPT], f1[CPT];
-            Vec<real, CPT>::ld(r0 + (a0 - 1), f0);
-            Vec<real, CPT>::ld(r1 + (a0 - 1), f1);
-            // scan-axis window f(a0-2 .. a0+CPT+1)
-            real w0[CPT + 4], w1[CPT + 4];
-            w0[0] = cellA(r0, a0 - 2); w0[1] = cellA(r0, a0 - 1);
-            w1[0] = cellA(r1, a0 - 2); w1[1] = cellA(r1, a0 - 1);
-#pragma unroll
-            for (int k = 0; k < CPT; k++) { w0[k + 2] = f0[k]; w1[k + 2] = f1[k]; }
-            w0[CPT + 2] = cellA(r0, a0 + CPT); w0[CPT + 3] = cellA(r0, a0 + CPT + 1);
-            w1[CPT + 2] = cellA(r1, a0 + CPT); w1[CPT + 3] = cellA(r1, a0 + CPT + 1);
-            // scan-axis face fluxes, faces a0 .. a0+CPT
-            real FA_G[CPT + 1], FA_H[CPT + 1], sAf[CPT + 1];
-#pragma unroll
-            for (int m = 0; m <= CPT; m++) {
-                const int q = a0 + m;
-                const real s = speedA(q, b);
-                sAf[m] = s;
-                if (!perA && q == 1) {
-                    FA_G[m] = s * A.fw_alo[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[m] = s * A.fw_alo[((size_t)v * 2 + 1) * Nb + (b - 1)];
-                } else if (!perA && q == Na + 1) {
-                    FA_G[m] = s * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[m] = s * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
-                } else if (!perA && q == 2) {
-                    FA_G[m] = face_flux_wall_lo_s(scheme, s, r0[0], r0[1], r0[2]);
-                    FA_H[m] = face_flux_wall_lo_s(scheme, s, r1[0], r1[1], r1[2]);
-                } else if (!perA && q == Na) {
-                    FA_G[m] = face_flux_wall_hi_s(scheme, s, r0[Na - 1], r0[Na - 2], r0[Na - 3]);
-                    FA_H[m] = face_flux_wall_hi_s(scheme, s, r1[Na - 1], r1[Na - 2], r1[Na - 3]);
-                } else {
-                    FA_G[m] = face_flux_s(scheme, s, w0[m], w0[m + 1], w0[m + 2], w0[m + 3]);
-                    FA_H[m] = face_flux_s(scheme, s, w1[m], w1[m + 1], w1[m + 2], w1[m + 3]);
-                }
-            }
-            // rows b-1, b+1, b+2 at the thread's cells for the march faces
-            real m0[CPT], m1[CPT], p0[CPT], p1[CPT], q0[CPT], q1[CPT];
-            Vec<real, CPT>::ld(rowp(b - 1, 0) + (a0 - 1), m0);
-            Vec<real, CPT>::ld(rowp(b - 1, 1) + (a0 - 1), m1);
-            const bool stdB = perB || (b + 1 >= 3 && b + 1 <= Nb - 1);
-            if (stdB) {
-                Vec<real, CPT>::ld(rowp(b + 1, 0) + (a0 - 1), p0);
-                Vec<real, CPT>::ld(rowp(b + 1, 1) + (a0 - 1), p1);
-                Vec<real, CPT>::ld(rowp(b + 2, 0) + (a0 - 1), q0);
-                Vec<real, CPT>::ld(rowp(b + 2, 1) + (a0 - 1), q1);
-            }
-            // Shakhov parameters of the thread's cells
-            const size_t cell0 = (size_t)(b - 1) * PA + (a0 - 1);
-            real e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT], vl[CPT];
-            Vec<real, CPT>::ld(ep + 0 * ncell + cell0, e_crt);
-            Vec<real, CPT>::ld(ep + 1 * ncell + cell0, e_u);
-            Vec<real, CPT>::ld(ep + 2 * ncell + cell0, e_v);
-            Vec<real, CPT>::ld(ep + 3 * ncell + cell0, e_it);
-            Vec<real, CPT>::ld(ep + 4 * ncell + cell0, e_ht);
-            Vec<real, CPT>::ld(ep + 5 * ncell + cell0, e_qx);
-            Vec<real, CPT>::ld(ep + 6 * ncell + cell0, e_qy);
-            Vec<real, CPT>::ld(ep + 7 * ncell + cell0, e_cf);
-            if (!UNI) Vec<real, CPT>::ld(A.vol + cell0, vl);
-            real rG[CPT], rH[CPT];
-#pragma unroll
-            for (int k = 0; k < CPT; k++) {
-                const int a = a0 + k;
-                fo0[k] = m0[k];
-                fo1[k] = m1[k];
-                sBh[k] = speedB(b + 1, a);
-                if (stdB) {
-                    FBh_G[k] = face_flux_s(scheme, sBh[k], m0[k], f0[k], p0[k], q0[k]);
-                    FBh_H[k] = face_flux_s(scheme, sBh[k], m1[k], f1[k], p1[k], q1[k]);
-                } else {
-                    FBh_G[k] = fluxB(b + 1, a, 0, sBh[k]);
-                    FBh_H[k] = fluxB(b + 1, a, 1, sBh[k]);
-                }
-                real divG, divH;
-                if (A.scan_is_j) {
-                    divG = (FBh_G[k] - FBl_G[k]) + FA_G[k + 1] - FA_G[k];
-                    divH = (FBh_H[k] - FBl_H[k]) + FA_H[k + 1] - FA_H[k];
-                } else {
-                    divG = (FA_G[k + 1] - FA_G[k]) + FBh_G[k] - FBl_G[k];
-                    divH = (FA_H[k + 1] - FA_H[k]) + FBh_H[k] - FBl_H[k];
-                }
-                // Shakhov equilibrium (GKUA_Residual.f90:441-458)
-                const real viu = vx - e_u[k], vjv = vy - e_v[k];
-                const real vij2 = (viu * viu + vjv * vjv) * e_it[k];
-                const real fvx = e_qx[k] * viu + e_qy[k] * vjv;
-                const real gdv = e_crt[k] * dexp<real>(-vij2);
-                const real geq = gdv * (real(1) + fvx * (real(2) * vij2 - real(4)));
-                const real heq = (e_ht[k] * gdv) * (real(1) + fvx * (real(2) * vij2 - real(2)));
-                const real vol = UNI ? vol_u : vl[k];
-                const real ivol = UNI ? ivol_u : real(1) / vol;
-                rG[k] = -divG * ivol + e_cf[k] * (geq - f0[k]);
-                rH[k] = -divH * ivol + e_cf[k] * (heq - f1[k]);
-                // LU-SGS forward element (GKUA_Residual.f90:39-57)
-                real alfa;
-                if (UNI) alfa = abase_u + vol * e_cf[k];
-                else
-                    alfa = vol / dt + (posp(sAf[k + 1]) - negp(sAf[k]) + posp(sBh[k]) - negp(sBl[k])) +
-                           vol * e_cf[k];
-                ia[k] = real(1) / alfa;
-                pc[k] = posp(sAf[k]) * ia[k];
-                const real pb = posp(sBl[k]);
-                cG[k] = (vol * rG[k] + pb * dG[k]) * ia[k];
-                cH[k] = (vol * rH[k] + pb * dH[k]) * ia[k];
-                sAh[k] = sAf[k + 1];
-                // thread-local composition of the affine maps
-                CGt = cG[k] + pc[k] * CGt;
-                CHt = cH[k] + pc[k] * CHt;
-                P = pc[k] * P;
-            }
-            if (A.rhs) {
-                Vec<real, CPT>::st(A.rhs + vrow0 + cell0, rG);
-                Vec<real, CPT>::st(A.rhs + vrow0 + rstride + cell0, rH);
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < CPT; k++) {
-                pc[k] = cG[k] = cH[k] = ia[k] = sAh[k] = sBh[k] = FBh_G[k] = FBh_H[k] = fo0[k] = fo1[k] = real(0);
-            }
-            P = real(0);
-        }
-        // inclusive warp scan of the composed maps (earlier lanes first)
-        real Pi = P, Gi = CGt, Hi = CHt;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            real pu = __shfl_up_sync(0xffffffffu, Pi, off);
-            real gu = __shfl_up_sync(0xffffffffu, Gi, off);
-            real hu = __shfl_up_sync(0xffffffffu, Hi, off);
-            if (lane >= off) {
-                Gi = Gi + Pi * gu;
-                Hi = Hi + Pi * hu;
-                Pi = Pi * pu;
-            }
-        }
-        // exclusive prefix of this lane
-        real Pe = __shfl_up_sync(0xffffffffu, Pi, 1), Ge = __shfl_up_sync(0xffffffffu, Gi, 1),
-             He = __shfl_up_sync(0xffffffffu, Hi, 1);
-        if (lane == 0) { Pe = real(1); Ge = real(0); He = real(0); }
-        real *aggb = agg + (size_t)(b & 1) * nw * 3;
-        if (lane == 31) {
-            aggb[warp * 3 + 0] = Pi;
-            aggb[warp * 3 + 1] = Gi;
-            aggb[warp * 3 + 2] = Hi;
-        }
-        __syncthreads();
-        if (producer) issue_row(b + RING - 3);
-        real carG = real(0), carH = real(0);
-        for (int w = 0; w < warp; w++) {
-            const real pw = aggb[w * 3 + 0];
-            carG = aggb[w * 3 + 1] + pw * carG;
-            carH = aggb[w * 3 + 2] + pw * carH;
-        }
-        real xG = Ge + Pe * carG, xH = He + Pe * carH;   // dF just before cell a0
-        real nG[CPT], nH[CPT];
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            xG = cG[k] + pc[k] * xG;
-            xH = cH[k] + pc[k] * xH;
-            nG[k] = xG;
-            nH[k] = xH;
-        }
-        real *dlb = dlf + (size_t)(b & 1) * 2 * TPV;
-        dlb[t] = act ? nG[0] : real(0);
-        dlb[TPV + t] = act ? nH[0] : real(0);
-        // backward + update of row b-1 (GKUA_Residual.f90:64-109)
-        if (b > 1 && act) {
-            const real *dlp = dlf + (size_t)((b - 1) & 1) * 2 * TPV;
-            const bool has_next = (a0 + CPT <= Na);
-            real uG[CPT], uH[CPT];
-#pragma unroll
-            for (int k = 0; k < CPT; k++) {
-                const real nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : real(0));
-                const real nxH = (k + 1 < CPT) ? dH[k + 1] : (has_next ? dlp[TPV + t + 1] : real(0));
-                const real ca = -negp(sAhp[k]);
-                const real cb = -negp(sBl[k]);
-                real fg = fo0[k] + (dG[k] + (ca * nxG + cb * nG[k]) * iap[k]);
-                real fh = fo1[k] + (dH[k] + (ca * nxH + cb * nH[k]) * iap[k]);
-                uG[k] = fg < fl ? fl : fg;
-                uH[k] = fh < fl ? fl : fh;
-            }
-            const size_t c1 = (size_t)(b - 2) * PA + (a0 - 1);
-            Vec<real, CPT>::st(A.f + vrow0 + c1, uG);
-            Vec<real, CPT>::st(A.f + vrow0 + rstride + c1, uH);
-        }
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            dG[k] = nG[k];
-            dH[k] = nH[k];
-            iap[k] = ia[k];
-            sAhp[k] = sAh[k];
-            sBl[k] = sBh[k];
-            FBl_G[k] = FBh_G[k];
-            FBl_H[k] = FBh_H[k];
-        }
-    }
-    __syncthreads();
-    if (act) {   // backward + update of the last row (downstream values are 0)
-        const real *dlp = dlf + (size_t)(Nb & 1) * 2 * TPV;
-        const bool has_next = (a0 + CPT <= Na);
-        const real *o0 = rowp(Nb, 0) + (a0 - 1), *o1 = rowp(Nb, 1) + (a0 - 1);
-        real f0[CPT], f1[CPT], uG[CPT], uH[CPT];
-        Vec<real, CPT>::ld(o0, f0);
-        Vec<real, CPT>::ld(o1, f1);
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            const real nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : real(0));
-            const real nxH = (k + 1 < CPT) ? dH[k + 1] : (has_next ? dlp[TPV + t + 1] : real(0));
-            const real ca = -negp(sAhp[k]);
-            real fg = f0[k] + (dG[k] + (ca * nxG) * iap[k]);
-            real fh = f1[k] + (dH[k] + (ca * nxH) * iap[k]);
-            uG[k] = fg < fl ? fl : fg;
-            uH[k] = fh < fl ? fl : fh;
-        }
-        const size_t c1 = (size_t)(Nb - 1) * PA + (a0 - 1);
-        Vec<real, CPT>::st(A.f + vrow0 + c1, uG);
-        Vec<real, CPT>::st(A.f + vrow0 + rstride + c1, uH);
-    }
-    // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
-    // for above, so no copy is in flight when the CTA exits
-}
-
-static int check_err(hyb_ctx *ctx, const char *what) {
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
-        return HYB_ERR_CUDA;
-    }
-    return HYB_OK;
-}
-
-// Launch shape of the sweep: cells per thread (cpt), velocity groups per CTA
-// (vpb) and the minimum resident CTAs per SM the registers are sized for
-// (minb).  hyb_autotune picks it by timing; HYB_SWEEP_SHAPE="cpt,vpb,minb"
-// overrides it.
-static void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb, int *minb) {
-    *cpt = ctx->sw_cpt > 0 ? ctx->sw_cpt : ctx->cpt;
-    int tpv = ctx->PA / *cpt;
+// Launch shape: cells per thread (cpt, dividing the context's layout chunk)
+// and velocity groups per CTA (vpb, CTAs of at most 256 threads).  The
+// autotuner sets ctx->sw_cpt / sw_vpb by timing; HYB_SWEEP_SHAPE="cpt,vpb,0"
+// overrides them at context creation.
+void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb) {
+    int c = ctx->sw_cpt > 0 ? ctx->sw_cpt : ctx->cpt;
+    if (ctx->cpt % c != 0 || ctx->PA / c > 256) c = ctx->cpt;
+    int tpv = ctx->PA / c;
     int v = ctx->sw_vpb > 0 ? ctx->sw_vpb : 256 / tpv;
     if (v < 1) v = 1;
     while (v > 1 && tpv * v > 256) v--;
+    *cpt = c;
     *vpb = v;
-    *minb = ctx->sw_minb > 0 ? ctx->sw_minb : 1;
 }
 
 size_t sweep_smem_bytes(const hyb_ctx *ctx) {
-    int cpt, vpb, minb;
-    sweep_shape(ctx, &cpt, &vpb, &minb);
+    int cpt, vpb;
+    sweep_shape(ctx, &cpt, &vpb);
     int tpv = ctx->PA / cpt;
-    size_t g = ctx->precision == HYB_PREC_FP64 ? sweep_group_bytes<double>(ctx->PA, tpv)
-                                               : sweep_group_bytes<float>(ctx->PA, tpv);
+    size_t g = ctx->precision == HYB_PREC_FP64 ? sweep_group_bytes_f64(ctx->PA, tpv)
+                                               : sweep_group_bytes_f32(ctx->PA, tpv);
     return g * vpb;
 }
 
-template <typename real, int CPT, bool UNI, int MINB>
-static int launch_t(hyb_ctx *ctx, const KinArgs<real> &A, int vpb) {
-    const int tpv = ctx->PA / CPT;
-    const size_t smem = sweep_group_bytes<real>(ctx->PA, tpv) * vpb;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sweep<real, CPT, UNI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             227 * 1024);
-        attr = true;
-    }
-    dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
-    k_sweep<real, CPT, UNI, MINB><<<grd, blk, smem, ctx->stream>>>(A);
-    ctx->launches++;
-    return check_err(ctx, "k_sweep");
-}
-
-template <typename real, int CPT, bool UNI>
-static int launch_m(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, int minb) {
-    if (minb >= 2) return launch_t<real, CPT, UNI, 2>(ctx, A, vpb);
-    return launch_t<real, CPT, UNI, 1>(ctx, A, vpb);
-}
-
 template <typename real>
-static int launch_sweep_t(hyb_ctx *ctx, int store_rhs) {
-    KinArgs<real> A;
+static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.f = (real *)ctx->d_f;
     A.rhs = store_rhs ? (real *)ctx->d_rhs : nullptr;
     A.fw_alo = A.fw_ahi = A.fw_blo = A.fw_bhi = nullptr;
@@ -552,19 +72,19 @@ static int launch_sweep_t(hyb_ctx *ctx, int store_rhs) {
     A.scan_is_j = ctx->scan_is_j;
     A.dt = (real)ctx->prm.dt;
     A.err = ctx->d_err;
-    const bool uni = ctx->uniform != 0;
-    int cpt, vpb, minb;
-    sweep_shape(ctx, &cpt, &vpb, &minb);
-    switch (cpt) {
-        case 4: return uni ? launch_m<real, 4, true>(ctx, A, vpb, minb) : launch_m<real, 4, false>(ctx, A, vpb, minb);
-        case 2: return uni ? launch_m<real, 2, true>(ctx, A, vpb, minb) : launch_m<real, 2, false>(ctx, A, vpb, minb);
-        default: return uni ? launch_m<real, 1, true>(ctx, A, vpb, minb) : launch_m<real, 1, false>(ctx, A, vpb, minb);
-    }
 }
 
 int launch_sweep(hyb_ctx *ctx, int store_rhs) {
-    if (ctx->precision == HYB_PREC_FP64) return launch_sweep_t<double>(ctx, store_rhs);
-    return launch_sweep_t<float>(ctx, store_rhs);
+    int cpt, vpb;
+    sweep_shape(ctx, &cpt, &vpb);
+    if (ctx->precision == HYB_PREC_FP64) {
+        KinArgs<double> A;
+        fill_args<double>(ctx, store_rhs, A);
+        return sweep_launch_f64(ctx, A, cpt, vpb);
+    }
+    KinArgs<float> A;
+    fill_args<float>(ctx, store_rhs, A);
+    return sweep_launch_f32(ctx, A, cpt, vpb);
 }
 
 }  // namespace hyb
