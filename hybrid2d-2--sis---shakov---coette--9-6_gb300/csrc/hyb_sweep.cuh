@@ -95,8 +95,11 @@ __device__ __forceinline__ real flux_std(real s, real u1, real u2, real u3, real
     if constexpr (SCHEME == HYB_SCHEME_UP1) {
         return s > real(0) ? s * u2 : s * u3;
     } else if constexpr (SCHEME == HYB_SCHEME_NND) {
-        const real d0 = u3 - u2;
-        return s > real(0) ? s * (u2 + real(0.5) * fminmd(d0, u2 - u1)) : s * (u3 - real(0.5) * fminmd(d0, u4 - u3));
+        // UR(u1,u2,u3,u4) = UL(u4,u3,u2,u1) because FMINMD(-x,-y) = -FMINMD(x,y)
+        // exactly, so one limiter on mirrored inputs gives the upwind value
+        const bool up = s > real(0);
+        const real x1 = up ? u1 : u4, x2 = up ? u2 : u3, x3 = up ? u3 : u2;
+        return s * (x2 + real(0.5) * fminmd(x3 - x2, x2 - x1));
     } else {
         return face_flux(HYB_SCHEME_WENO3, posp(s), negp(s), u1, u2, u3, u4);
     }
