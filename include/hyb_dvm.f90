@@ -1,0 +1,164 @@
+! hyb_dvm.f90 -- ISO_C_BINDING interface to the C ABI in hyb_dvm.h.
+!
+! The Fortran host of Hybrid2D keeps its mesh, input and restart handling and
+! calls the GB300 kinetic solver through these interfaces; every function
+! returns the int status of the C side (0 = ok, negative = HYB_ERR_*).
+module hyb_dvm
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: HYB_OK = 0, HYB_ERR_INVALID = -1, HYB_ERR_NOMEM = -2, &
+       HYB_ERR_CUDA = -3, HYB_ERR_NONFINITE = -4, HYB_ERR_TIMEOUT = -5, &
+       HYB_ERR_UNSUPPORTED = -6, HYB_ERR_TEMPERATURE = -7, HYB_ERR_NODEVICE = -8
+  integer(c_int), parameter :: HYB_BC_WALL = -2, HYB_BC_PERIODIC = 1
+  integer(c_int), parameter :: HYB_SCHEME_UP1 = 0, HYB_SCHEME_NND = 1, HYB_SCHEME_WENO3 = 3
+  integer(c_int), parameter :: HYB_PREC_FP64 = 0, HYB_PREC_MIXED = 1
+  integer(c_int), parameter :: HYB_NSUM = 11, HYB_NRD = 2
+
+  type, bind(c) :: hyb_mesh
+     integer(c_int) :: nx, ny
+     type(c_ptr)    :: x, y
+     integer(c_int) :: bc(4)
+     type(c_ptr)    :: wall_u(4), wall_v(4), wall_t(4)
+  end type hyb_mesh
+
+  type, bind(c) :: hyb_vgrid
+     integer(c_int) :: nvi, nvj
+     type(c_ptr)    :: vi, vj, wi, wj
+  end type hyb_vgrid
+
+  type, bind(c) :: hyb_params
+     real(c_double) :: dt, cfc, cpr, x1s, r00, t00
+     integer(c_int) :: scheme, precision
+     real(c_double) :: gamma, ma, pr, re, omega_ns
+     integer(c_int) :: device
+     integer(c_int) :: reserved(7)
+  end type hyb_params
+
+  type, bind(c) :: hyb_residual
+     real(c_double) :: res_max(4), res_rms(4), max_rms
+  end type hyb_residual
+
+  type, bind(c) :: hyb_gsis_params
+     integer(c_int) :: enable, max_inner
+     real(c_double) :: inner_tol, cfl, dtmax, dtmin
+     integer(c_int) :: flux, ns_scheme, use_mlp
+     integer(c_int) :: reserved(5)
+  end type hyb_gsis_params
+
+  interface
+     integer(c_int) function hyb_create(mesh, vgrid, params, ctx) bind(c, name="hyb_create")
+       import :: c_int, c_ptr, hyb_mesh, hyb_vgrid, hyb_params
+       type(hyb_mesh), intent(in) :: mesh
+       type(hyb_vgrid), intent(in) :: vgrid
+       type(hyb_params), intent(in) :: params
+       type(c_ptr), intent(out) :: ctx
+     end function
+     integer(c_int) function hyb_destroy(ctx) bind(c, name="hyb_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     type(c_ptr) function hyb_last_error(ctx) bind(c, name="hyb_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     type(c_ptr) function hyb_version() bind(c, name="hyb_version")
+       import :: c_ptr
+     end function
+     integer(c_int) function hyb_init_maxwellian(ctx, rho, u, v, t) bind(c, name="hyb_init_maxwellian")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: rho, u, v, t
+     end function
+     integer(c_int) function hyb_upload_f(ctx, frd) bind(c, name="hyb_upload_f")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: frd(*)
+     end function
+     integer(c_int) function hyb_download_f(ctx, frd) bind(c, name="hyb_download_f")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: frd(*)
+     end function
+     integer(c_int) function hyb_download_moments(ctx, s_gkua, cf) bind(c, name="hyb_download_moments")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: s_gkua(*), cf(*)
+     end function
+     integer(c_int) function hyb_download_hot(ctx, tao_i, q_i, tao_j, q_j) bind(c, name="hyb_download_hot")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: tao_i(*), q_i(*), tao_j(*), q_j(*)
+     end function
+     integer(c_int) function hyb_step(ctx, n_iter, res) bind(c, name="hyb_step")
+       import :: c_int, c_ptr, hyb_residual
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: n_iter
+       type(hyb_residual), intent(out) :: res
+     end function
+     integer(c_int) function hyb_phy_boundary(ctx) bind(c, name="hyb_phy_boundary")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function hyb_kinetic_step(ctx) bind(c, name="hyb_kinetic_step")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function hyb_detfp(ctx) bind(c, name="hyb_detfp")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function hyb_convert_ns(ctx) bind(c, name="hyb_convert_ns")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function hyb_detfp_res(ctx, res) bind(c, name="hyb_detfp_res")
+       import :: c_int, c_ptr, hyb_residual
+       type(c_ptr), value :: ctx
+       type(hyb_residual), intent(out) :: res
+     end function
+     integer(c_int) function hyb_gsis_configure(ctx, gp) bind(c, name="hyb_gsis_configure")
+       import :: c_int, c_ptr, hyb_gsis_params
+       type(c_ptr), value :: ctx
+       type(hyb_gsis_params), intent(in) :: gp
+     end function
+     integer(c_int) function hyb_gsis_last_inner(ctx, n_inner) bind(c, name="hyb_gsis_last_inner")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), intent(out) :: n_inner
+     end function
+     integer(c_int) function hyb_set_walls(ctx, face, wall_u, wall_v, wall_t) bind(c, name="hyb_set_walls")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: face
+       real(c_double), intent(in) :: wall_u(*), wall_v(*), wall_t(*)
+     end function
+     integer(c_int) function hyb_profile_enable(ctx, enable) bind(c, name="hyb_profile_enable")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: enable
+     end function
+     integer(c_int) function hyb_profile_read(ctx, ms, launches, n) bind(c, name="hyb_profile_read")
+       import :: c_int, c_ptr, c_double, c_long_long
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: ms(*)
+       integer(c_long_long), intent(out) :: launches(*)
+       integer(c_int), value :: n
+     end function
+     integer(c_int) function hyb_launch_count(ctx, count) bind(c, name="hyb_launch_count")
+       import :: c_int, c_ptr, c_long_long
+       type(c_ptr), value :: ctx
+       integer(c_long_long), intent(out) :: count
+     end function
+     integer(c_int) function hyb_last_step_ms(ctx, ms) bind(c, name="hyb_last_step_ms")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: ms
+     end function
+     integer(c_int) function hyb_stream(ctx, stream) bind(c, name="hyb_stream")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       type(c_ptr), intent(out) :: stream
+     end function
+  end interface
+end module hyb_dvm
