@@ -20,7 +20,7 @@ EXPORTS = [
     "hyb_download_hot", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
     "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
     "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
-    "hyb_profile_enable", "hyb_profile_read",
+    "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc",
 ]
 STAGES = ["wall", "sweep", "moments", "sghost", "convert_ns", "gsis", "residual"]
 
@@ -65,6 +65,7 @@ def load(path=None):
     L.hyb_set_walls.argtypes = [vp, ip, dp, dp, dp]
     L.hyb_profile_enable.argtypes = [vp, ip]
     L.hyb_profile_read.argtypes = [vp, dp, C.POINTER(C.c_longlong), ip]
+    L.hyb_detfp_noalloc.argtypes = [ip, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -14,6 +14,7 @@ module hyb_dvm
   integer(c_int), parameter :: HYB_SCHEME_UP1 = 0, HYB_SCHEME_NND = 1, HYB_SCHEME_WENO3 = 3
   integer(c_int), parameter :: HYB_PREC_FP64 = 0, HYB_PREC_MIXED = 1
   integer(c_int), parameter :: HYB_NSUM = 11, HYB_NRD = 2
+  integer(c_int), parameter :: HYB_NOALLOC_MAX_CELLS = 209715
 
   type, bind(c) :: hyb_mesh
      integer(c_int) :: nx, ny
@@ -132,6 +133,13 @@ module hyb_dvm
        type(c_ptr), value :: ctx
        integer(c_int), value :: face
        real(c_double), intent(in) :: wall_u(*), wall_v(*), wall_t(*)
+     end function
+     integer(c_int) function hyb_detfp_noalloc(nx, ny, nvi, nvj, frd_dev, vi_dev, vj_dev, wi_dev, wj_dev, &
+          params, s_gkua_dev, cf_dev, stream) bind(c, name="hyb_detfp_noalloc")
+       import :: c_int, c_ptr, hyb_params
+       integer(c_int), value :: nx, ny, nvi, nvj
+       type(c_ptr), value :: frd_dev, vi_dev, vj_dev, wi_dev, wj_dev, s_gkua_dev, cf_dev, stream
+       type(hyb_params), intent(in) :: params
      end function
      integer(c_int) function hyb_profile_enable(ctx, enable) bind(c, name="hyb_profile_enable")
        import :: c_int, c_ptr

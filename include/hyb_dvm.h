@@ -186,6 +186,34 @@ int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner);
 int hyb_set_walls(hyb_ctx *ctx, int face, const double *wall_u,
                   const double *wall_v, const double *wall_t);
 
+/* ---- DETFP without device allocation -----------------------------------
+ * No counterpart in the reference.  For callers that cannot let this library
+ * allocate device memory: a CUDA Fortran / OpenACC host that already keeps
+ * FRD and S_GKUA as its own device arrays, or a process whose device memory
+ * is reserved by another framework's pooling allocator.  Computes DETFP's
+ * moments, primitive conversion and CF (GKUA_DETFP.f90:4-105) for the
+ * interior cells i=1..nx-1, j=1..ny-1 of a device-resident FRD and writes
+ * them into caller-owned device arrays; no context is needed and nothing is
+ * allocated (no cudaMalloc / cudaFree, no library allocation).
+ *   frd_dev     FRD(NRD,-3:nx+3,-3:ny+3,nvi,nvj), double, on the device
+ *   vi/vj_dev   velocity nodes, wi/wj_dev full 1-D weights (hyb_vgrid)
+ *   p           host struct; only cfc, x1s, r00, t00 are read
+ *   s_gkua_dev  S_GKUA(Nsum,-3:nx+3,-3:ny+3); interior cells are written
+ *   cf_dev      CF on the (1-LAP:nx+LAP-1, 1-LAP:ny+LAP-1) extents, or NULL
+ *   stream      cudaStream_t to launch on (NULL: default stream)
+ * Limits: at most HYB_NOALLOC_MAX_CELLS interior cells, else
+ * HYB_ERR_UNSUPPORTED.  Intermediate sums live in one fixed 16 MiB device
+ * array of the library, held by every device that loads the library until
+ * the process exits; the first call on a device looks up that array's
+ * address (make it before any stream capture).  Calls share the array, so
+ * calls that overlap on the GPU (e.g. on two streams) race. */
+#define HYB_NOALLOC_MAX_CELLS 209715
+int hyb_detfp_noalloc(int nx, int ny, int nvi, int nvj, const double *frd_dev,
+                      const double *vi_dev, const double *vj_dev,
+                      const double *wi_dev, const double *wj_dev,
+                      const hyb_params *p, double *s_gkua_dev, double *cf_dev,
+                      void *stream);
+
 /* ---- timing / introspection -------------------------------------------- */
 /* Per-stage device timing with CUDA events on the context's stream.  While
  * enabled, hyb_step brackets every stage (wall, sweep, moments, sghost,
