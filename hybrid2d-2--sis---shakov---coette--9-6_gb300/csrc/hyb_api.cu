@@ -152,7 +152,7 @@ void free_all(hyb_ctx *c) {
     F(c->d_f); F(c->d_rhs);
     for (int k = 0; k < 4; k++) F(c->d_fw[k]);
     F(c->d_eqp); F(c->d_vol); F(c->d_gA1); F(c->d_gA2); F(c->d_gB1); F(c->d_gB2);
-    F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_S0); F(c->d_CF); F(c->d_wall);
+    F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_CF); F(c->d_wall);
     F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err); F(c->d_mpart);
     if (c->h_resid) cudaFreeHost(c->h_resid);
     if (c->h_wall) cudaFreeHost(c->h_wall);
@@ -274,7 +274,6 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     if (rc == HYB_OK) ALLOC(c->d_w, c->nv * sizeof(double));
     const size_t nc2 = (size_t)(c->nx + 3) * (c->ny + 3);
     if (rc == HYB_OK) ALLOC(c->d_S, HYB_NSUM * nc2 * sizeof(double));
-    if (rc == HYB_OK) ALLOC(c->d_S0, HYB_NSUM * nc2 * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_CF, nc2 * sizeof(double));
     const int maxfc = std::max(ncx, ncy);
     if (rc == HYB_OK) ALLOC(c->d_wall, (size_t)4 * 6 * 4096 * sizeof(double));
@@ -520,15 +519,11 @@ extern "C" {
 int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
     if (!ctx || n_iter < 1) return HYB_ERR_INVALID;
     cudaSetDevice(ctx->dev);
-    const size_t nc2 = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
     size_t evi = 0;
     ctx->prof_stage.clear();
     HYB_CK(cudaEventRecord(ctx->ev0, ctx->stream));
     for (int it = 0; it < n_iter; it++) {
         const bool last = (it == n_iter - 1);
-        if (ctx->gsis.enable)
-            HYB_CK(cudaMemcpyAsync(ctx->d_S0, ctx->d_S, HYB_NSUM * nc2 * sizeof(double), cudaMemcpyDeviceToDevice,
-                                   ctx->stream));
         int rc = staged(ctx, ST_WALL, &evi, [&] { return hyb::launch_wall(ctx); });
         if (!rc) rc = staged(ctx, ST_SWEEP, &evi, [&] { return hyb::launch_sweep(ctx, last ? 1 : 0); });
         if (!rc) rc = staged(ctx, ST_MOM, &evi, [&] { return hyb::launch_moments(ctx); });
@@ -723,16 +718,3 @@ int hyb_stream(const hyb_ctx *ctx, void **stream) {
 }
 
 }  // extern "C"
-
-// GSIS solver entry points; the synthetic solve lives in hyb_gsis.cu
-namespace hyb {
-__attribute__((weak)) int ns_create(hyb_ctx *ctx) {
-    ctx->last_error = "GSIS synthetic solve not built";
-    return HYB_ERR_UNSUPPORTED;
-}
-__attribute__((weak)) void ns_destroy(hyb_ctx *) {}
-__attribute__((weak)) int gsis_solve(hyb_ctx *ctx) {
-    ctx->last_error = "GSIS synthetic solve not built";
-    return HYB_ERR_UNSUPPORTED;
-}
-}  // namespace hyb

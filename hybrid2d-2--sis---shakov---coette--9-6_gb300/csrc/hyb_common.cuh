@@ -46,6 +46,7 @@ template <typename real>
 struct KinArgs {
     real *f;              // [Nv][2][Nb][PA]
     real *rhs;            // optional RHS store (same layout) or nullptr
+    int no_update;         // 1: compute (and store) the RHS only, f is left as is
     const real *fw_alo, *fw_ahi;   // wall slots at the scan-axis ends [Nv][2][Nb]
     const real *fw_blo, *fw_bhi;   // wall slots at the march-axis ends [Nv][2][PA]
     const real *eqp;      // [8][Nb*PA]: crt, u, v, invT, hT, cqx, cqy, cf
@@ -90,10 +91,9 @@ struct hyb_ctx {
     int uniform;                           // Cartesian uniform spacing
 
     // device buffers
-    void *d_f, *d_rhs, *d_fw[4], *d_eqp, *d_vol, *d_gA1, *d_gA2, *d_gB1, *d_gB2;
+    void *d_f, *d_rhs, *d_rhs_gsis, *d_fw[4], *d_eqp, *d_vol, *d_gA1, *d_gA2, *d_gB1, *d_gB2;
     double *d_vx, *d_vy, *d_w;             // per-velocity nodes and weights
     double *d_S;                           // [NSUM][(nx+3)(ny+3)]
-    double *d_S0;
     double *d_CF;                          // [(nx+3)(ny+3)]
     double *d_wall;                        // per wall face: u, v, t, normal
     double *d_x1, *d_y1;
@@ -140,6 +140,7 @@ int launch_moments(hyb_ctx *ctx);
 int moments_slices(const hyb_ctx *ctx);
 int launch_sghost(hyb_ctx *ctx);
 int launch_residual(hyb_ctx *ctx, hyb_residual *out);
+int launch_rhs_moments(hyb_ctx *ctx, double *cellm);
 int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);
 int launch_convert_ns(hyb_ctx *ctx);
 int ns_create(hyb_ctx *ctx);

@@ -1,0 +1,770 @@
+// hyb_gsis.cu -- the GSIS synthetic macroscopic solve, FP64 on the GPU.
+//
+// The coupling of Hybrid_Time_advance_LU_SGS (Hybrid_Sub.f90:45-153, shipped
+// commented out) around the OpenCFD-EC NS solver, in the consistent form of
+// the oracle (oracle/hyb_oracle_ns.c):
+//   1. R_K: moments 1-4 of the kinetic RHS of the current f with its own
+//      equilibrium (an RHS-only pass of the sweep kernel, then the residual
+//      kernel's per-cell moments), in NS units vol*k*(1,k,k,k^2/2);
+//   2. U = U_k (Convert_NS state of the kinetic moments), Q = R_K - R_NS(U_k)
+//      on the band;
+//   3. NS_Time_advance_LU_SGS on R_NS(U) + Q until max|Res(4)| over the band
+//      < max(inner_tol, inner_rtol * first value) or max_inner iterations
+//      (sub_NS_singlegrid.f90:4-221, sub_Residual.f90, sub_flux_split.f90,
+//      sub_LU_SGS.f90);
+//   4. S(1:4) += NS change of rho, u, v, T (the density change with its
+//      volume mean over the band removed), S(5,6,7,10) += TaoNS_out,
+//      S(8,9) += Q_out (getNSF, Hybrid_Sub.f90:617-654); the Shakhov
+//      parameters of the next kinetic step are recomputed from the new S.
+// At a converged kinetic state R_K = 0 and the correction vanishes.  The band
+// is cells 3..n-3 along wall-bounded axes and all cells along a periodic
+// axis.  The LU-SGS algebra is the reference's (alpha, comput_DFn, spectral
+// radii) with a two-colour ordering instead of the anti-diagonal wavefront:
+// forward red then black, backward black then red, dU reset to 0 each inner
+// iteration.  Reconstruction NND2 on primitive variables, Van Leer splitting
+// (the shipped control.in choices).
+//
+// Inner iterations run in batches of NS_BATCH captured in a CUDA graph; a
+// device control block carries the running max residual, the iteration count
+// and a done flag that turns the rest of a batch into no-ops, so the host
+// reads the control block once per batch.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "hyb_common.cuh"
+
+namespace hyb {
+
+constexpr int NS_BATCH = 8;
+
+struct NsCtrl {
+    unsigned long long res_bits;   // max |Res(4)| of the current inner iteration (bit pattern)
+    int it;                        // inner iterations done
+    int done;                      // 1: converged or capped
+    int err;                       // HYB_ERR_TEMPERATURE / HYB_ERR_NONFINITE
+    int max_it;
+    double tol;                    // absolute stop; raised to rtol * first residual
+    double rtol;
+    double lam;                    // volume mean of the band's density change
+};
+
+struct NsDev {
+    int nx, ny, ilo, ihi, jlo, jhi, perx, pery;
+    size_t nc;
+    double gamma, ma, pr, re, omega, cv, cp, ptmp, cfl, dtmax, dtmin;
+    double *U, *U2, *dU, *Res, *dt, *Lci, *Lcj, *Lvi, *Lvj;
+    double *src;                                             // synthetic source Q [4][nc]
+    const double *rk;                                        // kinetic RHS moments [4][Nb*PA]
+    int src_on, PA, scan_is_j, mass_proj;
+    double *d, *uu, *vv, *T, *p, *cc, *amu;
+    double *fluxi, *fluxj, *ti_out, *qi_out, *tj_out, *qj_out;
+    const double *vol, *si, *sj, *ni1, *ni2, *nj1, *nj2;   // (nx,ny)
+    const double *x1, *y1;
+    const double *tg_i, *qg_i, *tg_j, *qg_j;                // HoT, SoA [c][nc]
+    const double *tin_i, *qin_i, *tin_j, *qin_j;            // NSF of the kinetic state
+    double *S;                                               // [NSUM][nc]
+    NsCtrl *ctrl;
+};
+
+struct NsState {
+    NsDev D;
+    double *buf;            // all state arrays
+    double *geo;            // vol, si, sj, ni1, ni2, nj1, nj2
+    NsCtrl *ctrl;
+    NsCtrl *h_ctrl;         // pinned
+    double *rk;             // [4][Nb*PA]
+    cudaGraphExec_t graph;
+    bool have_graph;
+};
+
+__device__ __forceinline__ size_t c2(const NsDev &D, int i, int j) { return hyb_c2(D.nx, i, j); }
+__device__ __forceinline__ size_t mi(const NsDev &D, int i, int j) { return (size_t)(i - 1) + (size_t)D.nx * (j - 1); }
+
+// ---- kernels of one inner iteration -----------------------------------------
+// comput_duvtpckw + get_viscous (sub_NS_singlegrid.f90:121-157, sub_Residual.f90:553-576)
+__global__ void k_ns_prims(NsDev D) {
+    if (D.ctrl->done) return;
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx == 0) D.ctrl->res_bits = 0ull;
+    if (idx >= D.nc) return;
+    int i = (int)(idx % (D.nx + 3)) - 1, j = (int)(idx / (D.nx + 3)) - 1;
+    double d = D.U[idx];
+    double u = D.U[D.nc + idx] / d, v = D.U[2 * D.nc + idx] / d;
+    double t = (D.U[3 * D.nc + idx] - 0.5 * d * (u * u + v * v)) / (D.cv * d);
+    D.d[idx] = d;
+    D.uu[idx] = u;
+    D.vv[idx] = v;
+    D.T[idx] = t;
+    D.p[idx] = D.ptmp * d * t;
+    if (i >= 1 && i <= D.nx - 1 && j >= 1 && j <= D.ny - 1) {
+        if (t < 0.1) atomicExch(&D.ctrl->err, HYB_ERR_TEMPERATURE);
+        D.cc[idx] = sqrt(t) / D.ma;
+    }
+    if (i >= 0 && i <= D.nx && j >= 0 && j <= D.ny) D.amu[idx] = 1.0 / D.re * pow(t, D.omega);
+}
+
+__device__ __forceinline__ double minmod_ns(double a, double b) {
+    if (a * b <= 0.0) return 0.0;
+    return (fabs(a) <= fabs(b)) ? a : b;
+}
+
+// Flux_Van_Leer_1Da (sub_flux_split.f90:141-192), Q = (d, un, ut, p)
+__device__ void van_leer(const double *QL, const double *QR, double *F, double g) {
+    double dl = QL[0], ul = QL[1], vl = QL[2], pl = QL[3];
+    double dr = QR[0], ur = QR[1], vr = QR[2], pr = QR[3];
+    double al = sqrt(g * pl / dl), ar = sqrt(g * pr / dr);
+    double Ml = ul / al, Mr = ur / ar;
+    double fp[4], fm[4];
+    if (Ml >= 1.0) {
+        fp[0] = dl * ul; fp[1] = dl * ul * ul + pl; fp[2] = dl * ul * vl;
+        fp[3] = ul * (g * pl / (g - 1.0) + 0.5 * dl * (ul * ul + vl * vl));
+    } else if (fabs(Ml) < 1.0) {
+        double Mp = 0.25 * (1.0 + Ml) * (1.0 + Ml), t0 = dl * al * Mp;
+        fp[0] = t0;
+        fp[1] = t0 * ((g - 1.0) * ul + 2.0 * al) / g;
+        fp[2] = t0 * vl;
+        fp[3] = t0 * (((g - 1.0) * ul + 2.0 * al) * ((g - 1.0) * ul + 2.0 * al) * 0.5 / (g * g - 1.0) + 0.5 * (vl * vl));
+    } else {
+        fp[0] = fp[1] = fp[2] = fp[3] = 0.0;
+    }
+    if (Mr >= 1.0) {
+        fm[0] = fm[1] = fm[2] = fm[3] = 0.0;
+    } else if (fabs(Mr) < 1.0) {
+        double Mm = -0.25 * (Mr - 1.0) * (Mr - 1.0), t0 = dr * ar * Mm;
+        fm[0] = t0;
+        fm[1] = t0 * ((g - 1.0) * ur - 2.0 * ar) / g;
+        fm[2] = t0 * vr;
+        fm[3] = t0 * (((g - 1.0) * ur - 2.0 * ar) * ((g - 1.0) * ur - 2.0 * ar) * 0.5 / (g * g - 1.0) + 0.5 * (vr * vr));
+    } else {
+        fm[0] = dr * ur; fm[1] = dr * ur * ur + pr; fm[2] = dr * ur * vr;
+        fm[3] = ur * (g * pr / (g - 1.0) + 0.5 * dr * (ur * ur + vr * vr));
+    }
+    for (int k = 0; k < 4; k++) F[k] = fp[k] + fm[k];
+}
+
+// Residual_FVM face fluxes (sub_Residual.f90:66-342), dir 0: i-faces, 1: j-faces
+__global__ void k_ns_faces(NsDev D, int dir) {
+    if (D.ctrl->done) return;
+    const int nx = D.nx, ny = D.ny;
+    int ni = dir == 0 ? nx : nx - 1, nj = dir == 0 ? ny - 1 : ny;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ni * nj) return;
+    int i = idx % ni + 1, j = idx / ni + 1;
+    double s, n1, n2;
+    size_t cs[4];
+    if (dir == 0) {
+        s = D.si[mi(D, i, j)]; n1 = D.ni1[mi(D, i, j)]; n2 = D.ni2[mi(D, i, j)];
+        cs[0] = c2(D, i - 2, j); cs[1] = c2(D, i - 1, j); cs[2] = c2(D, i, j); cs[3] = c2(D, i + 1, j);
+    } else {
+        s = D.sj[mi(D, i, j)]; n1 = D.nj1[mi(D, i, j)]; n2 = D.nj2[mi(D, i, j)];
+        cs[0] = c2(D, i, j - 2); cs[1] = c2(D, i, j - 1); cs[2] = c2(D, i, j); cs[3] = c2(D, i, j + 1);
+    }
+    const double *vars[4] = {D.d, D.uu, D.vv, D.p};
+    double UL[4], UR[4];
+    for (int m = 0; m < 4; m++) {
+        double u1 = vars[m][cs[0]], u2 = vars[m][cs[1]], u3 = vars[m][cs[2]], u4 = vars[m][cs[3]];
+        UL[m] = u2 + 0.5 * minmod_ns(u2 - u1, u3 - u2);
+        UR[m] = u3 - 0.5 * minmod_ns(u3 - u2, u4 - u3);
+    }
+    double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+    double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+    double F0[4];
+    van_leer(QL, QR, F0, D.gamma);
+    const size_t cf = c2(D, i, j);
+    double *Fx = dir == 0 ? D.fluxi : D.fluxj;
+    double f0 = -F0[0] * s, f1 = -(F0[1] * n1 - F0[2] * n2) * s, f2 = -(F0[1] * n2 + F0[2] * n1) * s,
+           f3 = -F0[3] * s;
+    // viscous stresses (same geometry as Convert_NS)
+    const double *x1 = D.x1, *y1 = D.y1, *uu = D.uu, *vv = D.vv, *T = D.T, *amu = D.amu;
+    const double cp = D.cp, pr = D.pr;
+    int lo, hi;
+    double amu1, amk1, dix, diy, djx, djy, diu, div, dit, dju, djv, djt, u1, v1;
+    if (dir == 0) {
+        lo = (i == 1) && !D.perx;
+        hi = (i == nx) && !D.perx;
+        if (lo) { amu1 = amu[c2(D, i, j)]; amk1 = cp * (amu[c2(D, i, j)] / pr); }
+        else if (hi) { amu1 = amu[c2(D, i - 1, j)]; amk1 = cp * (amu[c2(D, i - 1, j)] / pr); }
+        else { amu1 = (amu[c2(D, i - 1, j)] + amu[c2(D, i, j)]) * 0.5;
+               amk1 = cp * ((amu[c2(D, i - 1, j)] + amu[c2(D, i, j)]) / pr) * 0.5; }
+        dix = x1[c2(D, i, j)] - x1[c2(D, i - 1, j)];
+        diy = y1[c2(D, i, j)] - y1[c2(D, i - 1, j)];
+        djx = (x1[c2(D, i - 1, j + 1)] + x1[c2(D, i, j + 1)] - x1[c2(D, i - 1, j - 1)] - x1[c2(D, i, j - 1)]) * 0.25;
+        djy = (y1[c2(D, i - 1, j + 1)] + y1[c2(D, i, j + 1)] - y1[c2(D, i - 1, j - 1)] - y1[c2(D, i, j - 1)]) * 0.25;
+        diu = uu[c2(D, i, j)] - uu[c2(D, i - 1, j)];
+        div = vv[c2(D, i, j)] - vv[c2(D, i - 1, j)];
+        dit = T[c2(D, i, j)] - T[c2(D, i - 1, j)];
+        dju = (uu[c2(D, i - 1, j + 1)] + uu[c2(D, i, j + 1)] - uu[c2(D, i - 1, j - 1)] - uu[c2(D, i, j - 1)]) * 0.25;
+        djv = (vv[c2(D, i - 1, j + 1)] + vv[c2(D, i, j + 1)] - vv[c2(D, i - 1, j - 1)] - vv[c2(D, i, j - 1)]) * 0.25;
+        djt = (T[c2(D, i - 1, j + 1)] + T[c2(D, i, j + 1)] - T[c2(D, i - 1, j - 1)] - T[c2(D, i, j - 1)]) * 0.25;
+        u1 = (uu[c2(D, i, j)] + uu[c2(D, i - 1, j)]) * 0.5;
+        v1 = (vv[c2(D, i, j)] + vv[c2(D, i - 1, j)]) * 0.5;
+    } else {
+        lo = (j == 1) && !D.pery;
+        hi = (j == ny) && !D.pery;
+        if (lo) { amu1 = amu[c2(D, i, j)]; amk1 = cp * (amu[c2(D, i, j)] / pr); }
+        else if (hi) { amu1 = amu[c2(D, i, j - 1)]; amk1 = cp * (amu[c2(D, i, j - 1)] / pr); }
+        else { amu1 = (amu[c2(D, i, j)] + amu[c2(D, i, j - 1)]) * 0.5;
+               amk1 = cp * ((amu[c2(D, i, j - 1)] + amu[c2(D, i, j)]) / pr) * 0.5; }
+        dix = (x1[c2(D, i + 1, j - 1)] + x1[c2(D, i + 1, j)] - x1[c2(D, i - 1, j - 1)] - x1[c2(D, i - 1, j)]) * 0.25;
+        diy = (y1[c2(D, i + 1, j - 1)] + y1[c2(D, i + 1, j)] - y1[c2(D, i - 1, j - 1)] - y1[c2(D, i - 1, j)]) * 0.25;
+        djx = x1[c2(D, i, j)] - x1[c2(D, i, j - 1)];
+        djy = y1[c2(D, i, j)] - y1[c2(D, i, j - 1)];
+        diu = (uu[c2(D, i + 1, j - 1)] + uu[c2(D, i + 1, j)] - uu[c2(D, i - 1, j - 1)] - uu[c2(D, i - 1, j)]) * 0.25;
+        div = (vv[c2(D, i + 1, j - 1)] + vv[c2(D, i + 1, j)] - vv[c2(D, i - 1, j - 1)] - vv[c2(D, i - 1, j)]) * 0.25;
+        dit = (T[c2(D, i + 1, j - 1)] + T[c2(D, i + 1, j)] - T[c2(D, i - 1, j - 1)] - T[c2(D, i - 1, j)]) * 0.25;
+        dju = uu[c2(D, i, j)] - uu[c2(D, i, j - 1)];
+        djv = vv[c2(D, i, j)] - vv[c2(D, i, j - 1)];
+        djt = T[c2(D, i, j)] - T[c2(D, i, j - 1)];
+        u1 = (uu[c2(D, i, j)] + uu[c2(D, i, j - 1)]) * 0.5;
+        v1 = (vv[c2(D, i, j)] + vv[c2(D, i, j - 1)]) * 0.5;
+    }
+    double ds = 1.0 / (dix * djy - djx * diy);
+    double ux = (diu * djy - dju * diy) * ds, vx = (div * djy - djv * diy) * ds, tx = (dit * djy - djt * diy) * ds;
+    double uy = (-diu * djx + dju * dix) * ds, vy = (-div * djx + djv * dix) * ds, ty = (-dit * djx + djt * dix) * ds;
+    double t11 = ((4.0 / 3.0) * ux - (2.0 / 3.0) * vy) * amu1;
+    double t22 = ((4.0 / 3.0) * vy - (2.0 / 3.0) * ux) * amu1;
+    double t12 = (uy + vx) * amu1;
+    double t33 = amu1 * (-(2.0 / 3.0) * ux - (2.0 / 3.0) * vy);
+    double qx = amk1 * tx, qy = amk1 * ty;
+    double *to = dir == 0 ? D.ti_out : D.tj_out, *qo = dir == 0 ? D.qi_out : D.qj_out;
+    to[cf] = t11;
+    to[D.nc + cf] = t22;
+    to[2 * D.nc + cf] = t12;
+    to[3 * D.nc + cf] = t33;
+    qo[cf] = qx;
+    qo[D.nc + cf] = qy;
+    const double *tg = dir == 0 ? D.tg_i : D.tg_j, *qg = dir == 0 ? D.qg_i : D.qg_j;
+    t11 = t11 + tg[cf];
+    t22 = t22 + tg[D.nc + cf];
+    t12 = t12 + tg[2 * D.nc + cf];
+    qx = qx + qg[cf];
+    qy = qy + qg[D.nc + cf];
+    double E1 = u1 * t11 + v1 * t12 + qx, E2 = u1 * t12 + v1 * t22 + qy;
+    Fx[cf] = f0;
+    Fx[D.nc + cf] = f1 + (t11 * n1 + t12 * n2) * s;
+    Fx[2 * D.nc + cf] = f2 + (t12 * n1 + t22 * n2) * s;
+    Fx[3 * D.nc + cf] = f3 + (E1 * n1 + E2 * n2) * s;
+}
+
+// residual, spectral radii, local dt, band max of |Res(4)|; dU reset
+__global__ void k_ns_res(NsDev D) {
+    if (D.ctrl->done) return;
+    const int nx = D.nx, ny = D.ny;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    double r4 = 0.0;
+    if (idx < (nx - 1) * (ny - 1)) {
+        int i = idx % (nx - 1) + 1, j = idx / (nx - 1) + 1;
+        size_t c = c2(D, i, j), ci = c2(D, i + 1, j), cj = c2(D, i, j + 1);
+        const bool in_band = i >= D.ilo && i <= D.ihi && j >= D.jlo && j <= D.jhi;
+        for (int m = 0; m < 4; m++) {
+            size_t o = (size_t)m * D.nc;
+            double r = D.fluxi[o + ci] - D.fluxi[o + c] + D.fluxj[o + cj] - D.fluxj[o + c];
+            if (D.src_on && in_band) r += D.src[o + c];
+            D.Res[o + c] = r;
+            D.dU[o + c] = 0.0;
+        }
+        // comput_Lvc / comput_dt (sub_NS_singlegrid.f90:160-221)
+        double s0 = D.vol[mi(D, i, j)];
+        double si = 0.5 * (D.si[mi(D, i, j)] + D.si[mi(D, i + 1, j)]);
+        double n1 = 0.5 * (D.ni1[mi(D, i, j)] + D.ni1[mi(D, i + 1, j)]);
+        double n2 = 0.5 * (D.ni2[mi(D, i, j)] + D.ni2[mi(D, i + 1, j)]);
+        double sj = 0.5 * (D.sj[mi(D, i, j)] + D.sj[mi(D, i, j + 1)]);
+        double m1 = 0.5 * (D.nj1[mi(D, i, j)] + D.nj1[mi(D, i, j + 1)]);
+        double m2 = 0.5 * (D.nj2[mi(D, i, j)] + D.nj2[mi(D, i, j + 1)]);
+        double uni = D.uu[c] * n1 + D.vv[c] * n2, unj = D.uu[c] * m1 + D.vv[c] * m2;
+        double lci = (fabs(uni) + D.cc[c]) * si, lcj = (fabs(unj) + D.cc[c]) * sj;
+        double tmp1 = D.gamma / D.d[c] * (D.amu[c] / D.pr);
+        double lvi = tmp1 * si * si / s0, lvj = tmp1 * sj * sj / s0;
+        D.Lci[c] = lci;
+        D.Lcj[c] = lcj;
+        D.Lvi[c] = lvi;
+        D.Lvj[c] = lvj;
+        double dt = D.cfl * s0 / (lci + lcj + 1.0 * (lvi + lvj));
+        if (dt > D.dtmax) dt = D.dtmax;
+        if (dt < D.dtmin) dt = D.dtmin;
+        D.dt[c] = dt;
+        if (in_band) {
+            r4 = fabs(D.Res[3 * D.nc + c]);
+            if (r4 != r4) atomicExch(&D.ctrl->err, HYB_ERR_NONFINITE);
+        }
+    }
+    // block max, then one atomic per block (max is order independent)
+    __shared__ double sm[256];
+    sm[threadIdx.x] = r4;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s && sm[threadIdx.x + s] > sm[threadIdx.x]) sm[threadIdx.x] = sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicMax(&D.ctrl->res_bits, (unsigned long long)__double_as_longlong(sm[0]));
+}
+
+// comput_DFn (sub_LU_SGS.f90:122-144)
+__device__ __forceinline__ void dfn(const double *U, const double *dU, double n1, double n2, double g, double *DF) {
+    double U2[4];
+    for (int m = 0; m < 4; m++) U2[m] = U[m] + dU[m];
+    double un1 = (U[1] * n1 + U[2] * n2) / U[0];
+    double p1 = (g - 1.0) * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]);
+    double un2 = (U2[1] * n1 + U2[2] * n2) / U2[0];
+    double p2 = (g - 1.0) * (U2[3] - 0.5 * (U2[1] * U2[1] + U2[2] * U2[2]) / U2[0]);
+    DF[0] = U2[0] * un2 - U[0] * un1;
+    DF[1] = (U2[1] * un2 + p2 * n1) - (U[1] * un1 + p1 * n1);
+    DF[2] = (U2[2] * un2 + p2 * n2) - (U[2] * un1 + p1 * n2);
+    DF[3] = (U2[3] + p2) * un2 - (U[3] + p1) * un1;
+}
+
+// one colour of the forward (bwd = 0) or backward (bwd = 1) LU-SGS sweep
+// (du_LU_SGS_2D, sub_LU_SGS.f90:26-111)
+__global__ void k_ns_lusgs(NsDev D, int color, int bwd) {
+    if (D.ctrl->done) return;
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= bw * bh) return;
+    int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
+    if (((i + j) & 1) != color) return;
+    const double g = D.gamma, w = 1.0;
+    size_t c = c2(D, i, j);
+    double alfa = D.vol[mi(D, i, j)] / D.dt[c] + w * (D.Lci[c] + D.Lcj[c]);
+    alfa = alfa + 2.0 * (D.Lvi[c] + D.Lvj[c]);
+    double dui[4] = {0, 0, 0, 0}, duj[4] = {0, 0, 0, 0}, Un[4], dUn[4], DF[4];
+    if (!bwd) {
+        if (i != D.ilo) {
+            size_t cn = c2(D, i - 1, j);
+            for (int m = 0; m < 4; m++) { Un[m] = D.U[m * D.nc + cn]; dUn[m] = D.dU[m * D.nc + cn]; }
+            dfn(Un, dUn, D.ni1[mi(D, i, j)], D.ni2[mi(D, i, j)], g, DF);
+            for (int m = 0; m < 4; m++)
+                dui[m] = 0.5 * (DF[m] * D.si[mi(D, i, j)] + w * D.Lci[cn] * dUn[m]) + D.Lvi[cn] * dUn[m];
+        }
+        if (j != D.jlo) {
+            size_t cn = c2(D, i, j - 1);
+            for (int m = 0; m < 4; m++) { Un[m] = D.U[m * D.nc + cn]; dUn[m] = D.dU[m * D.nc + cn]; }
+            dfn(Un, dUn, D.nj1[mi(D, i, j)], D.nj2[mi(D, i, j)], g, DF);
+            for (int m = 0; m < 4; m++)
+                duj[m] = 0.5 * (DF[m] * D.sj[mi(D, i, j)] + w * D.Lcj[cn] * dUn[m]) + D.Lvj[cn] * dUn[m];
+        }
+        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = (D.Res[m * D.nc + c] + dui[m] + duj[m]) / alfa;
+    } else {
+        if (i != D.ihi) {
+            size_t cn = c2(D, i + 1, j);
+            for (int m = 0; m < 4; m++) { Un[m] = D.U[m * D.nc + cn]; dUn[m] = D.dU[m * D.nc + cn]; }
+            dfn(Un, dUn, D.ni1[mi(D, i, j)], D.ni2[mi(D, i, j)], g, DF);
+            for (int m = 0; m < 4; m++)
+                dui[m] = -0.5 * (DF[m] * D.si[mi(D, i + 1, j)] - w * D.Lci[cn] * dUn[m]) + D.Lvi[cn] * dUn[m];
+        }
+        if (j != D.jhi) {
+            size_t cn = c2(D, i, j + 1);
+            for (int m = 0; m < 4; m++) { Un[m] = D.U[m * D.nc + cn]; dUn[m] = D.dU[m * D.nc + cn]; }
+            dfn(Un, dUn, D.nj1[mi(D, i, j)], D.nj2[mi(D, i, j)], g, DF);
+            for (int m = 0; m < 4; m++)
+                duj[m] = -0.5 * (DF[m] * D.sj[mi(D, i, j + 1)] - w * D.Lcj[cn] * dUn[m]) + D.Lvj[cn] * dUn[m];
+        }
+        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = D.dU[m * D.nc + c] + (dui[m] + duj[m]) / alfa;
+    }
+}
+
+// U += dU on the band
+__global__ void k_ns_update(NsDev D) {
+    if (D.ctrl->done) return;
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= bw * bh) return;
+    int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
+    size_t c = c2(D, i, j);
+    for (int m = 0; m < 4; m++) D.U[m * D.nc + c] += D.dU[m * D.nc + c];
+}
+
+// periodic ghost U from the band (the NS solver's inner-boundary exchange)
+__device__ void ns_ghosts(const NsDev &D) {
+    const int nx = D.nx, ny = D.ny;
+    if (D.perx)
+        for (int j = (int)threadIdx.x - 1; j <= ny + 1; j += blockDim.x)
+            for (int m = 0; m < 4; m++) {
+                double *Um = D.U + (size_t)m * D.nc;
+                Um[c2(D, 0, j)] = Um[c2(D, nx - 1, j)];
+                Um[c2(D, -1, j)] = Um[c2(D, nx - 2, j)];
+                Um[c2(D, nx, j)] = Um[c2(D, 1, j)];
+                Um[c2(D, nx + 1, j)] = Um[c2(D, 2, j)];
+            }
+    __syncthreads();
+    if (D.pery)
+        for (int i = (int)threadIdx.x - 1; i <= nx + 1; i += blockDim.x)
+            for (int m = 0; m < 4; m++) {
+                double *Um = D.U + (size_t)m * D.nc;
+                Um[c2(D, i, 0)] = Um[c2(D, i, ny - 1)];
+                Um[c2(D, i, -1)] = Um[c2(D, i, ny - 2)];
+                Um[c2(D, i, ny)] = Um[c2(D, i, 1)];
+                Um[c2(D, i, ny + 1)] = Um[c2(D, i, 2)];
+            }
+}
+
+__global__ void k_ns_ghosts(NsDev D) { ns_ghosts(D); }
+
+// periodic ghosts, then the loop decision (one block)
+__global__ void k_ns_close(NsDev D) {
+    if (D.ctrl->done) return;
+    ns_ghosts(D);
+    if (threadIdx.x == 0) {
+        NsCtrl *C = D.ctrl;
+        C->it += 1;
+        double res = __longlong_as_double((long long)C->res_bits);
+        if (C->it == 1 && C->rtol * res > C->tol) C->tol = C->rtol * res;
+        if (!(res > C->tol) || C->it >= C->max_it || C->err) C->done = 1;
+    }
+}
+
+// ---- set-up and finish -------------------------------------------------------
+__device__ __forceinline__ void prim_ns(const double *U, size_t nc, size_t c, double cv, double *r, double *u,
+                                        double *v, double *t) {
+    double d = U[c], uu = U[nc + c] / d, vv = U[2 * nc + c] / d;
+    *r = d;
+    *u = uu;
+    *v = vv;
+    *t = (U[3 * nc + c] - 0.5 * d * (uu * uu + vv * vv)) / (cv * d);
+}
+
+// U = U_k (the Convert_NS state of the kinetic moments) everywhere
+__global__ void k_gsis_start(NsDev D, const double *Ukin) {
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 4 * D.nc) return;
+    D.U[idx] = Ukin[idx];
+}
+
+// synthetic source Q = R_K - R_NS(U_k) on the band; Res holds R_NS(U_k)
+__global__ void k_gsis_src(NsDev D) {
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= bw * bh) return;
+    int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
+    size_t c = c2(D, i, j);
+    int a = D.scan_is_j ? j : i, b = D.scan_is_j ? i : j;
+    size_t ncell = (size_t)(D.scan_is_j ? D.nx - 1 : D.ny - 1) * D.PA;
+    size_t cell = (size_t)(b - 1) * D.PA + (a - 1);
+    const double k = sqrt(2.0 / D.gamma) / D.ma;
+    const double sc[4] = {k, k * k, k * k, 0.5 * k * k * k};
+    const double vol = D.vol[mi(D, i, j)];
+    for (int m = 0; m < 4; m++)
+        D.src[(size_t)m * D.nc + c] = vol * sc[m] * D.rk[(size_t)m * ncell + cell] - D.Res[(size_t)m * D.nc + c];
+}
+
+// volume mean of the band's density change (one block, fixed summation order)
+__global__ void k_gsis_mass(NsDev D) {
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1, n = bw * bh;
+    double num = 0.0, den = 0.0;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
+        size_t c = c2(D, i, j);
+        double vol = D.vol[mi(D, i, j)];
+        num += vol * (D.U[c] - D.U2[c]);
+        den += vol;
+    }
+    __shared__ double sn[256], sd[256];
+    sn[threadIdx.x] = num;
+    sd[threadIdx.x] = den;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sn[threadIdx.x] += sn[threadIdx.x + s];
+            sd[threadIdx.x] += sd[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) D.ctrl->lam = D.mass_proj ? sn[0] / sd[0] : 0.0;
+}
+
+__global__ void k_gsis_copy(double *dst, const double *src, size_t n) {
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < n) dst[idx] = src[idx];
+}
+
+// moment correction with getNSF, on the band
+__global__ void k_gsis_finish(NsDev D) {
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= bw * bh) return;
+    int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
+    size_t c = c2(D, i, j), ci1 = c2(D, i + 1, j), cj1 = c2(D, i, j + 1);
+    const size_t nc = D.nc;
+    const double lam = D.ctrl->lam;
+    const double k2n = sqrt(2.0 / D.gamma) / D.ma;
+    double r, u, v, t, r2, u2, v2, t2;
+    prim_ns(D.U, nc, c, D.cv, &r, &u, &v, &t);
+    prim_ns(D.U2, nc, c, D.cv, &r2, &u2, &v2, &t2);
+    D.S[c] += r - r2 - lam;
+    D.S[nc + c] += (u - u2) / k2n;
+    D.S[2 * nc + c] += (v - v2) / k2n;
+    D.S[3 * nc + c] += t - t2;
+    const double g2 = D.gamma * D.ma * D.ma, q2 = pow(D.ma, 3) * pow(D.gamma, 1.5) / sqrt(2.0);
+    double tao[4], q[2];
+    for (int k = 0; k < 4; k++) {
+        double out = 0.25 * (D.ti_out[k * nc + c] + D.tj_out[k * nc + c] + D.ti_out[k * nc + ci1] + D.tj_out[k * nc + cj1]);
+        double in = 0.25 * (D.tin_i[k * nc + c] + D.tin_j[k * nc + c] + D.tin_i[k * nc + ci1] + D.tin_j[k * nc + cj1]);
+        tao[k] = -1.0 * (out - in) * g2;
+    }
+    for (int k = 0; k < 2; k++) {
+        double out = 0.25 * (D.qi_out[k * nc + c] + D.qj_out[k * nc + c] + D.qi_out[k * nc + ci1] + D.qj_out[k * nc + cj1]);
+        double in = 0.25 * (D.qin_i[k * nc + c] + D.qin_j[k * nc + c] + D.qin_i[k * nc + ci1] + D.qin_j[k * nc + cj1]);
+        q[k] = -1.0 * (out - in) * q2;
+    }
+    D.S[4 * nc + c] += tao[0];
+    D.S[5 * nc + c] += tao[1];
+    D.S[6 * nc + c] += tao[2];
+    D.S[9 * nc + c] += tao[3];
+    D.S[7 * nc + c] += q[0];
+    D.S[8 * nc + c] += q[1];
+}
+
+// Shakhov parameters of the next kinetic step from the corrected moments
+template <typename real>
+__global__ void k_gsis_eqp(const double *S, size_t nc, int nx, real *eqp, int Na, int Nb, int PA, int scan_is_j,
+                           double cpr) {
+    const size_t ncell = (size_t)Nb * PA;
+    size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ncell) return;
+    int a = (int)(cell % PA) + 1, b = (int)(cell / PA) + 1;
+    if (a > Na) return;
+    int i = scan_is_j ? b : a, j = scan_is_j ? a : b;
+    size_t c = hyb_c2(nx, i, j);
+    double S1 = S[c], u = S[nc + c], vv = S[2 * nc + c], tt = S[3 * nc + c], qx = S[7 * nc + c], qy = S[8 * nc + c];
+    double cpt = cpr / (S1 * tt * tt);
+    eqp[0 * ncell + cell] = (real)(S1 / (HYB_PI * tt));
+    eqp[1 * ncell + cell] = (real)u;
+    eqp[2 * ncell + cell] = (real)vv;
+    eqp[3 * ncell + cell] = (real)(1.0 / tt);
+    eqp[4 * ncell + cell] = (real)(tt / 2.0);
+    eqp[5 * ncell + cell] = (real)(cpt * qx);
+    eqp[6 * ncell + cell] = (real)(cpt * qy);
+}
+
+// ---- host ----------------------------------------------------------------------
+static int ck(hyb_ctx *ctx, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+        return HYB_ERR_CUDA;
+    }
+    return HYB_OK;
+}
+
+void ns_destroy(hyb_ctx *ctx) {
+    NsState *st = (NsState *)ctx->ns;
+    if (!st) return;
+    if (st->have_graph) cudaGraphExecDestroy(st->graph);
+    if (st->buf) cudaFree(st->buf);
+    if (st->geo) cudaFree(st->geo);
+    if (st->ctrl) cudaFree(st->ctrl);
+    if (st->h_ctrl) cudaFreeHost(st->h_ctrl);
+    if (st->rk) cudaFree(st->rk);
+    if (ctx->d_rhs_gsis) cudaFree(ctx->d_rhs_gsis);
+    ctx->d_rhs_gsis = nullptr;
+    delete st;
+    ctx->ns = nullptr;
+}
+
+int ns_create(hyb_ctx *ctx) {
+    if (ctx->ns) {   // reconfigured: re-capture with the new parameters
+        NsState *st = (NsState *)ctx->ns;
+        if (st->have_graph) cudaGraphExecDestroy(st->graph);
+        st->have_graph = false;
+        st->D.mass_proj = ctx->gsis.reserved[1] == 0;
+        return HYB_OK;
+    }
+    if ((ctx->nx < 7 && ctx->bc[0] != HYB_BC_PERIODIC) || (ctx->ny < 7 && ctx->bc[1] != HYB_BC_PERIODIC)) {
+        ctx->last_error = "synthetic solve: a wall-bounded axis needs at least 6 cells";
+        return HYB_ERR_UNSUPPORTED;
+    }
+    // the energy moment maps onto the NS energy only for a monatomic gas
+    if (fabs(ctx->prm.gamma - 5.0 / 3.0) > 1e-9) {
+        ctx->last_error = "synthetic solve: gamma must be 5/3";
+        return HYB_ERR_UNSUPPORTED;
+    }
+    NsState *st = new NsState();
+    memset(&st->D, 0, sizeof(NsDev));
+    NsDev &D = st->D;
+    D.nx = ctx->nx;
+    D.ny = ctx->ny;
+    D.perx = ctx->bc[0] == HYB_BC_PERIODIC;
+    D.pery = ctx->bc[1] == HYB_BC_PERIODIC;
+    if (D.perx) { D.ilo = 1; D.ihi = D.nx - 1; } else { D.ilo = 3; D.ihi = D.nx - 3; }
+    if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = 3; D.jhi = D.ny - 3; }
+    D.nc = (size_t)(D.nx + 3) * (D.ny + 3);
+    const size_t nc = D.nc;
+    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2;   // see the pointer carve below
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
+    if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
+    if (cudaMalloc((void **)&st->rk, 4 * ncell * sizeof(double)) != cudaSuccess) {
+        cudaFree(ctx->d_rhs_gsis);
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
+    cudaMemsetAsync(st->rk, 0, 4 * ncell * sizeof(double), ctx->stream);
+    if (cudaMalloc((void **)&st->buf, (size_t)ncomp * nc * sizeof(double)) != cudaSuccess) {
+        cudaFree(st->rk);
+        cudaFree(ctx->d_rhs_gsis);
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
+    cudaMemsetAsync(st->buf, 0, (size_t)ncomp * nc * sizeof(double), ctx->stream);
+    double *h = st->buf;
+    D.U = h; h += 4 * nc; D.src = h; h += 4 * nc; D.U2 = h; h += 4 * nc; D.dU = h; h += 4 * nc; D.Res = h; h += 4 * nc;
+    D.dt = h; h += nc; D.Lci = h; h += nc; D.Lcj = h; h += nc; D.Lvi = h; h += nc; D.Lvj = h; h += nc;
+    D.d = h; h += nc; D.uu = h; h += nc; D.vv = h; h += nc; D.T = h; h += nc; D.p = h; h += nc; D.cc = h; h += nc;
+    D.amu = h; h += nc;
+    D.fluxi = h; h += 4 * nc; D.fluxj = h; h += 4 * nc;
+    D.ti_out = h; h += 4 * nc; D.qi_out = h; h += 2 * nc; D.tj_out = h; h += 4 * nc; D.qj_out = h; h += 2 * nc;
+    const size_t nm = (size_t)ctx->nx * ctx->ny;
+    if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
+        cudaFree(st->buf);
+        cudaFree(st->rk);
+        cudaFree(ctx->d_rhs_gsis);
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
+    const std::vector<double> *g7[7] = {&ctx->vol, &ctx->si, &ctx->sj, &ctx->ni1, &ctx->ni2, &ctx->nj1, &ctx->nj2};
+    for (int k = 0; k < 7; k++)
+        cudaMemcpy(st->geo + k * nm, g7[k]->data(), nm * sizeof(double), cudaMemcpyHostToDevice);
+    D.vol = st->geo; D.si = st->geo + nm; D.sj = st->geo + 2 * nm; D.ni1 = st->geo + 3 * nm;
+    D.ni2 = st->geo + 4 * nm; D.nj1 = st->geo + 5 * nm; D.nj2 = st->geo + 6 * nm;
+    D.x1 = ctx->d_x1;
+    D.y1 = ctx->d_y1;
+    // d_hot: U[4] d uu vv T amu tin_i[4] qin_i[2] tin_j[4] qin_j[2] tg_i[4] qg_i[2] tg_j[4] qg_j[2]
+    const double *hot = ctx->d_hot;
+    D.tin_i = hot + 9 * nc; D.qin_i = hot + 13 * nc; D.tin_j = hot + 15 * nc; D.qin_j = hot + 19 * nc;
+    D.tg_i = hot + 21 * nc; D.qg_i = hot + 25 * nc; D.tg_j = hot + 27 * nc; D.qg_j = hot + 31 * nc;
+    D.S = ctx->d_S;
+    D.rk = st->rk;
+    D.PA = ctx->PA;
+    D.scan_is_j = ctx->scan_is_j;
+    D.mass_proj = ctx->gsis.reserved[1] == 0;
+    D.src_on = 1;
+    D.gamma = ctx->prm.gamma;
+    D.ma = ctx->prm.ma;
+    D.pr = ctx->prm.pr;
+    D.re = ctx->prm.re;
+    D.omega = ctx->prm.omega_ns;
+    D.cv = 1.0 / (D.gamma * (D.gamma - 1.0) * D.ma * D.ma);
+    D.cp = D.cv * D.gamma;
+    D.ptmp = 1.0 / (D.gamma * D.ma * D.ma);
+    if (cudaMalloc((void **)&st->ctrl, sizeof(NsCtrl)) != cudaSuccess ||
+        cudaMallocHost((void **)&st->h_ctrl, sizeof(NsCtrl)) != cudaSuccess) {
+        cudaFree(st->buf); cudaFree(st->geo); cudaFree(st->rk); cudaFree(ctx->d_rhs_gsis);
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
+    D.ctrl = st->ctrl;
+    st->have_graph = false;
+    ctx->ns = st;
+    return ck(ctx, "ns_create");
+}
+
+// launches of one inner iteration (captured NS_BATCH times into a graph)
+static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
+    const int bs = 256;
+    const unsigned gc = (unsigned)((D.nc + bs - 1) / bs);
+    const int nfi = D.nx * (D.ny - 1), nfj = (D.nx - 1) * D.ny;
+    const int ncell = (D.nx - 1) * (D.ny - 1);
+    const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
+    cudaStream_t s = ctx->stream;
+    k_ns_prims<<<gc, bs, 0, s>>>(D);
+    k_ns_faces<<<(nfi + bs - 1) / bs, bs, 0, s>>>(D, 0);
+    k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D, 1);
+    k_ns_res<<<(ncell + bs - 1) / bs, bs, 0, s>>>(D);
+    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 0);
+    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 0);
+    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 1);
+    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 1);
+    k_ns_update<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+    k_ns_close<<<1, 256, 0, s>>>(D);
+}
+
+int gsis_solve(hyb_ctx *ctx) {
+    NsState *st = (NsState *)ctx->ns;
+    if (!st) return HYB_ERR_INVALID;
+    NsDev &D = st->D;
+    D.cfl = ctx->gsis.cfl > 0 ? ctx->gsis.cfl : 20.0;
+    D.dtmax = ctx->gsis.dtmax > 0 ? ctx->gsis.dtmax : 10.0;
+    D.dtmin = ctx->gsis.dtmin > 0 ? ctx->gsis.dtmin : 1e-7;
+    const int bs = 256;
+    const unsigned gc = (unsigned)((D.nc + bs - 1) / bs);
+    const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
+    cudaStream_t s = ctx->stream;
+    // kinetic residual of the current f with its own equilibrium: wall slots,
+    // an RHS-only sweep, per-cell moments (the next step's wall pass
+    // recomputes the same slots)
+    int rc = launch_wall(ctx);
+    if (!rc) rc = launch_sweep(ctx, 2);
+    if (!rc) rc = launch_rhs_moments(ctx, st->rk);
+    if (rc) return rc;
+    // U = U_k, the state Convert_NS left in d_hot
+    k_gsis_start<<<(unsigned)((4 * D.nc + bs - 1) / bs), bs, 0, s>>>(D, ctx->d_hot);
+    k_ns_ghosts<<<1, 256, 0, s>>>(D);
+    k_gsis_copy<<<(unsigned)((4 * D.nc + bs - 1) / bs), bs, 0, s>>>(D.U2, D.U, 4 * D.nc);
+    NsCtrl c0;
+    memset(&c0, 0, sizeof(c0));
+    c0.max_it = ctx->gsis.max_inner > 0 ? ctx->gsis.max_inner : 2000;
+    c0.tol = ctx->gsis.inner_tol;
+    c0.rtol = ctx->gsis.inner_rtol;
+    *st->h_ctrl = c0;
+    HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
+    // R_NS(U_k) without the source, then Q = R_K - R_NS(U_k)
+    {
+        NsDev D0 = D;
+        D0.src_on = 0;
+        const int nfi = D.nx * (D.ny - 1), nfj = (D.nx - 1) * D.ny, ncl = (D.nx - 1) * (D.ny - 1);
+        k_ns_prims<<<gc, bs, 0, s>>>(D0);
+        k_ns_faces<<<(nfi + bs - 1) / bs, bs, 0, s>>>(D0, 0);
+        k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D0, 1);
+        k_ns_res<<<(ncl + bs - 1) / bs, bs, 0, s>>>(D0);
+        k_gsis_src<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+    }
+    ctx->launches += 8;
+    HYB_CK(cudaGetLastError());
+    if (!st->have_graph) {
+        cudaGraph_t g;
+        HYB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < NS_BATCH; k++) inner_iteration(ctx, D);
+        HYB_CK(cudaStreamEndCapture(s, &g));
+        HYB_CK(cudaGraphInstantiate(&st->graph, g, 0));
+        cudaGraphDestroy(g);
+        st->have_graph = true;
+    }
+    int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
+    for (int b = 0; b < nbatch; b++) {
+        HYB_CK(cudaGraphLaunch(st->graph, s));
+        ctx->launches += NS_BATCH * 10;
+        HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
+        HYB_CK(cudaStreamSynchronize(s));
+        if (st->h_ctrl->done) break;
+    }
+    ctx->gsis_last_inner = st->h_ctrl->it;
+    if (st->h_ctrl->err) {
+        ctx->last_error = "synthetic solve: temperature below 0.1 or non-finite residual";
+        return st->h_ctrl->err;
+    }
+    k_gsis_mass<<<1, 256, 0, s>>>(D);
+    k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    if (ctx->precision == HYB_PREC_FP64)
+        k_gsis_eqp<double><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (double *)ctx->d_eqp,
+                                                                          ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
+                                                                          ctx->prm.cpr);
+    else
+        k_gsis_eqp<float><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (float *)ctx->d_eqp,
+                                                                        ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
+                                                                        ctx->prm.cpr);
+    ctx->launches += 3;
+    return ck(ctx, "gsis_finish");
+}
+
+}  // namespace hyb

@@ -293,7 +293,7 @@ template <typename real, int VS>
 __global__ void __launch_bounds__(32 * VS) k_residual(const real *__restrict__ rhs, const double *__restrict__ vx,
                                                        const double *__restrict__ vy, const double *__restrict__ w,
                                                        int nvi, int nv, int Na, int Nb, int PA,
-                                                       double *__restrict__ part) {
+                                                       double *__restrict__ part, double *__restrict__ cellm) {
     const int tx = threadIdx.x, sl = threadIdx.y;
     const int a = blockIdx.x * 32 + tx + 1, b = blockIdx.y + 1;
     const bool act = a <= Na;
@@ -333,6 +333,7 @@ __global__ void __launch_bounds__(32 * VS) k_residual(const real *__restrict__ r
             double x = 0.0;
             for (int q = 0; q < VS; q++) x += red[q][k][tx];
             cellv[k][tx] = act ? x : 0.0;
+            if (cellm && act) cellm[(size_t)k * Nb * PA + cell] = x;
         }
     }
     __syncthreads();
@@ -521,21 +522,33 @@ int launch_moments(hyb_ctx *ctx) {
     return check_err(ctx, "k_moments_finish");
 }
 
-int launch_residual(hyb_ctx *ctx, hyb_residual *out) {
+static int residual_part(hyb_ctx *ctx, const void *rhs, double *cellm, int *nblk_out) {
     constexpr int VS = 8;
     dim3 blk(32, VS), grd((ctx->Na + 31) / 32, ctx->Nb);
-    int nblk = grd.x * grd.y;
+    *nblk_out = grd.x * grd.y;
     double *part = ctx->d_resid + 16;
     if (ctx->precision == HYB_PREC_FP64)
-        k_residual<double, VS><<<grd, blk, 0, ctx->stream>>>((const double *)ctx->d_rhs, ctx->d_vx, ctx->d_vy,
-                                                              ctx->d_w, ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA,
-                                                              part);
+        k_residual<double, VS><<<grd, blk, 0, ctx->stream>>>((const double *)rhs, ctx->d_vx, ctx->d_vy, ctx->d_w,
+                                                              ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA, part,
+                                                              cellm);
     else
-        k_residual<float, VS><<<grd, blk, 0, ctx->stream>>>((const float *)ctx->d_rhs, ctx->d_vx, ctx->d_vy,
-                                                             ctx->d_w, ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA,
-                                                             part);
+        k_residual<float, VS><<<grd, blk, 0, ctx->stream>>>((const float *)rhs, ctx->d_vx, ctx->d_vy, ctx->d_w,
+                                                             ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA, part,
+                                                             cellm);
     ctx->launches++;
-    int rc = check_err(ctx, "k_residual");
+    return check_err(ctx, "k_residual");
+}
+
+// per-cell moments 1-4 of the RHS-only sweep's output, [4][Nb*PA]
+int launch_rhs_moments(hyb_ctx *ctx, double *cellm) {
+    int nblk;
+    return residual_part(ctx, ctx->d_rhs_gsis, cellm, &nblk);
+}
+
+int launch_residual(hyb_ctx *ctx, hyb_residual *out) {
+    int nblk;
+    double *part = ctx->d_resid + 16;
+    int rc = residual_part(ctx, ctx->d_rhs, nullptr, &nblk);
     if (rc) return rc;
     k_residual_final<<<1, 32, 0, ctx->stream>>>(part, nblk, (double)ctx->ncx * ctx->ncy, ctx->d_resid);
     ctx->launches++;

@@ -39,7 +39,8 @@ size_t sweep_smem_bytes(const hyb_ctx *ctx) {
 template <typename real>
 static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.f = (real *)ctx->d_f;
-    A.rhs = store_rhs ? (real *)ctx->d_rhs : nullptr;
+    A.rhs = store_rhs == 2 ? (real *)ctx->d_rhs_gsis : store_rhs ? (real *)ctx->d_rhs : nullptr;
+    A.no_update = store_rhs == 2;
     A.fw_alo = A.fw_ahi = A.fw_blo = A.fw_bhi = nullptr;
     for (int face = 1; face <= 4; face++) {
         if (ctx->bc[face - 1] != HYB_BC_WALL) continue;
@@ -74,6 +75,8 @@ static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.err = ctx->d_err;
 }
 
+// store_rhs: 0 no RHS store, 1 RHS to d_rhs with the update, 2 RHS only
+// (to d_rhs_gsis, f unchanged)
 int launch_sweep(hyb_ctx *ctx, int store_rhs) {
     int cpt, vpb;
     sweep_shape(ctx, &cpt, &vpb);

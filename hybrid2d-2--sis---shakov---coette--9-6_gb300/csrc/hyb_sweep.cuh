@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
         dlb[t] = act ? nG[0] : real(0);
         dlb[TPV + t] = act ? nH[0] : real(0);
         // backward + update of row b-1 (GKUA_Residual.f90:64-109)
-        if (b > 1 && act) {
+        if (b > 1 && act && !A.no_update) {
             const real *dlp = dlf + (size_t)((b - 1) & 1) * 2 * TPV;
             const bool has_next = (a0 + CPT <= Na);
             const real lastG = has_next ? dlp[t + 1] : real(0), lastH = has_next ? dlp[TPV + t + 1] : real(0);
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
         }
     }
     __syncthreads();
-    if (act) {   // backward + update of the last row (downstream values are 0)
+    if (act && !A.no_update) {   // backward + update of the last row (downstream values are 0)
         const real *dlp = dlf + (size_t)(Nb & 1) * 2 * TPV;
         const bool has_next = (a0 + CPT <= Na);
         const real *o0 = rowp(Nb) + (a0 - 1);

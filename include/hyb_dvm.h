@@ -123,6 +123,8 @@ typedef struct hyb_gsis_params {
     int    enable;          /* 0: plain kinetic iteration                    */
     int    max_inner;       /* cap on NS inner iterations per outer step     */
     double inner_tol;       /* reference: res_iter > 1e-6 (Hybrid_Sub.f90:99) */
+    double inner_rtol;      /* also stop once max|Res(4)| <= inner_rtol times its
+                               value at the first inner iteration (0: off)   */
     double cfl, dtmax, dtmin;   /* local time step (sub_NS_singlegrid.f90:160-183) */
     int    flux;            /* NS flux splitting, Flux_* (COMMONDATA.f90:12) */
     int    ns_scheme;       /* NS reconstruction scheme, Scheme_* (:11)      */

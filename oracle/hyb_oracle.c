@@ -19,7 +19,7 @@
  *   Hybrid2D/src/sub_Residual.f90         get_viscous (used by Convert_NS)
  *   Hybrid2D/src/Functions.f90            FMINMD
  */
-#include "hyb_oracle.h"
+#include "hyb_oracle_impl.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -27,48 +27,6 @@
 #ifdef _OPENMP
 #include <omp.h>
 #endif
-
-#define LAP 2
-#define NRD 2
-#define NSUM 11
-#define PI 3.1415926535897932
-
-/* REAL(4) literals of the reference, widened to double the way the Fortran
- * compiler widens them: 1.E-30 (GKUA_Residual.f90:104), 1.E-15
- * (RHSFDVsub :143), 1./3. and 2./3. (:144). */
-#define F_FLOOR ((double)1.0e-30f)
-#define EPSWENO ((double)1.0e-15f)
-#define CWENO1 ((double)(1.0f / 3.0f))
-#define CWENO2 ((double)(2.0f / 3.0f))
-
-struct orc {
-    int nx, ny, nvi, nvj, nv;
-    int pw;               /* (nx+7): pitch of -3:nx+3 arrays                  */
-    size_t P;             /* (nx+7)*(ny+7)                                    */
-    int bc[4];
-    double *wall_u[4], *wall_v[4], *wall_t[4];
-    double *vi, *vj, *wi, *wj;
-    hyb_params prm;
-    /* geometry */
-    double *xn, *yn;      /* nodes on (1-LAP:nx+LAP, 1-LAP:ny+LAP)           */
-    double *vol, *si, *sj, *ni1, *ni2, *nj1, *nj2;   /* (nx,ny)               */
-    double *x1, *y1;      /* cell centres on (1-LAP:nx+LAP-1, ...)           */
-    /* state */
-    double *frd, *frd00, *S, *S0, *CF;
-    double *tao_i_g, *q_i_g, *tao_j_g, *q_j_g;        /* HoT, C2 extents      */
-    double *tao_i_in, *q_i_in, *tao_j_in, *q_j_in;    /* NSF from kinetic     */
-    double err;
-};
-
-/* ---- index helpers ------------------------------------------------------ */
-#define IX(o, i, j) ((size_t)((i) + 3) + (size_t)(o)->pw * (size_t)((j) + 3))
-#define FRD(o, ird, i, j, v) (o)->frd[((size_t)(v) * (o)->P + IX(o, i, j)) * NRD + (ird)]
-#define FRD00(o, ird, i, j, v) (o)->frd00[((size_t)(v) * (o)->P + IX(o, i, j)) * NRD + (ird)]
-#define SG(o, k, i, j) (o)->S[IX(o, i, j) * NSUM + (k) - 1]
-#define CFA(o, i, j) (o)->CF[IX(o, i, j)]
-#define MI(o, i, j) ((size_t)((i) - 1) + (size_t)(o)->nx * (size_t)((j) - 1))
-#define XN(o, i, j) ((size_t)((i) + 1) + (size_t)((o)->nx + 4) * (size_t)((j) + 1))
-#define C2(o, i, j) ((size_t)((i) + 1) + (size_t)((o)->nx + 3) * (size_t)((j) + 1))
 
 static double pos_part(double a) { return (a + fabs(a)) * 0.5; }
 static double neg_part(double a) { return (a - fabs(a)) * 0.5; }
@@ -239,6 +197,7 @@ void orc_destroy(orc *o)
     free(o->frd); free(o->frd00); free(o->S); free(o->S0); free(o->CF);
     free(o->tao_i_g); free(o->q_i_g); free(o->tao_j_g); free(o->q_j_g);
     free(o->tao_i_in); free(o->q_i_in); free(o->tao_j_in); free(o->q_j_in);
+    orc_ns_free(o);
     free(o);
 }
 
@@ -632,6 +591,65 @@ static void rhs_velocity(const orc *o, int iv, int jv, double *rhs, double *atsv
 #undef F
 }
 
+/* ---- moments 1-4 of the kinetic RHS of the current f with its own
+ * equilibrium (RHSFDVsub with the moments of DETFP_res), per cell on the C2
+ * extents: rk[m*nc2 + C2(i,j)], m = rho, rho u, rho v, energy; the per-volume
+ * rate in kinetic time.  The synthetic solve is driven by it. ------------- */
+int orc_kinetic_residual_moments(orc *o, double *rk)
+{
+    const int nx = o->nx, ny = o->ny, fp = nx + 2;
+    const size_t nc2 = (size_t)(nx + 3) * (ny + 3);
+    const size_t ncell = (size_t)(nx - 1) * (ny - 1);
+    int nth = 1;
+#ifdef _OPENMP
+    nth = omp_get_max_threads();
+#endif
+    double *part = (double *)calloc((size_t)nth * 4 * ncell, sizeof(double));
+    if (!part) return HYB_ERR_NOMEM;
+#pragma omp parallel num_threads(nth)
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        double *acc = part + (size_t)tid * 4 * ncell;
+        double *rhs = (double *)calloc(o->P * NRD, sizeof(double));
+        double *ax = (double *)calloc((size_t)fp * (ny + 2), sizeof(double));
+        double *ay = (double *)calloc((size_t)fp * (ny + 2), sizeof(double));
+        double *flux = (double *)calloc((size_t)fp * (ny + 2) * NRD, sizeof(double));
+        int mx = (nx > ny ? nx : ny) + 8;
+        double *dfrd = (double *)calloc((size_t)mx * NRD, sizeof(double));
+#pragma omp for schedule(static)
+        for (int v = 0; v < o->nv; v++) {
+            int iv = v % o->nvi, jv = v / o->nvi;
+            rhs_velocity(o, iv, jv, rhs, ax, ay, flux, dfrd);
+            double vx = o->vi[iv], vy = o->vj[jv], w = o->wi[iv] * o->wj[jv];
+            for (int j = 1; j <= ny - 1; j++)
+                for (int i = 1; i <= nx - 1; i++) {
+                    size_t k = (size_t)(i - 1) + (size_t)(nx - 1) * (j - 1);
+                    double g = rhs[IX(o, i, j) * NRD + 0], h = rhs[IX(o, i, j) * NRD + 1];
+                    acc[k] += w * g;
+                    acc[ncell + k] += w * vx * g;
+                    acc[2 * ncell + k] += w * vy * g;
+                    acc[3 * ncell + k] += w * (h + (vx * vx + vy * vy) * g);
+                }
+        }
+        free(rhs); free(ax); free(ay); free(flux); free(dfrd);
+    }
+    memset(rk, 0, 4 * nc2 * sizeof(double));
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+            size_t k = (size_t)(i - 1) + (size_t)(nx - 1) * (j - 1);
+            for (int m = 0; m < 4; m++) {
+                double x = 0.0;
+                for (int t = 0; t < nth; t++) x += part[((size_t)t * 4 + m) * ncell + k];
+                rk[(size_t)m * nc2 + C2(o, i, j)] = x;
+            }
+        }
+    free(part);
+    return HYB_OK;
+}
+
 /* ---- GKUA_Residual (GKUA_Residual.f90:4-114) ---------------------------- */
 int orc_kinetic_step(orc *o)
 {
@@ -887,6 +905,54 @@ int orc_upload_f(orc *o, const double *frd)
  * block-connection view); the reference's single-block formulas (one-sided
  * face values, linear U extrapolation, corner S extrapolation) are kept for
  * wall faces. */
+/* NS conservative variables from the moments on 0..nx x 0..ny and their
+ * ghost cells (Hybrid_Sub.f90:225-239), U on the C2 extents, 4 per cell. */
+void orc_build_u(orc *o, double *U)
+{
+    const int nx = o->nx, ny = o->ny;
+    const double gam = o->prm.gamma, ma = o->prm.ma;
+    const double cv = 1.0 / (gam * (gam - 1.0) * ma * ma);
+    const int perx = (o->bc[0] == HYB_BC_PERIODIC), pery = (o->bc[1] == HYB_BC_PERIODIC);
+#define UU(m, i, j) U[C2(o, i, j) * 4 + (m)]
+    /* U outside 0..n keeps the reference's initial state (sub_init.f90:416-419) */
+    for (int j = -1; j <= ny + 1; j++)
+        for (int i = -1; i <= nx + 1; i++) {
+            UU(0, i, j) = 1.0; UU(1, i, j) = 0.0; UU(2, i, j) = 0.0; UU(3, i, j) = cv;
+        }
+    for (int i = 0; i <= nx; i++)
+        for (int j = 0; j <= ny; j++) {
+            UU(0, i, j) = SG(o, 1, i, j);
+            double tu = SG(o, 2, i, j) / ma * sqrt(2.0 / gam);
+            UU(1, i, j) = UU(0, i, j) * tu;
+            double tv = SG(o, 3, i, j) / ma * sqrt(2.0 / gam);
+            UU(2, i, j) = UU(0, i, j) * tv;
+            double tt = SG(o, 4, i, j);
+            UU(3, i, j) = UU(0, i, j) * cv * tt + 0.5 * UU(0, i, j) * (tu * tu + tv * tv);
+        }
+    /* ghost U, :236-239 */
+    for (int j = -1; j <= ny + 1; j++)
+        for (int m = 0; m < 4; m++) {
+            if (perx) {
+                UU(m, 0, j) = UU(m, nx - 1, j); UU(m, -1, j) = UU(m, nx - 2, j);
+                UU(m, nx, j) = UU(m, 1, j);     UU(m, nx + 1, j) = UU(m, 2, j);
+            } else {
+                UU(m, 0, j) = 2.0 * UU(m, 1, j) - UU(m, 2, j);
+                UU(m, nx, j) = 2.0 * UU(m, nx - 1, j) - UU(m, nx - 2, j);
+            }
+        }
+    for (int i = -1; i <= nx + 1; i++)
+        for (int m = 0; m < 4; m++) {
+            if (pery) {
+                UU(m, i, 0) = UU(m, i, ny - 1); UU(m, i, -1) = UU(m, i, ny - 2);
+                UU(m, i, ny) = UU(m, i, 1);     UU(m, i, ny + 1) = UU(m, i, 2);
+            } else {
+                UU(m, i, 0) = 2.0 * UU(m, i, 1) - UU(m, i, 2);
+                UU(m, i, ny) = 2.0 * UU(m, i, ny - 1) - UU(m, i, ny - 2);
+            }
+        }
+#undef UU
+}
+
 int orc_convert_ns(orc *o)
 {
     const int nx = o->nx, ny = o->ny;
@@ -914,45 +980,8 @@ int orc_convert_ns(orc *o)
     double *vv = (double *)calloc(nc, sizeof(double)), *T = (double *)calloc(nc, sizeof(double));
     double *amu = (double *)calloc(nc, sizeof(double));
     if (!U || !d || !uu || !vv || !T || !amu) { free(U); free(d); free(uu); free(vv); free(T); free(amu); return HYB_ERR_NOMEM; }
+    orc_build_u(o, U);
 #define UU(m, i, j) U[C2(o, i, j) * 4 + (m)]
-    /* U outside 0..n keeps the reference's initial state (sub_init.f90:416-419) */
-    for (int j = -1; j <= ny + 1; j++)
-        for (int i = -1; i <= nx + 1; i++) {
-            UU(0, i, j) = 1.0; UU(1, i, j) = 0.0; UU(2, i, j) = 0.0; UU(3, i, j) = cv;
-        }
-    const double sc = sqrt(2.0 / gam) / ma;   /* kinetic -> NS velocity, :228 */
-    for (int i = 0; i <= nx; i++)
-        for (int j = 0; j <= ny; j++) {
-            UU(0, i, j) = SG(o, 1, i, j);
-            double tu = SG(o, 2, i, j) / ma * sqrt(2.0 / gam);
-            UU(1, i, j) = UU(0, i, j) * tu;
-            double tv = SG(o, 3, i, j) / ma * sqrt(2.0 / gam);
-            UU(2, i, j) = UU(0, i, j) * tv;
-            double tt = SG(o, 4, i, j);
-            UU(3, i, j) = UU(0, i, j) * cv * tt + 0.5 * UU(0, i, j) * (tu * tu + tv * tv);
-        }
-    (void)sc;
-    /* ghost U, :236-239 */
-    for (int j = -1; j <= ny + 1; j++)
-        for (int m = 0; m < 4; m++) {
-            if (perx) {
-                UU(m, 0, j) = UU(m, nx - 1, j); UU(m, -1, j) = UU(m, nx - 2, j);
-                UU(m, nx, j) = UU(m, 1, j);     UU(m, nx + 1, j) = UU(m, 2, j);
-            } else {
-                UU(m, 0, j) = 2.0 * UU(m, 1, j) - UU(m, 2, j);
-                UU(m, nx, j) = 2.0 * UU(m, nx - 1, j) - UU(m, nx - 2, j);
-            }
-        }
-    for (int i = -1; i <= nx + 1; i++)
-        for (int m = 0; m < 4; m++) {
-            if (pery) {
-                UU(m, i, 0) = UU(m, i, ny - 1); UU(m, i, -1) = UU(m, i, ny - 2);
-                UU(m, i, ny) = UU(m, i, 1);     UU(m, i, ny + 1) = UU(m, i, 2);
-            } else {
-                UU(m, i, 0) = 2.0 * UU(m, i, 1) - UU(m, i, 2);
-                UU(m, i, ny) = 2.0 * UU(m, i, ny - 1) - UU(m, i, ny - 2);
-            }
-        }
     /* comput_duvtpckw (sub_NS_singlegrid.f90:121-157) and get_viscous
      * (sub_Residual.f90:553-576) */
     for (int j = -1; j <= ny + 1; j++)
@@ -1109,6 +1138,10 @@ int orc_step(orc *o, int n_iter, hyb_residual *r)
         orc_kinetic_step(o);
         orc_detfp(o);
         orc_convert_ns(o);
+        if (o->gsis.enable) {
+            int rc = orc_gsis_solve(o);
+            if (rc) return rc;
+        }
     }
     if (r) orc_detfp_res(o, r);
     return HYB_OK;

@@ -58,6 +58,12 @@ int     orc_hot(orc *o, double *tao_i, double *q_i, double *tao_j, double *q_j);
 int     orc_nsf_in(orc *o, double *tao_i, double *q_i, double *tao_j, double *q_j);
 double  orc_err(orc *o);                /* DETFP's CF-change diagnostic ERR     */
 
+/* GSIS synthetic solve (hyb_oracle_ns.c) */
+int orc_gsis_configure(orc *o, const hyb_gsis_params *gp);
+int orc_gsis_last_inner(orc *o);
+int orc_ns_state(orc *o, double *U);                  /* U[4][(nx+3)(ny+3)] */
+int orc_ns_residual(orc *o, const double *U, double *res);
+
 /* geometry derived from the nodes (Creat_Mesh, Update_coordinate_buffer) */
 int orc_geometry(orc *o, double *vol, double *si, double *sj, double *ni1,
                  double *ni2, double *nj1, double *nj2, double *x1, double *y1);

@@ -1,0 +1,607 @@
+/*
+ * hyb_oracle_ns.c -- CPU FP64 restatement of the GSIS synthetic macroscopic
+ * solve.  TEST INFRASTRUCTURE ONLY (see hyb_oracle.h).
+ *
+ * Reference files restated here (paths inside the reference project):
+ *   Hybrid2D/src/Hybrid_Sub.f90          the commented GSIS coupling :45-153, getNSF :617-654
+ *   Hybrid2D/src/sub_NS_singlegrid.f90   NS_Time_advance_LU_SGS, comput_duvtpckw, comput_dt, comput_Lvc
+ *   Hybrid2D/src/sub_Residual.f90        Residual_FVM, scheme_fP/fm, get_viscous
+ *   Hybrid2D/src/sub_flux_split.f90      Flux_Van_Leer_1Da, Flux_steger_warming_1Da
+ *   Hybrid2D/src/sub_LU_SGS.f90          du_LU_SGS_2D, comput_DFn
+ *   Hybrid2D/src/IO.f90                  get_res :286-303
+ *
+ * Restated semantics.  The reference's coupling block is commented out; taken
+ * literally (NS started from its previous solution plus the kinetic
+ * increment, the moments replaced by the NS change) its fixed point is not
+ * the kinetic one: on a closed Couette channel the band-limited NS solution
+ * does not conserve mass, the collision term then feeds a constant mass
+ * source into f and the kinetic residual stalls (about 7e-6 at Kn 0.1).  The
+ * synthetic equation is therefore made consistent with the kinetic one:
+ *   - R_K = moments 1-4 of the kinetic RHS of the current f with its own
+ *     equilibrium (RHSFDVsub + DETFP_res), in NS units
+ *     vol * k * (1, k, k, k^2/2), k = sqrt(2/gamma)/Ma (gamma = 5/3);
+ *   - source Q = R_K - R_NS(U_k), U_k = Convert_NS state of the kinetic
+ *     moments, on the band;
+ *   - NS+HoT started from U_k is iterated on R_NS(U) + Q until
+ *     max|Res(4)| over the band < inner_tol or max_inner iterations; the
+ *     band is cells 3..n-3 along wall-bounded axes (sub_NS_singlegrid.f90:
+ *     23-30) and every cell along a periodic axis;
+ *   - S(1:4) += the NS change of rho, u, v, T; S(5,6,7,10) += TaoNS_out and
+ *     S(8,9) += Q_out from getNSF, on the band cells (Hybrid_Sub.f90:121-149).
+ *   At a converged kinetic state R_K = 0, so U_k solves the synthetic
+ *   equation and the correction vanishes whatever the inner iteration count.
+ *   - The inner LU-SGS uses the reference's algebra (alpha, comput_DFn,
+ *     spectral radii) with a two-colour cell ordering: forward sweep red then
+ *     black, backward sweep black then red, dU reset to 0 at each inner
+ *     iteration.  HYB_ORC_LUSGS_PLANES=1 (gsis.reserved[0]) selects the
+ *     reference's anti-diagonal order instead.
+ */
+#include "hyb_oracle_impl.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_ns {
+    size_t nc;
+    double *U, *U2, *dU, *Res, *dt, *Lci, *Lcj, *Lvi, *Lvj;
+    double *rk, *src;                            /* kinetic residual moments, synthetic source [4][nc] */
+    double *d, *uu, *vv, *T, *p, *cc, *amu;
+    double *fluxi, *fluxj;                       /* [4][nc], faces at the C2 index of (i,j) */
+    double *ti_out, *qi_out, *tj_out, *qj_out;   /* NS stress at faces, no HoT */
+    int src_on;
+};
+
+#define NC(o) ((size_t)((o)->nx + 3) * ((o)->ny + 3))
+#define A4(arr, m, c) (arr)[(size_t)(m) * ns->nc + (c)]
+
+void orc_ns_free(orc *o)
+{
+    if (!o || !o->ns) return;
+    struct orc_ns *ns = o->ns;
+    double **ps[] = {&ns->U, &ns->rk, &ns->src, &ns->U2, &ns->dU, &ns->Res, &ns->dt, &ns->Lci, &ns->Lcj, &ns->Lvi, &ns->Lvj,
+                     &ns->d, &ns->uu, &ns->vv, &ns->T, &ns->p, &ns->cc, &ns->amu, &ns->fluxi, &ns->fluxj,
+                     &ns->ti_out, &ns->qi_out, &ns->tj_out, &ns->qj_out};
+    for (size_t k = 0; k < sizeof(ps) / sizeof(ps[0]); k++) free(*ps[k]);
+    free(ns);
+    o->ns = NULL;
+}
+
+static int ns_alloc(orc *o)
+{
+    if (o->ns) return HYB_OK;
+    struct orc_ns *ns = (struct orc_ns *)calloc(1, sizeof(struct orc_ns));
+    if (!ns) return HYB_ERR_NOMEM;
+    size_t nc = NC(o);
+    ns->nc = nc;
+    ns->U = calloc(4 * nc, sizeof(double));
+    ns->rk = calloc(4 * nc, sizeof(double)); ns->src = calloc(4 * nc, sizeof(double));
+    ns->U2 = calloc(4 * nc, sizeof(double)); ns->dU = calloc(4 * nc, sizeof(double));
+    ns->Res = calloc(4 * nc, sizeof(double)); ns->dt = calloc(nc, sizeof(double));
+    ns->Lci = calloc(nc, sizeof(double)); ns->Lcj = calloc(nc, sizeof(double));
+    ns->Lvi = calloc(nc, sizeof(double)); ns->Lvj = calloc(nc, sizeof(double));
+    ns->d = calloc(nc, sizeof(double)); ns->uu = calloc(nc, sizeof(double)); ns->vv = calloc(nc, sizeof(double));
+    ns->T = calloc(nc, sizeof(double)); ns->p = calloc(nc, sizeof(double)); ns->cc = calloc(nc, sizeof(double));
+    ns->amu = calloc(nc, sizeof(double));
+    ns->fluxi = calloc(4 * nc, sizeof(double)); ns->fluxj = calloc(4 * nc, sizeof(double));
+    ns->ti_out = calloc(4 * nc, sizeof(double)); ns->qi_out = calloc(2 * nc, sizeof(double));
+    ns->tj_out = calloc(4 * nc, sizeof(double)); ns->qj_out = calloc(2 * nc, sizeof(double));
+    o->ns = ns;
+    if (!ns->qj_out || !ns->rk || !ns->src) { orc_ns_free(o); return HYB_ERR_NOMEM; }
+    return HYB_OK;
+}
+
+int orc_gsis_configure(orc *o, const hyb_gsis_params *gp)
+{
+    if (!o || !gp) return HYB_ERR_INVALID;
+    if (gp->enable && fabs(o->prm.gamma - 5.0 / 3.0) > 1e-9) return HYB_ERR_UNSUPPORTED;
+    o->gsis = *gp;
+    if (gp->enable) return ns_alloc(o);
+    return HYB_OK;
+}
+
+int orc_gsis_last_inner(orc *o) { return o->gsis_last_inner; }
+
+/* band of cells the synthetic solve updates */
+static void band(const orc *o, int *ilo, int *ihi, int *jlo, int *jhi)
+{
+    if (o->bc[0] == HYB_BC_PERIODIC) { *ilo = 1; *ihi = o->nx - 1; } else { *ilo = 3; *ihi = o->nx - 3; }
+    if (o->bc[1] == HYB_BC_PERIODIC) { *jlo = 1; *jhi = o->ny - 1; } else { *jlo = 3; *jhi = o->ny - 3; }
+}
+
+/* periodic ghost U from the band (the inner-boundary exchange of the NS
+ * solver, update_buffer_onemesh, for a block connected to itself) */
+static void ns_periodic_ghosts(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const int nx = o->nx, ny = o->ny;
+    if (o->bc[0] == HYB_BC_PERIODIC)
+        for (int j = -1; j <= ny + 1; j++)
+            for (int m = 0; m < 4; m++) {
+                A4(ns->U, m, C2(o, 0, j)) = A4(ns->U, m, C2(o, nx - 1, j));
+                A4(ns->U, m, C2(o, -1, j)) = A4(ns->U, m, C2(o, nx - 2, j));
+                A4(ns->U, m, C2(o, nx, j)) = A4(ns->U, m, C2(o, 1, j));
+                A4(ns->U, m, C2(o, nx + 1, j)) = A4(ns->U, m, C2(o, 2, j));
+            }
+    if (o->bc[1] == HYB_BC_PERIODIC)
+        for (int i = -1; i <= nx + 1; i++)
+            for (int m = 0; m < 4; m++) {
+                A4(ns->U, m, C2(o, i, 0)) = A4(ns->U, m, C2(o, i, ny - 1));
+                A4(ns->U, m, C2(o, i, -1)) = A4(ns->U, m, C2(o, i, ny - 2));
+                A4(ns->U, m, C2(o, i, ny)) = A4(ns->U, m, C2(o, i, 1));
+                A4(ns->U, m, C2(o, i, ny + 1)) = A4(ns->U, m, C2(o, i, 2));
+            }
+}
+
+/* minmod of sub_Residual.f90:357-368 */
+static double minmod_ns(double a, double b)
+{
+    if (a * b <= 0.0) return 0.0;
+    return (fabs(a) <= fabs(b)) ? a : b;
+}
+
+/* scheme_fP / scheme_fm, NND2 (sub_Residual.f90:490-491, 526-527) */
+static void recon_nnd(double u1, double u2, double u3, double u4, double *ul, double *ur)
+{
+    *ul = u2 + 0.5 * minmod_ns(u2 - u1, u3 - u2);
+    *ur = u3 - 0.5 * minmod_ns(u3 - u2, u4 - u3);
+}
+
+/* Flux_Van_Leer_1Da (sub_flux_split.f90:141-192), Q = (d, un, ut, p) */
+static void flux_van_leer(const double *QL, const double *QR, double *F, double g)
+{
+    double dl = QL[0], ul = QL[1], vl = QL[2], pl = QL[3];
+    double dr = QR[0], ur = QR[1], vr = QR[2], pr = QR[3];
+    double al = sqrt(g * pl / dl), ar = sqrt(g * pr / dr);
+    double Ml = ul / al, Mr = ur / ar;
+    double fp[4], fm[4];
+    if (Ml >= 1.0) {
+        fp[0] = dl * ul; fp[1] = dl * ul * ul + pl; fp[2] = dl * ul * vl;
+        fp[3] = ul * (g * pl / (g - 1.0) + 0.5 * dl * (ul * ul + vl * vl));
+    } else if (fabs(Ml) < 1.0) {
+        double Mp = 0.25 * (1.0 + Ml) * (1.0 + Ml), t0 = dl * al * Mp;
+        fp[0] = t0;
+        fp[1] = t0 * ((g - 1.0) * ul + 2.0 * al) / g;
+        fp[2] = t0 * vl;
+        fp[3] = t0 * (((g - 1.0) * ul + 2.0 * al) * ((g - 1.0) * ul + 2.0 * al) * 0.5 / (g * g - 1.0) + 0.5 * (vl * vl));
+    } else {
+        fp[0] = fp[1] = fp[2] = fp[3] = 0.0;
+    }
+    if (Mr >= 1.0) {
+        fm[0] = fm[1] = fm[2] = fm[3] = 0.0;
+    } else if (fabs(Mr) < 1.0) {
+        double Mm = -0.25 * (Mr - 1.0) * (Mr - 1.0), t0 = dr * ar * Mm;
+        fm[0] = t0;
+        fm[1] = t0 * ((g - 1.0) * ur - 2.0 * ar) / g;
+        fm[2] = t0 * vr;
+        fm[3] = t0 * (((g - 1.0) * ur - 2.0 * ar) * ((g - 1.0) * ur - 2.0 * ar) * 0.5 / (g * g - 1.0) + 0.5 * (vr * vr));
+    } else {
+        fm[0] = dr * ur; fm[1] = dr * ur * ur + pr; fm[2] = dr * ur * vr;
+        fm[3] = ur * (g * pr / (g - 1.0) + 0.5 * dr * (ur * ur + vr * vr));
+    }
+    for (int k = 0; k < 4; k++) F[k] = fp[k] + fm[k];
+}
+
+/* comput_duvtpckw (sub_NS_singlegrid.f90:121-157) + get_viscous */
+static int ns_prims(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const int nx = o->nx, ny = o->ny;
+    const double gam = o->prm.gamma, ma = o->prm.ma, cv = 1.0 / (gam * (gam - 1.0) * ma * ma);
+    const double ptmp = 1.0 / (gam * ma * ma);
+    for (int j = -1; j <= ny + 1; j++)
+        for (int i = -1; i <= nx + 1; i++) {
+            size_t c = C2(o, i, j);
+            double d = A4(ns->U, 0, c);
+            double u = A4(ns->U, 1, c) / d, v = A4(ns->U, 2, c) / d;
+            double t = (A4(ns->U, 3, c) - 0.5 * d * (u * u + v * v)) / (cv * d);
+            ns->d[c] = d; ns->uu[c] = u; ns->vv[c] = v; ns->T[c] = t; ns->p[c] = ptmp * d * t;
+        }
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+            size_t c = C2(o, i, j);
+            if (ns->T[c] < 0.1) return HYB_ERR_TEMPERATURE;
+            ns->cc[c] = sqrt(ns->T[c]) / ma;
+        }
+    for (int j = 0; j <= ny; j++)
+        for (int i = 0; i <= nx; i++) ns->amu[C2(o, i, j)] = 1.0 / o->prm.re * pow(ns->T[C2(o, i, j)], o->prm.omega_ns);
+    return HYB_OK;
+}
+
+/* Residual_FVM (sub_Residual.f90:38-354) with Reconst_Original + NND2 and the
+ * Van Leer splitting; the HoT of Convert_NS is added to tau and q */
+static void ns_residual(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const int nx = o->nx, ny = o->ny;
+    const double gam = o->prm.gamma, ma = o->prm.ma, pr = o->prm.pr;
+    const double cv = 1.0 / (gam * (gam - 1.0) * ma * ma), cp = cv * gam;
+    const int perx = (o->bc[0] == HYB_BC_PERIODIC), pery = (o->bc[1] == HYB_BC_PERIODIC);
+    for (int dir = 0; dir < 2; dir++) {
+        int ni = dir == 0 ? nx : nx - 1, nj = dir == 0 ? ny - 1 : ny;
+        for (int j = 1; j <= nj; j++)
+            for (int i = 1; i <= ni; i++) {
+                double s, n1, n2;
+                int im2, jm2, im1, jm1, ip1, jp1;   /* stencil cells k-2, k-1, k, k+1 */
+                if (dir == 0) {
+                    s = o->si[MI(o, i, j)]; n1 = o->ni1[MI(o, i, j)]; n2 = o->ni2[MI(o, i, j)];
+                    im2 = i - 2; im1 = i - 1; ip1 = i + 1; jm2 = jm1 = jp1 = j;
+                } else {
+                    s = o->sj[MI(o, i, j)]; n1 = o->nj1[MI(o, i, j)]; n2 = o->nj2[MI(o, i, j)];
+                    jm2 = j - 2; jm1 = j - 1; jp1 = j + 1; im2 = im1 = ip1 = i;
+                }
+                size_t c0 = C2(o, im2, jm2), c1 = C2(o, im1, jm1), c2 = C2(o, i, j), c3 = C2(o, ip1, jp1);
+                double UL[4], UR[4];
+                const double *vars[4] = {ns->d, ns->uu, ns->vv, ns->p};
+                for (int m = 0; m < 4; m++)
+                    recon_nnd(vars[m][c0], vars[m][c1], vars[m][c2], vars[m][c3], &UL[m], &UR[m]);
+                double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+                double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+                double F0[4];
+                flux_van_leer(QL, QR, F0, gam);
+                double *Fx = dir == 0 ? ns->fluxi : ns->fluxj;
+                size_t cf = C2(o, i, j);
+                A4(Fx, 0, cf) = -F0[0] * s;
+                A4(Fx, 1, cf) = -(F0[1] * n1 - F0[2] * n2) * s;
+                A4(Fx, 2, cf) = -(F0[1] * n2 + F0[2] * n1) * s;
+                A4(Fx, 3, cf) = -F0[3] * s;
+                /* viscous part, identical geometry to Convert_NS */
+                int lo, hi;
+                double amu1, amk1, dix, diy, djx, djy, diu, div, dit, dju, djv, djt;
+                const double *x1 = o->x1, *y1 = o->y1, *uu = ns->uu, *vv = ns->vv, *T = ns->T, *amu = ns->amu;
+                if (dir == 0) {
+                    lo = (i == 1) && !perx; hi = (i == nx) && !perx;
+                    if (lo) { amu1 = amu[C2(o, i, j)]; amk1 = cp * (amu[C2(o, i, j)] / pr); }
+                    else if (hi) { amu1 = amu[C2(o, i - 1, j)]; amk1 = cp * (amu[C2(o, i - 1, j)] / pr); }
+                    else { amu1 = (amu[C2(o, i - 1, j)] + amu[C2(o, i, j)]) * 0.5;
+                           amk1 = cp * ((amu[C2(o, i - 1, j)] + amu[C2(o, i, j)]) / pr) * 0.5; }
+                    dix = x1[C2(o, i, j)] - x1[C2(o, i - 1, j)];
+                    diy = y1[C2(o, i, j)] - y1[C2(o, i - 1, j)];
+                    djx = (x1[C2(o, i - 1, j + 1)] + x1[C2(o, i, j + 1)] - x1[C2(o, i - 1, j - 1)] - x1[C2(o, i, j - 1)]) * 0.25;
+                    djy = (y1[C2(o, i - 1, j + 1)] + y1[C2(o, i, j + 1)] - y1[C2(o, i - 1, j - 1)] - y1[C2(o, i, j - 1)]) * 0.25;
+                    diu = uu[C2(o, i, j)] - uu[C2(o, i - 1, j)];
+                    div = vv[C2(o, i, j)] - vv[C2(o, i - 1, j)];
+                    dit = T[C2(o, i, j)] - T[C2(o, i - 1, j)];
+                    dju = (uu[C2(o, i - 1, j + 1)] + uu[C2(o, i, j + 1)] - uu[C2(o, i - 1, j - 1)] - uu[C2(o, i, j - 1)]) * 0.25;
+                    djv = (vv[C2(o, i - 1, j + 1)] + vv[C2(o, i, j + 1)] - vv[C2(o, i - 1, j - 1)] - vv[C2(o, i, j - 1)]) * 0.25;
+                    djt = (T[C2(o, i - 1, j + 1)] + T[C2(o, i, j + 1)] - T[C2(o, i - 1, j - 1)] - T[C2(o, i, j - 1)]) * 0.25;
+                } else {
+                    lo = (j == 1) && !pery; hi = (j == ny) && !pery;
+                    if (lo) { amu1 = amu[C2(o, i, j)]; amk1 = cp * (amu[C2(o, i, j)] / pr); }
+                    else if (hi) { amu1 = amu[C2(o, i, j - 1)]; amk1 = cp * (amu[C2(o, i, j - 1)] / pr); }
+                    else { amu1 = (amu[C2(o, i, j)] + amu[C2(o, i, j - 1)]) * 0.5;
+                           amk1 = cp * ((amu[C2(o, i, j - 1)] + amu[C2(o, i, j)]) / pr) * 0.5; }
+                    dix = (x1[C2(o, i + 1, j - 1)] + x1[C2(o, i + 1, j)] - x1[C2(o, i - 1, j - 1)] - x1[C2(o, i - 1, j)]) * 0.25;
+                    diy = (y1[C2(o, i + 1, j - 1)] + y1[C2(o, i + 1, j)] - y1[C2(o, i - 1, j - 1)] - y1[C2(o, i - 1, j)]) * 0.25;
+                    djx = x1[C2(o, i, j)] - x1[C2(o, i, j - 1)];
+                    djy = y1[C2(o, i, j)] - y1[C2(o, i, j - 1)];
+                    diu = (uu[C2(o, i + 1, j - 1)] + uu[C2(o, i + 1, j)] - uu[C2(o, i - 1, j - 1)] - uu[C2(o, i - 1, j)]) * 0.25;
+                    div = (vv[C2(o, i + 1, j - 1)] + vv[C2(o, i + 1, j)] - vv[C2(o, i - 1, j - 1)] - vv[C2(o, i - 1, j)]) * 0.25;
+                    dit = (T[C2(o, i + 1, j - 1)] + T[C2(o, i + 1, j)] - T[C2(o, i - 1, j - 1)] - T[C2(o, i - 1, j)]) * 0.25;
+                    dju = uu[C2(o, i, j)] - uu[C2(o, i, j - 1)];
+                    djv = vv[C2(o, i, j)] - vv[C2(o, i, j - 1)];
+                    djt = T[C2(o, i, j)] - T[C2(o, i, j - 1)];
+                }
+                double ds = 1.0 / (dix * djy - djx * diy);
+                double ux = (diu * djy - dju * diy) * ds, vx = (div * djy - djv * diy) * ds, tx = (dit * djy - djt * diy) * ds;
+                double uy = (-diu * djx + dju * dix) * ds, vy = (-div * djx + djv * dix) * ds, ty = (-dit * djx + djt * dix) * ds;
+                double u1, v1;
+                if (dir == 0) { u1 = (uu[C2(o, i, j)] + uu[C2(o, i - 1, j)]) * 0.5; v1 = (vv[C2(o, i, j)] + vv[C2(o, i - 1, j)]) * 0.5; }
+                else { u1 = (uu[C2(o, i, j)] + uu[C2(o, i, j - 1)]) * 0.5; v1 = (vv[C2(o, i, j)] + vv[C2(o, i, j - 1)]) * 0.5; }
+                double t11 = ((4.0 / 3.0) * ux - (2.0 / 3.0) * vy) * amu1;
+                double t22 = ((4.0 / 3.0) * vy - (2.0 / 3.0) * ux) * amu1;
+                double t12 = (uy + vx) * amu1;
+                double t33 = amu1 * (-(2.0 / 3.0) * ux - (2.0 / 3.0) * vy);
+                double qx = amk1 * tx, qy = amk1 * ty;
+                double *to = dir == 0 ? ns->ti_out : ns->tj_out, *qo = dir == 0 ? ns->qi_out : ns->qj_out;
+                A4(to, 0, cf) = t11; A4(to, 1, cf) = t22; A4(to, 2, cf) = t12; A4(to, 3, cf) = t33;
+                qo[0 * ns->nc + cf] = qx; qo[1 * ns->nc + cf] = qy;
+                const double *tg = dir == 0 ? o->tao_i_g : o->tao_j_g, *qg = dir == 0 ? o->q_i_g : o->q_j_g;
+                t11 = t11 + tg[cf * 4 + 0];
+                t22 = t22 + tg[cf * 4 + 1];
+                t12 = t12 + tg[cf * 4 + 2];
+                t33 = t33 + tg[cf * 4 + 3];
+                qx = qx + qg[cf * 2 + 0];
+                qy = qy + qg[cf * 2 + 1];
+                (void)t33;
+                double E1 = u1 * t11 + v1 * t12 + qx, E2 = u1 * t12 + v1 * t22 + qy;
+                A4(Fx, 1, cf) = A4(Fx, 1, cf) + (t11 * n1 + t12 * n2) * s;
+                A4(Fx, 2, cf) = A4(Fx, 2, cf) + (t12 * n1 + t22 * n2) * s;
+                A4(Fx, 3, cf) = A4(Fx, 3, cf) + (E1 * n1 + E2 * n2) * s;
+            }
+    }
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++)
+            for (int m = 0; m < 4; m++)
+                A4(ns->Res, m, C2(o, i, j)) = A4(ns->fluxi, m, C2(o, i + 1, j)) - A4(ns->fluxi, m, C2(o, i, j)) +
+                                              A4(ns->fluxj, m, C2(o, i, j + 1)) - A4(ns->fluxj, m, C2(o, i, j));
+}
+
+/* comput_Lvc and comput_dt (sub_NS_singlegrid.f90:160-221), local time step */
+static void ns_lvc_dt(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const int nx = o->nx, ny = o->ny;
+    const double gam = o->prm.gamma, pr = o->prm.pr;
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+            size_t c = C2(o, i, j);
+            double s0 = o->vol[MI(o, i, j)];
+            double si = 0.5 * (o->si[MI(o, i, j)] + o->si[MI(o, i + 1, j)]);
+            double n1 = 0.5 * (o->ni1[MI(o, i, j)] + o->ni1[MI(o, i + 1, j)]);
+            double n2 = 0.5 * (o->ni2[MI(o, i, j)] + o->ni2[MI(o, i + 1, j)]);
+            double sj = 0.5 * (o->sj[MI(o, i, j)] + o->sj[MI(o, i, j + 1)]);
+            double m1 = 0.5 * (o->nj1[MI(o, i, j)] + o->nj1[MI(o, i, j + 1)]);
+            double m2 = 0.5 * (o->nj2[MI(o, i, j)] + o->nj2[MI(o, i, j + 1)]);
+            double uni = ns->uu[c] * n1 + ns->vv[c] * n2, unj = ns->uu[c] * m1 + ns->vv[c] * m2;
+            ns->Lci[c] = (fabs(uni) + ns->cc[c]) * si;
+            ns->Lcj[c] = (fabs(unj) + ns->cc[c]) * sj;
+            double tmp1 = gam / ns->d[c] * (ns->amu[c] / pr);
+            ns->Lvi[c] = tmp1 * si * si / s0;
+            ns->Lvj[c] = tmp1 * sj * sj / s0;
+            double dt = o->gsis.cfl * s0 / (ns->Lci[c] + ns->Lcj[c] + 1.0 * (ns->Lvi[c] + ns->Lvj[c]));
+            if (dt > o->gsis.dtmax) dt = o->gsis.dtmax;
+            if (dt < o->gsis.dtmin) dt = o->gsis.dtmin;
+            ns->dt[c] = dt;
+        }
+}
+
+/* comput_DFn (sub_LU_SGS.f90:122-144) */
+static void dfn(const double *U, const double *dU, double n1, double n2, double g, double *DF)
+{
+    double U2[4];
+    for (int m = 0; m < 4; m++) U2[m] = U[m] + dU[m];
+    double un1 = (U[1] * n1 + U[2] * n2) / U[0];
+    double p1 = (g - 1.0) * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]);
+    double un2 = (U2[1] * n1 + U2[2] * n2) / U2[0];
+    double p2 = (g - 1.0) * (U2[3] - 0.5 * (U2[1] * U2[1] + U2[2] * U2[2]) / U2[0]);
+    DF[0] = U2[0] * un2 - U[0] * un1;
+    DF[1] = (U2[1] * un2 + p2 * n1) - (U[1] * un1 + p1 * n1);
+    DF[2] = (U2[2] * un2 + p2 * n2) - (U[2] * un1 + p1 * n2);
+    DF[3] = (U2[3] + p2) * un2 - (U[3] + p1) * un1;
+}
+
+static void get4(const struct orc_ns *ns, const double *a, size_t c, double *out)
+{
+    for (int m = 0; m < 4; m++) out[m] = a[(size_t)m * ns->nc + c];
+}
+
+/* forward element of du_LU_SGS_2D at (i,j) (sub_LU_SGS.f90:33-65) */
+static void lusgs_fwd_cell(orc *o, int i, int j, int ilo, int jlo)
+{
+    struct orc_ns *ns = o->ns;
+    const double g = o->prm.gamma, w = 1.0;
+    size_t c = C2(o, i, j);
+    double alfa = o->vol[MI(o, i, j)] / ns->dt[c] + w * (ns->Lci[c] + ns->Lcj[c]);
+    alfa = alfa + 2.0 * (ns->Lvi[c] + ns->Lvj[c]);
+    double dui[4] = {0, 0, 0, 0}, duj[4] = {0, 0, 0, 0}, Un[4], dUn[4], DF[4];
+    if (i != ilo) {
+        size_t cn = C2(o, i - 1, j);
+        get4(ns, ns->U, cn, Un); get4(ns, ns->dU, cn, dUn);
+        dfn(Un, dUn, o->ni1[MI(o, i, j)], o->ni2[MI(o, i, j)], g, DF);
+        for (int m = 0; m < 4; m++)
+            dui[m] = 0.5 * (DF[m] * o->si[MI(o, i, j)] + w * ns->Lci[cn] * dUn[m]) + ns->Lvi[cn] * dUn[m];
+    }
+    if (j != jlo) {
+        size_t cn = C2(o, i, j - 1);
+        get4(ns, ns->U, cn, Un); get4(ns, ns->dU, cn, dUn);
+        dfn(Un, dUn, o->nj1[MI(o, i, j)], o->nj2[MI(o, i, j)], g, DF);
+        for (int m = 0; m < 4; m++)
+            duj[m] = 0.5 * (DF[m] * o->sj[MI(o, i, j)] + w * ns->Lcj[cn] * dUn[m]) + ns->Lvj[cn] * dUn[m];
+    }
+    for (int m = 0; m < 4; m++) A4(ns->dU, m, c) = (A4(ns->Res, m, c) + dui[m] + duj[m]) / alfa;
+}
+
+/* backward element (sub_LU_SGS.f90:76-107) */
+static void lusgs_bwd_cell(orc *o, int i, int j, int ihi, int jhi)
+{
+    struct orc_ns *ns = o->ns;
+    const double g = o->prm.gamma, w = 1.0;
+    size_t c = C2(o, i, j);
+    double alfa = o->vol[MI(o, i, j)] / ns->dt[c] + w * (ns->Lci[c] + ns->Lcj[c]);
+    alfa = alfa + 2.0 * (ns->Lvi[c] + ns->Lvj[c]);
+    double dui[4] = {0, 0, 0, 0}, duj[4] = {0, 0, 0, 0}, Un[4], dUn[4], DF[4];
+    if (i != ihi) {
+        size_t cn = C2(o, i + 1, j);
+        get4(ns, ns->U, cn, Un); get4(ns, ns->dU, cn, dUn);
+        dfn(Un, dUn, o->ni1[MI(o, i, j)], o->ni2[MI(o, i, j)], g, DF);
+        for (int m = 0; m < 4; m++)
+            dui[m] = -0.5 * (DF[m] * o->si[MI(o, i + 1, j)] - w * ns->Lci[cn] * dUn[m]) + ns->Lvi[cn] * dUn[m];
+    }
+    if (j != jhi) {
+        size_t cn = C2(o, i, j + 1);
+        get4(ns, ns->U, cn, Un); get4(ns, ns->dU, cn, dUn);
+        dfn(Un, dUn, o->nj1[MI(o, i, j)], o->nj2[MI(o, i, j)], g, DF);
+        for (int m = 0; m < 4; m++)
+            duj[m] = -0.5 * (DF[m] * o->sj[MI(o, i, j + 1)] - w * ns->Lcj[cn] * dUn[m]) + ns->Lvj[cn] * dUn[m];
+    }
+    for (int m = 0; m < 4; m++) A4(ns->dU, m, c) = A4(ns->dU, m, c) + (dui[m] + duj[m]) / alfa;
+}
+
+static void ns_lusgs(orc *o, int ilo, int ihi, int jlo, int jhi)
+{
+    struct orc_ns *ns = o->ns;
+    if (o->gsis.reserved[0] == 1) {   /* reference anti-diagonal order */
+        for (int plane = ilo + jlo; plane <= ihi + jhi; plane++)
+            for (int j = jlo; j <= jhi; j++) {
+                int i = plane - j;
+                if (i < ilo || i > ihi) continue;
+                lusgs_fwd_cell(o, i, j, ilo, jlo);
+            }
+        for (int plane = ihi + jhi; plane >= ilo + jlo; plane--)
+            for (int j = jhi; j >= jlo; j--) {
+                int i = plane - j;
+                if (i < ilo || i > ihi) continue;
+                lusgs_bwd_cell(o, i, j, ihi, jhi);
+            }
+        return;
+    }
+    memset(ns->dU, 0, 4 * ns->nc * sizeof(double));
+    for (int col = 0; col < 2; col++)
+        for (int j = jlo; j <= jhi; j++)
+            for (int i = ilo; i <= ihi; i++)
+                if (((i + j) & 1) == col) lusgs_fwd_cell(o, i, j, ilo, jlo);
+    for (int col = 1; col >= 0; col--)
+        for (int j = jlo; j <= jhi; j++)
+            for (int i = ilo; i <= ihi; i++)
+                if (((i + j) & 1) == col) lusgs_bwd_cell(o, i, j, ihi, jhi);
+}
+
+/* NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:4-40); returns the max
+ * |Res(4)| over the band before the update (get_res, IO.f90:286-303) */
+static int ns_advance(orc *o, double *res4)
+{
+    struct orc_ns *ns = o->ns;
+    int ilo, ihi, jlo, jhi;
+    band(o, &ilo, &ihi, &jlo, &jhi);
+    int rc = ns_prims(o);
+    if (rc) return rc;
+    ns_residual(o);
+    if (ns->src_on)
+        for (int j = jlo; j <= jhi; j++)
+            for (int i = ilo; i <= ihi; i++)
+                for (int m = 0; m < 4; m++) A4(ns->Res, m, C2(o, i, j)) += A4(ns->src, m, C2(o, i, j));
+    double rmax = 0.0;
+    for (int j = jlo; j <= jhi; j++)
+        for (int i = ilo; i <= ihi; i++) {
+            double r = fabs(A4(ns->Res, 3, C2(o, i, j)));
+            if (r > rmax || r != r) rmax = r;
+        }
+    *res4 = rmax;
+    ns_lvc_dt(o);
+    ns_lusgs(o, ilo, ihi, jlo, jhi);
+    for (int j = jlo; j <= jhi; j++)
+        for (int i = ilo; i <= ihi; i++)
+            for (int m = 0; m < 4; m++) A4(ns->U, m, C2(o, i, j)) += A4(ns->dU, m, C2(o, i, j));
+    ns_periodic_ghosts(o);
+    return HYB_OK;
+}
+
+static void prim_ns(const double *U4, size_t nc, size_t c, double cv, double *r, double *u, double *v, double *t)
+{
+    double d = U4[c], uu = U4[nc + c] / d, vv = U4[2 * nc + c] / d;
+    *r = d; *u = uu; *v = vv;
+    *t = (U4[3 * nc + c] - 0.5 * d * (uu * uu + vv * vv)) / (cv * d);
+}
+
+/* the synthetic solve of one outer iteration (Hybrid_Sub.f90:45-153 with the
+ * consistent source described at the top of this file) */
+int orc_gsis_solve(orc *o)
+{
+    int rc = ns_alloc(o);
+    if (rc) return rc;
+    struct orc_ns *ns = o->ns;
+    const double gam = o->prm.gamma, ma = o->prm.ma, cv = 1.0 / (gam * (gam - 1.0) * ma * ma);
+    const double kin2ns = sqrt(2.0 / gam) / ma;     /* u_NS = u_kin sqrt(2/gamma)/Ma */
+    int ilo, ihi, jlo, jhi;
+    band(o, &ilo, &ihi, &jlo, &jhi);
+    /* kinetic residual of the current f; the wall ghosts are refreshed first
+     * (the next step's boundary call recomputes the same values) */
+    orc_exchange_f(o);
+    orc_phy_boundary(o);
+    rc = orc_kinetic_residual_moments(o, ns->rk);
+    if (rc) return rc;
+    /* NS state of the kinetic moments (Convert_NS) */
+    double *Uk = (double *)calloc(NC(o) * 4, sizeof(double));
+    if (!Uk) return HYB_ERR_NOMEM;
+    orc_build_u(o, Uk);   /* AoS [c][4] */
+    for (size_t c = 0; c < ns->nc; c++)
+        for (int m = 0; m < 4; m++) A4(ns->U, m, c) = Uk[c * 4 + m];
+    free(Uk);
+    ns_periodic_ghosts(o);
+    memcpy(ns->U2, ns->U, 4 * ns->nc * sizeof(double));
+    /* source Q = R_K - R_NS(U_k) on the band */
+    rc = ns_prims(o);
+    if (rc) return rc;
+    ns_residual(o);
+    const double sc[4] = {kin2ns, kin2ns * kin2ns, kin2ns * kin2ns, 0.5 * kin2ns * kin2ns * kin2ns};
+    memset(ns->src, 0, 4 * ns->nc * sizeof(double));
+    for (int j = jlo; j <= jhi; j++)
+        for (int i = ilo; i <= ihi; i++) {
+            size_t c = C2(o, i, j);
+            double vol = o->vol[MI(o, i, j)];
+            for (int m = 0; m < 4; m++) A4(ns->src, m, c) = vol * sc[m] * A4(ns->rk, m, c) - A4(ns->Res, m, c);
+        }
+    ns->src_on = 1;
+    int it = 0;
+    double res = 1.0, tol = o->gsis.inner_tol;
+    const int maxit = o->gsis.max_inner > 0 ? o->gsis.max_inner : 2000;
+    while (res > tol && it < maxit) {
+        rc = ns_advance(o, &res);
+        if (rc) { ns->src_on = 0; return rc; }
+        if (it == 0 && o->gsis.inner_rtol * res > tol) tol = o->gsis.inner_rtol * res;
+        it++;
+    }
+    ns->src_on = 0;
+    o->gsis_last_inner = it;
+    /* the band's Dirichlet edges make the NS density change non-conservative;
+     * its volume-weighted mean is removed so that the correction adds no mass */
+    double lam = 0.0;
+    if (o->gsis.reserved[1] == 0) {
+        double num = 0.0, den = 0.0;
+        for (int j = jlo; j <= jhi; j++)
+            for (int i = ilo; i <= ihi; i++) {
+                double vol = o->vol[MI(o, i, j)];
+                num += vol * (A4(ns->U, 0, C2(o, i, j)) - A4(ns->U2, 0, C2(o, i, j)));
+                den += vol;
+            }
+        lam = num / den;
+    }
+    /* correction of the moments, with getNSF (Hybrid_Sub.f90:617-654) */
+    const double g2 = gam * ma * ma, q2 = pow(ma, 3) * pow(gam, 1.5) / sqrt(2.0);
+    for (int j = jlo; j <= jhi; j++)
+        for (int i = ilo; i <= ihi; i++) {
+            size_t c = C2(o, i, j);
+            double r, u, v, t, r2, u2, v2, t2;
+            prim_ns(ns->U, ns->nc, c, cv, &r, &u, &v, &t);
+            prim_ns(ns->U2, ns->nc, c, cv, &r2, &u2, &v2, &t2);
+            SG(o, 1, i, j) += r - r2 - lam;
+            SG(o, 2, i, j) += (u - u2) / kin2ns;
+            SG(o, 3, i, j) += (v - v2) / kin2ns;
+            SG(o, 4, i, j) += t - t2;
+            size_t ci1 = C2(o, i + 1, j), cj1 = C2(o, i, j + 1);
+            double tao[4], q[2];
+            for (int k = 0; k < 4; k++) {
+                double out = 0.25 * (A4(ns->ti_out, k, c) + A4(ns->tj_out, k, c) + A4(ns->ti_out, k, ci1) +
+                                     A4(ns->tj_out, k, cj1));
+                double in = 0.25 * (o->tao_i_in[c * 4 + k] + o->tao_j_in[c * 4 + k] + o->tao_i_in[ci1 * 4 + k] +
+                                    o->tao_j_in[cj1 * 4 + k]);
+                tao[k] = -1.0 * (out - in) * g2;
+            }
+            for (int k = 0; k < 2; k++) {
+                double out = 0.25 * (ns->qi_out[k * ns->nc + c] + ns->qj_out[k * ns->nc + c] +
+                                     ns->qi_out[k * ns->nc + ci1] + ns->qj_out[k * ns->nc + cj1]);
+                double in = 0.25 * (o->q_i_in[c * 2 + k] + o->q_j_in[c * 2 + k] + o->q_i_in[ci1 * 2 + k] +
+                                    o->q_j_in[cj1 * 2 + k]);
+                q[k] = -1.0 * (out - in) * q2;
+            }
+            SG(o, 5, i, j) += tao[0];
+            SG(o, 6, i, j) += tao[1];
+            SG(o, 7, i, j) += tao[2];
+            SG(o, 10, i, j) += tao[3];
+            SG(o, 8, i, j) += q[0];
+            SG(o, 9, i, j) += q[1];
+        }
+    return HYB_OK;
+}
+
+/* NS state after the last synthetic solve, U[4][C2] */
+int orc_ns_state(orc *o, double *U)
+{
+    if (!o->ns) return HYB_ERR_INVALID;
+    memcpy(U, o->ns->U, 4 * o->ns->nc * sizeof(double));
+    return HYB_OK;
+}
+
+/* one NS residual evaluation on a given state (for kernel-level parity) */
+int orc_ns_residual(orc *o, const double *U, double *res)
+{
+    int rc = ns_alloc(o);
+    if (rc) return rc;
+    memcpy(o->ns->U, U, 4 * o->ns->nc * sizeof(double));
+    rc = ns_prims(o);
+    if (rc) return rc;
+    ns_residual(o);
+    memcpy(res, o->ns->Res, 4 * o->ns->nc * sizeof(double));
+    return HYB_OK;
+}

@@ -49,6 +49,10 @@ def lib():
         L.orc_grid_nc.argtypes = [ip, C.c_double, C.c_double, ip, dp, dp]
         L.orc_cfc_vhs.argtypes = [C.c_double] * 10 + [dp]
         L.orc_cfc_vhs.restype = C.c_double
+        L.orc_gsis_configure.argtypes = [vp, vp]
+        L.orc_gsis_last_inner.argtypes = [vp]
+        L.orc_ns_state.argtypes = [vp, dp]
+        L.orc_ns_residual.argtypes = [vp, dp, dp]
         _lib = L
     return _lib
 
@@ -144,6 +148,43 @@ class Oracle:
         ti, qi, tj, qj = np.zeros(4 * nc), np.zeros(2 * nc), np.zeros(4 * nc), np.zeros(2 * nc)
         self.L.orc_hot(self.h, _dp(ti), _dp(qi), _dp(tj), _dp(qj))
         return ti, qi, tj, qj
+
+    def gsis(self, **kw):
+        T = _types()
+        gp = T.HybGsisParams()
+        gp.enable = kw.get("enable", 1)
+        gp.max_inner = kw.get("max_inner", 2000)
+        gp.inner_tol = kw.get("inner_tol", 1e-6)
+        gp.inner_rtol = kw.get("inner_rtol", 0.0)
+        gp.cfl = kw.get("cfl", 20.0)
+        gp.dtmax = kw.get("dtmax", 10.0)
+        gp.dtmin = kw.get("dtmin", 1e-7)
+        gp.flux = kw.get("flux", 5)
+        gp.ns_scheme = kw.get("ns_scheme", 1)
+        gp.use_mlp = kw.get("use_mlp", 0)
+        gp.reserved[0] = kw.get("plane_order", 0)
+        gp.reserved[1] = kw.get("no_mass_projection", 0)
+        rc = self.L.orc_gsis_configure(self.h, C.byref(gp))
+        if rc != 0:
+            raise RuntimeError(f"orc_gsis_configure failed: {rc}")
+
+    def gsis_last_inner(self):
+        return self.L.orc_gsis_last_inner(self.h)
+
+    def ns_state(self):
+        nc = (self.nx + 3) * (self.ny + 3)
+        U = np.zeros(4 * nc)
+        self.L.orc_ns_state(self.h, _dp(U))
+        return U
+
+    def ns_residual(self, U):
+        nc = (self.nx + 3) * (self.ny + 3)
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        R = np.zeros(4 * nc)
+        rc = self.L.orc_ns_residual(self.h, _dp(U), _dp(R))
+        if rc != 0:
+            raise RuntimeError(f"orc_ns_residual failed: {rc}")
+        return R
 
     def err(self):
         return self.L.orc_err(self.h)
