@@ -150,7 +150,9 @@ class Solver:
         gp.flux = kw.get("flux", 5)
         gp.ns_scheme = kw.get("ns_scheme", 1)
         gp.use_mlp = kw.get("use_mlp", 0)
+        gp.ns_solver = kw.get("ns_solver", 0)
         gp.reserved[1] = kw.get("no_mass_projection", 0)
+        gp.reserved[2] = kw.get("correct_f", 0)
         self._ck(self.L.hyb_gsis_configure(self.h, C.byref(gp)), "gsis_configure")
 
     def gsis_last_inner(self):

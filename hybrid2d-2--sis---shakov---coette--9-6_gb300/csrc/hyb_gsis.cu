@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "hyb_common.cuh"
+#include "hyb_device.cuh"
 
 namespace hyb {
 
@@ -58,7 +59,9 @@ struct NsDev {
     double *U, *U2, *dU, *Res, *dt, *Lci, *Lcj, *Lvi, *Lvj;
     double *src;                                             // synthetic source Q [4][nc]
     const double *rk;                                        // kinetic RHS moments [4][Nb*PA]
-    int src_on, PA, scan_is_j, mass_proj;
+    int src_on, PA, scan_is_j, mass_proj, ns_scheme, correct_f;
+    double *sk;                                              // band moments before the correction [6][nc]
+    double *lin;                                             // line-solver scratch [16][nc]
     double *d, *uu, *vv, *T, *p, *cc, *amu;
     double *fluxi, *fluxj, *ti_out, *qi_out, *tj_out, *qj_out;
     const double *vol, *si, *sj, *ni1, *ni2, *nj1, *nj2;   // (nx,ny)
@@ -166,8 +169,16 @@ __global__ void k_ns_faces(NsDev D, int dir) {
     double UL[4], UR[4];
     for (int m = 0; m < 4; m++) {
         double u1 = vars[m][cs[0]], u2 = vars[m][cs[1]], u3 = vars[m][cs[2]], u4 = vars[m][cs[3]];
-        UL[m] = u2 + 0.5 * minmod_ns(u2 - u1, u3 - u2);
-        UR[m] = u3 - 0.5 * minmod_ns(u3 - u2, u4 - u3);
+        if (D.ns_scheme == 0) {
+            UL[m] = u2;
+            UR[m] = u3;
+        } else if (D.ns_scheme == 2) {   // upwind-biased stencil without the limiter
+            UL[m] = u2 + 0.25 * ((u2 - u1) + (u3 - u2));
+            UR[m] = u3 - 0.25 * ((u3 - u2) + (u4 - u3));
+        } else {                         // NND2, sub_Residual.f90:490-491, 526-527
+            UL[m] = u2 + 0.5 * minmod_ns(u2 - u1, u3 - u2);
+            UR[m] = u3 - 0.5 * minmod_ns(u3 - u2, u4 - u3);
+        }
     }
     double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
     double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
@@ -365,6 +376,148 @@ __global__ void k_ns_lusgs(NsDev D, int color, int bwd) {
     }
 }
 
+// ---- line-implicit ADI inner solve (no counterpart in the reference) -----
+// The matrix du_LU_SGS_2D factorises approximately, without the flux
+// differences of comput_DFn: diagonal alpha, couplings 0.5 Lc + Lv of the
+// neighbour.  Every j line is solved exactly (one thread per line and
+// variable), then every i line with the j-neighbour terms of the first half
+// on the right-hand side.  Band edges are Dirichlet; lines along a periodic
+// axis are cyclic (Sherman-Morrison).  Scratch D.lin: jt[4][nc], w[12][nc].
+
+__device__ __forceinline__ double alfa_ns(const NsDev &D, size_t c, int i, int j) {
+    return D.vol[mi(D, i, j)] / D.dt[c] + D.Lci[c] + D.Lcj[c] + 2.0 * (D.Lvi[c] + D.Lvj[c]);
+}
+
+// scalar (cyclic) Thomas of one line: b_k x_k - a_k x_{k-1} - c_k x_{k+1} = d_k.
+// Coefficients and right-hand side come from the functor; w: 3 scratch
+// arrays with the line's own stride.
+template <class Line>
+__device__ void tri_line(const Line &L, int n, bool cyclic, double *cp, double *dp, double *z, size_t ws) {
+    if (!cyclic || n < 3) {
+        double den = L.b(0);
+        cp[0] = -L.c(0) / den;
+        dp[0] = L.d(0) / den;
+        for (int k = 1; k < n; k++) {
+            const double ak = L.a(k);
+            den = L.b(k) + ak * cp[(size_t)(k - 1) * ws];
+            cp[(size_t)k * ws] = -L.c(k) / den;
+            dp[(size_t)k * ws] = (L.d(k) + ak * dp[(size_t)(k - 1) * ws]) / den;
+        }
+        L.x(n - 1, dp[(size_t)(n - 1) * ws]);
+        double xn = dp[(size_t)(n - 1) * ws];
+        for (int k = n - 2; k >= 0; k--) {
+            xn = dp[(size_t)k * ws] - cp[(size_t)k * ws] * xn;
+            L.x(k, xn);
+        }
+        return;
+    }
+    const double b0 = L.b(0), a0 = L.a(0), cn = L.c(n - 1);
+    const double gam = -b0;
+    double den = b0 - gam;
+    cp[0] = -L.c(0) / den;
+    dp[0] = L.d(0) / den;
+    z[0] = gam / den;
+    for (int k = 1; k < n; k++) {
+        const double ak = L.a(k);
+        const double bk = (k == n - 1) ? L.b(k) - (a0 * cn) / gam : L.b(k);
+        const double uk = (k == n - 1) ? -cn : 0.0;
+        den = bk + ak * cp[(size_t)(k - 1) * ws];
+        cp[(size_t)k * ws] = -L.c(k) / den;
+        dp[(size_t)k * ws] = (L.d(k) + ak * dp[(size_t)(k - 1) * ws]) / den;
+        z[(size_t)k * ws] = (uk + ak * z[(size_t)(k - 1) * ws]) / den;
+    }
+    for (int k = n - 2; k >= 0; k--) {
+        dp[(size_t)k * ws] -= cp[(size_t)k * ws] * dp[(size_t)(k + 1) * ws];
+        z[(size_t)k * ws] -= cp[(size_t)k * ws] * z[(size_t)(k + 1) * ws];
+    }
+    const double vy = dp[0] - a0 / gam * dp[(size_t)(n - 1) * ws];
+    const double vz = z[0] - a0 / gam * z[(size_t)(n - 1) * ws];
+    const double f = vy / (1.0 + vz);
+    for (int k = 0; k < n; k++) L.x(k, dp[(size_t)k * ws] - f * z[(size_t)k * ws]);
+}
+
+// line along j at column i, variable m: d1 -> dU
+struct JLine {
+    const NsDev *D;
+    int i, m;
+    bool per;
+    __device__ int jj(int k) const { return D->jlo + k; }
+    __device__ int wrap(int j) const { return j < D->jlo ? D->jhi : (j > D->jhi ? D->jlo : j); }
+    __device__ double b(int k) const { return alfa_ns(*D, c2(*D, i, jj(k)), i, jj(k)); }
+    __device__ double a(int k) const {
+        if (!per && k == 0) return 0.0;
+        size_t c = c2(*D, i, wrap(jj(k) - 1));
+        return 0.5 * D->Lcj[c] + D->Lvj[c];
+    }
+    __device__ double c(int k) const {
+        if (!per && jj(k) == D->jhi) return 0.0;
+        size_t c = c2(*D, i, wrap(jj(k) + 1));
+        return 0.5 * D->Lcj[c] + D->Lvj[c];
+    }
+    __device__ double d(int k) const { return D->Res[m * D->nc + c2(*D, i, jj(k))]; }
+    __device__ void x(int k, double v) const { D->dU[m * D->nc + c2(*D, i, jj(k))] = v; }
+};
+
+// j lines, then the j-neighbour terms of the i lines
+__global__ void k_ns_jlines(NsDev D) {
+    if (D.ctrl->done) return;
+    const int nb = D.ihi - D.ilo + 1, nj = D.jhi - D.jlo + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * nb) return;
+    const int i = D.ilo + t % nb, m = t / nb;
+    const bool per = D.pery != 0;
+    JLine L{&D, i, m, per};
+    double *w = D.lin + 4 * D.nc + (size_t)m * 3 * D.nc;
+    const size_t base = c2(D, i, D.jlo), ws = (size_t)(D.nx + 3);
+    tri_line(L, nj, per, w + base, w + D.nc + base, w + 2 * D.nc + base, ws);
+    double *jt = D.lin + (size_t)m * D.nc;
+    const double *du = D.dU + (size_t)m * D.nc;
+    for (int k = 0; k < nj; k++) {
+        const int j = D.jlo + k;
+        double v = 0.0;
+        if (per || j > D.jlo) v += L.a(k) * du[c2(D, i, L.wrap(j - 1))];
+        if (per || j < D.jhi) v += L.c(k) * du[c2(D, i, L.wrap(j + 1))];
+        jt[c2(D, i, j)] = v;
+    }
+}
+
+// line along i at row j, variable m; right-hand side Res + jt
+struct ILine {
+    const NsDev *D;
+    int j, m;
+    bool per;
+    __device__ int ii(int k) const { return D->ilo + k; }
+    __device__ int wrap(int i) const { return i < D->ilo ? D->ihi : (i > D->ihi ? D->ilo : i); }
+    __device__ double b(int k) const { return alfa_ns(*D, c2(*D, ii(k), j), ii(k), j); }
+    __device__ double a(int k) const {
+        if (!per && k == 0) return 0.0;
+        size_t c = c2(*D, wrap(ii(k) - 1), j);
+        return 0.5 * D->Lci[c] + D->Lvi[c];
+    }
+    __device__ double c(int k) const {
+        if (!per && ii(k) == D->ihi) return 0.0;
+        size_t c = c2(*D, wrap(ii(k) + 1), j);
+        return 0.5 * D->Lci[c] + D->Lvi[c];
+    }
+    __device__ double d(int k) const {
+        size_t c = c2(*D, ii(k), j);
+        return D->Res[m * D->nc + c] + D->lin[(size_t)m * D->nc + c];
+    }
+    __device__ void x(int k, double v) const { D->dU[m * D->nc + c2(*D, ii(k), j)] = v; }
+};
+
+__global__ void k_ns_ilines(NsDev D) {
+    if (D.ctrl->done) return;
+    const int nb = D.jhi - D.jlo + 1, ni = D.ihi - D.ilo + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * nb) return;
+    const int j = D.jlo + t % nb, m = t / nb;
+    ILine L{&D, j, m, D.perx != 0};
+    double *w = D.lin + 4 * D.nc + (size_t)m * 3 * D.nc;
+    const size_t base = c2(D, D.ilo, j);
+    tri_line(L, ni, D.perx != 0, w + base, w + D.nc + base, w + 2 * D.nc + base, 1);
+}
+
 // U += dU on the band
 __global__ void k_ns_update(NsDev D) {
     if (D.ctrl->done) return;
@@ -489,6 +642,8 @@ __global__ void k_gsis_finish(NsDev D) {
     const size_t nc = D.nc;
     const double lam = D.ctrl->lam;
     const double k2n = sqrt(2.0 / D.gamma) / D.ma;
+    const int sidx[6] = {0, 1, 2, 3, 7, 8};
+    for (int k = 0; k < 6; k++) D.sk[k * nc + c] = D.S[sidx[k] * nc + c];
     double r, u, v, t, r2, u2, v2, t2;
     prim_ns(D.U, nc, c, D.cv, &r, &u, &v, &t);
     prim_ns(D.U2, nc, c, D.cv, &r2, &u2, &v2, &t2);
@@ -514,6 +669,65 @@ __global__ void k_gsis_finish(NsDev D) {
     D.S[9 * nc + c] += tao[3];
     D.S[7 * nc + c] += q[0];
     D.S[8 * nc + c] += q[1];
+}
+
+// distribution correction f += feq(S) - feq(S_k) on the band (the usual
+// GSIS step; the reference corrects the moments only), with the sweep's
+// floor.  One thread per cell and velocity slice.
+template <typename real>
+__device__ __forceinline__ void shakhov(real vx, real vy, const real *p, real *g, real *h) {
+    // p: crt, u, v, 1/T, T/2, cpt qx, cpt qy (Get_Feq, GKUA_Residual.f90:441-458)
+    const real viu = vx - p[1], vjv = vy - p[2];
+    const real vij2 = (viu * viu + vjv * vjv) * p[3];
+    const real fvx = p[5] * viu + p[6] * vjv;
+    const real gdv = p[0] * dexp<real>(-vij2);
+    *g = gdv * (real(1) + fvx * (real(2) * vij2 - real(4)));
+    *h = (p[4] * gdv) * (real(1) + fvx * (real(2) * vij2 - real(2)));
+}
+
+template <typename real>
+__device__ __forceinline__ void shakhov_params(double r, double u, double v, double t, double qx, double qy,
+                                               double cpr, real *p) {
+    const double cpt = cpr / (r * t * t);
+    p[0] = (real)(r / (HYB_PI * t));
+    p[1] = (real)u;
+    p[2] = (real)v;
+    p[3] = (real)(1.0 / t);
+    p[4] = (real)(t / 2.0);
+    p[5] = (real)(cpt * qx);
+    p[6] = (real)(cpt * qy);
+}
+
+template <typename real>
+__global__ void k_gsis_fcorr(NsDev D, real *f, const double *vx, const double *vy, int nvi, int nv, int Na, int Nb,
+                             double cpr) {
+    const int PA = D.PA;
+    const size_t ncell = (size_t)Nb * PA;
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ncell) return;
+    const int a = (int)(cell % PA) + 1, b = (int)(cell / PA) + 1;
+    if (a > Na) return;
+    const int i = D.scan_is_j ? b : a, j = D.scan_is_j ? a : b;
+    if (i < D.ilo || i > D.ihi || j < D.jlo || j > D.jhi) return;
+    const size_t c = c2(D, i, j), nc = D.nc;
+    real pn[7], po[7];
+    shakhov_params<real>(D.S[c], D.S[nc + c], D.S[2 * nc + c], D.S[3 * nc + c], D.S[7 * nc + c], D.S[8 * nc + c], cpr,
+                         pn);
+    shakhov_params<real>(D.sk[c], D.sk[nc + c], D.sk[2 * nc + c], D.sk[3 * nc + c], D.sk[4 * nc + c],
+                         D.sk[5 * nc + c], cpr, po);
+    const real fl = Consts<real>::floor_();
+    const int nsl = gridDim.y, per = (nv + nsl - 1) / nsl;
+    const int v0 = blockIdx.y * per, v1 = min(nv, v0 + per);
+    for (int vv = v0; vv < v1; vv++) {
+        const real ex = (real)vx[vv % nvi], ey = (real)vy[vv / nvi];
+        real g1, h1, g0, h0;
+        shakhov<real>(ex, ey, pn, &g1, &h1);
+        shakhov<real>(ex, ey, po, &g0, &h0);
+        real *fg = f + ((size_t)vv * 2) * ncell + cell, *fh = fg + ncell;
+        const real ng = *fg + (g1 - g0), nh = *fh + (h1 - h0);
+        *fg = ng < fl ? fl : ng;
+        *fh = nh < fl ? fl : nh;
+    }
 }
 
 // Shakhov parameters of the next kinetic step from the corrected moments
@@ -569,6 +783,8 @@ int ns_create(hyb_ctx *ctx) {
         if (st->have_graph) cudaGraphExecDestroy(st->graph);
         st->have_graph = false;
         st->D.mass_proj = ctx->gsis.reserved[1] == 0;
+        st->D.ns_scheme = ctx->gsis.ns_scheme;
+        st->D.correct_f = ctx->gsis.reserved[2] != 0;
         return HYB_OK;
     }
     if ((ctx->nx < 7 && ctx->bc[0] != HYB_BC_PERIODIC) || (ctx->ny < 7 && ctx->bc[1] != HYB_BC_PERIODIC)) {
@@ -591,7 +807,7 @@ int ns_create(hyb_ctx *ctx) {
     if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = 3; D.jhi = D.ny - 3; }
     D.nc = (size_t)(D.nx + 3) * (D.ny + 3);
     const size_t nc = D.nc;
-    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2;   // see the pointer carve below
+    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6;   // see the pointer carve below
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
     if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
@@ -621,6 +837,8 @@ int ns_create(hyb_ctx *ctx) {
     D.amu = h; h += nc;
     D.fluxi = h; h += 4 * nc; D.fluxj = h; h += 4 * nc;
     D.ti_out = h; h += 4 * nc; D.qi_out = h; h += 2 * nc; D.tj_out = h; h += 4 * nc; D.qj_out = h; h += 2 * nc;
+    D.lin = h; h += 16 * nc;
+    D.sk = h; h += 6 * nc;
     const size_t nm = (size_t)ctx->nx * ctx->ny;
     if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
         cudaFree(st->buf);
@@ -646,6 +864,8 @@ int ns_create(hyb_ctx *ctx) {
     D.PA = ctx->PA;
     D.scan_is_j = ctx->scan_is_j;
     D.mass_proj = ctx->gsis.reserved[1] == 0;
+    D.ns_scheme = ctx->gsis.ns_scheme;
+    D.correct_f = ctx->gsis.reserved[2] != 0;
     D.src_on = 1;
     D.gamma = ctx->prm.gamma;
     D.ma = ctx->prm.ma;
@@ -680,13 +900,21 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     k_ns_faces<<<(nfi + bs - 1) / bs, bs, 0, s>>>(D, 0);
     k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D, 1);
     k_ns_res<<<(ncell + bs - 1) / bs, bs, 0, s>>>(D);
-    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 0);
-    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 0);
-    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 1);
-    k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 1);
+    if (ctx->gsis.ns_solver == 1) {
+        const int ncol = D.ihi - D.ilo + 1, nrow = D.jhi - D.jlo + 1;
+        k_ns_jlines<<<(4 * ncol + 63) / 64, 64, 0, s>>>(D);
+        k_ns_ilines<<<(4 * nrow + 63) / 64, 64, 0, s>>>(D);
+    } else {
+        k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 0);
+        k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 0);
+        k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 1, 1);
+        k_ns_lusgs<<<(nband + bs - 1) / bs, bs, 0, s>>>(D, 0, 1);
+    }
     k_ns_update<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
     k_ns_close<<<1, 256, 0, s>>>(D);
 }
+
+static int inner_launches(const hyb_ctx *ctx) { return ctx->gsis.ns_solver == 1 ? 8 : 10; }
 
 int gsis_solve(hyb_ctx *ctx) {
     NsState *st = (NsState *)ctx->ns;
@@ -742,7 +970,7 @@ int gsis_solve(hyb_ctx *ctx) {
     int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
     for (int b = 0; b < nbatch; b++) {
         HYB_CK(cudaGraphLaunch(st->graph, s));
-        ctx->launches += NS_BATCH * 10;
+        ctx->launches += NS_BATCH * inner_launches(ctx);
         HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
         HYB_CK(cudaStreamSynchronize(s));
         if (st->h_ctrl->done) break;
@@ -755,6 +983,16 @@ int gsis_solve(hyb_ctx *ctx) {
     k_gsis_mass<<<1, 256, 0, s>>>(D);
     k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    if (D.correct_f) {
+        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)(ctx->nvj < 16 ? ctx->nvj : 16));
+        if (ctx->precision == HYB_PREC_FP64)
+            k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
+                                                     ctx->Na, ctx->Nb, ctx->prm.cpr);
+        else
+            k_gsis_fcorr<float><<<grd, 256, 0, s>>>(D, (float *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
+                                                    ctx->Na, ctx->Nb, ctx->prm.cpr);
+        ctx->launches++;
+    }
     if (ctx->precision == HYB_PREC_FP64)
         k_gsis_eqp<double><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (double *)ctx->d_eqp,
                                                                           ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,

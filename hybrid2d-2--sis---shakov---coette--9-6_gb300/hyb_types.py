@@ -73,7 +73,7 @@ class HybGsisParams(C.Structure):
         ("enable", C.c_int), ("max_inner", C.c_int), ("inner_tol", C.c_double),
         ("inner_rtol", C.c_double), ("cfl", C.c_double), ("dtmax", C.c_double), ("dtmin", C.c_double),
         ("flux", C.c_int), ("ns_scheme", C.c_int), ("use_mlp", C.c_int),
-        ("reserved", C.c_int * 5),
+        ("ns_solver", C.c_int), ("reserved", C.c_int * 4),
     ]
 
 

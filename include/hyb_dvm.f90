@@ -43,8 +43,8 @@ module hyb_dvm
   type, bind(c) :: hyb_gsis_params
      integer(c_int) :: enable, max_inner
      real(c_double) :: inner_tol, inner_rtol, cfl, dtmax, dtmin
-     integer(c_int) :: flux, ns_scheme, use_mlp
-     integer(c_int) :: reserved(5)
+     integer(c_int) :: flux, ns_scheme, use_mlp, ns_solver
+     integer(c_int) :: reserved(4)
   end type hyb_gsis_params
 
   interface

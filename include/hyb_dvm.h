@@ -129,7 +129,12 @@ typedef struct hyb_gsis_params {
     int    flux;            /* NS flux splitting, Flux_* (COMMONDATA.f90:12) */
     int    ns_scheme;       /* NS reconstruction scheme, Scheme_* (:11)      */
     int    use_mlp;         /* use the learned closure as warm start         */
-    int    reserved[5];
+    int    ns_solver;       /* inner solver: 0 LU-SGS (du_LU_SGS_2D,
+                               sub_LU_SGS.f90), 1 line-implicit ADI with the
+                               LU-SGS diagonal and scalar couplings, exact
+                               along each mesh line (no counterpart in the
+                               reference)                                    */
+    int    reserved[4];
 } hyb_gsis_params;
 
 typedef struct hyb_ctx hyb_ctx;

@@ -394,21 +394,29 @@ int orc_phy_boundary(orc *o)
     return HYB_OK;
 }
 
-/* ---- Get_Feq (GKUA_Residual.f90:420-469) for one velocity ---------------- */
-static void feq_cell(const orc *o, int i, int j, int iv, int jv, double *g, double *h)
+/* ---- Get_Feq (GKUA_Residual.f90:420-469) for one velocity, from the
+ * moments s6 = (rho, u, v, T, qx, qy) ------------------------------------- */
+void orc_feq(const orc *o, const double *s6, int iv, int jv, double *g, double *h)
 {
-    double s1 = SG(o, 1, i, j), s2 = SG(o, 2, i, j), s3 = SG(o, 3, i, j), s4 = SG(o, 4, i, j);
+    double s1 = s6[0], s2 = s6[1], s3 = s6[2], s4 = s6[3];
     double vjv = o->vj[jv] - s3;
     double viu = o->vi[iv] - s2;
     double crt = s1 / (PI * s4);
     double cpt = o->prm.cpr / (s1 * s4 * s4);
-    double viuq = viu * SG(o, 8, i, j);
-    double vq = viuq + vjv * SG(o, 9, i, j);
+    double viuq = viu * s6[4];
+    double vq = viuq + vjv * s6[5];
     double vij2 = (viu * viu + vjv * vjv) / s4;
     double fvxdv = cpt * vq;
     double gdv = crt * exp(-vij2);
     *g = gdv * (1.0 + fvxdv * (2. * vij2 - 4.));
     *h = (s4 * gdv / 2.) * (1.0 + fvxdv * (2. * vij2 - 2.));
+}
+
+static void feq_cell(const orc *o, int i, int j, int iv, int jv, double *g, double *h)
+{
+    const double s6[6] = {SG(o, 1, i, j), SG(o, 2, i, j), SG(o, 3, i, j), SG(o, 4, i, j), SG(o, 8, i, j),
+                          SG(o, 9, i, j)};
+    orc_feq(o, s6, iv, jv, g, h);
 }
 
 /* ---- RHSFDVsub (GKUA_Residual.f90:117-418) for one velocity ---------------

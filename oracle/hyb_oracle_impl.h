@@ -60,6 +60,7 @@ struct orc {
 void orc_ns_free(orc *o);
 void orc_build_u(orc *o, double *U);
 int orc_kinetic_residual_moments(orc *o, double *rk);
+void orc_feq(const orc *o, const double *s6, int iv, int jv, double *g, double *h);
 int orc_gsis_solve(orc *o);
 
 #endif

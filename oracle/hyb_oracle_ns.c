@@ -46,6 +46,7 @@ struct orc_ns {
     size_t nc;
     double *U, *U2, *dU, *Res, *dt, *Lci, *Lcj, *Lvi, *Lvj;
     double *rk, *src;                            /* kinetic residual moments, synthetic source [4][nc] */
+    double *sk;                                  /* band moments before the correction [6][nc] */
     double *d, *uu, *vv, *T, *p, *cc, *amu;
     double *fluxi, *fluxj;                       /* [4][nc], faces at the C2 index of (i,j) */
     double *ti_out, *qi_out, *tj_out, *qj_out;   /* NS stress at faces, no HoT */
@@ -59,7 +60,7 @@ void orc_ns_free(orc *o)
 {
     if (!o || !o->ns) return;
     struct orc_ns *ns = o->ns;
-    double **ps[] = {&ns->U, &ns->rk, &ns->src, &ns->U2, &ns->dU, &ns->Res, &ns->dt, &ns->Lci, &ns->Lcj, &ns->Lvi, &ns->Lvj,
+    double **ps[] = {&ns->U, &ns->rk, &ns->src, &ns->sk, &ns->U2, &ns->dU, &ns->Res, &ns->dt, &ns->Lci, &ns->Lcj, &ns->Lvi, &ns->Lvj,
                      &ns->d, &ns->uu, &ns->vv, &ns->T, &ns->p, &ns->cc, &ns->amu, &ns->fluxi, &ns->fluxj,
                      &ns->ti_out, &ns->qi_out, &ns->tj_out, &ns->qj_out};
     for (size_t k = 0; k < sizeof(ps) / sizeof(ps[0]); k++) free(*ps[k]);
@@ -76,6 +77,7 @@ static int ns_alloc(orc *o)
     ns->nc = nc;
     ns->U = calloc(4 * nc, sizeof(double));
     ns->rk = calloc(4 * nc, sizeof(double)); ns->src = calloc(4 * nc, sizeof(double));
+    ns->sk = calloc(6 * nc, sizeof(double));
     ns->U2 = calloc(4 * nc, sizeof(double)); ns->dU = calloc(4 * nc, sizeof(double));
     ns->Res = calloc(4 * nc, sizeof(double)); ns->dt = calloc(nc, sizeof(double));
     ns->Lci = calloc(nc, sizeof(double)); ns->Lcj = calloc(nc, sizeof(double));
@@ -87,7 +89,7 @@ static int ns_alloc(orc *o)
     ns->ti_out = calloc(4 * nc, sizeof(double)); ns->qi_out = calloc(2 * nc, sizeof(double));
     ns->tj_out = calloc(4 * nc, sizeof(double)); ns->qj_out = calloc(2 * nc, sizeof(double));
     o->ns = ns;
-    if (!ns->qj_out || !ns->rk || !ns->src) { orc_ns_free(o); return HYB_ERR_NOMEM; }
+    if (!ns->qj_out || !ns->rk || !ns->src || !ns->sk) { orc_ns_free(o); return HYB_ERR_NOMEM; }
     return HYB_OK;
 }
 
@@ -140,9 +142,17 @@ static double minmod_ns(double a, double b)
     return (fabs(a) <= fabs(b)) ? a : b;
 }
 
-/* scheme_fP / scheme_fm, NND2 (sub_Residual.f90:490-491, 526-527) */
-static void recon_nnd(double u1, double u2, double u3, double u4, double *ul, double *ur)
+/* face states of the NS reconstruction.  sch 1: scheme_fP / scheme_fm NND2
+ * (sub_Residual.f90:490-491, 526-527); 0: first order; 2: the same
+ * upwind-biased stencil without the limiter (smooth, for the synthetic solve) */
+static void recon_nnd(int sch, double u1, double u2, double u3, double u4, double *ul, double *ur)
 {
+    if (sch == 0) { *ul = u2; *ur = u3; return; }
+    if (sch == 2) {
+        *ul = u2 + 0.25 * ((u2 - u1) + (u3 - u2));
+        *ur = u3 - 0.25 * ((u3 - u2) + (u4 - u3));
+        return;
+    }
     *ul = u2 + 0.5 * minmod_ns(u2 - u1, u3 - u2);
     *ur = u3 - 0.5 * minmod_ns(u3 - u2, u4 - u3);
 }
@@ -234,7 +244,7 @@ static void ns_residual(orc *o)
                 double UL[4], UR[4];
                 const double *vars[4] = {ns->d, ns->uu, ns->vv, ns->p};
                 for (int m = 0; m < 4; m++)
-                    recon_nnd(vars[m][c0], vars[m][c1], vars[m][c2], vars[m][c3], &UL[m], &UR[m]);
+                    recon_nnd(o->gsis.ns_scheme, vars[m][c0], vars[m][c1], vars[m][c2], vars[m][c3], &UL[m], &UR[m]);
                 double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
                 double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
                 double F0[4];
@@ -447,6 +457,116 @@ static void ns_lusgs(orc *o, int ilo, int ihi, int jlo, int jhi)
                 if (((i + j) & 1) == col) lusgs_bwd_cell(o, i, j, ihi, jhi);
 }
 
+/* Tridiagonal solve b_k x_k - a_k x_{k-1} - c_k x_{k+1} = d_k, k = 0..n-1;
+ * cyclic couples x_{-1} = x_{n-1} and x_n = x_0 (Sherman-Morrison).  w is
+ * scratch of 3n doubles.  Thomas algorithm. */
+static void tri_solve(int n, const double *a, const double *b, const double *c, const double *d, double *x,
+                      int cyclic, double *w)
+{
+    double *cp = w, *dp = w + n, *z = w + 2 * n;
+    if (!cyclic || n < 3) {
+        double den = b[0];
+        cp[0] = -c[0] / den;
+        dp[0] = d[0] / den;
+        for (int k = 1; k < n; k++) {
+            den = b[k] + a[k] * cp[k - 1];
+            cp[k] = -c[k] / den;
+            dp[k] = (d[k] + a[k] * dp[k - 1]) / den;
+        }
+        x[n - 1] = dp[n - 1];
+        for (int k = n - 2; k >= 0; k--) x[k] = dp[k] - cp[k] * x[k + 1];
+        return;
+    }
+    /* A = T + u v^T with u = (gamma, 0.., -c_{n-1}... ) : corner terms
+     * A[0][n-1] = -a_0, A[n-1][0] = -c_{n-1}; choose gamma = -b_0 */
+    const double gam = -b[0];
+    double bb0 = b[0] - gam, bbn = b[n - 1] - (a[0] * c[n - 1]) / gam;
+    /* solve T y = d and T z = u, u = (gam, 0, .., 0, -c_{n-1}) */
+    double den = bb0;
+    cp[0] = -c[0] / den;
+    dp[0] = d[0] / den;
+    z[0] = gam / den;
+    for (int k = 1; k < n; k++) {
+        double bk = (k == n - 1) ? bbn : b[k];
+        double uk = (k == n - 1) ? -c[n - 1] : 0.0;
+        den = bk + a[k] * cp[k - 1];
+        cp[k] = -c[k] / den;
+        dp[k] = (d[k] + a[k] * dp[k - 1]) / den;
+        z[k] = (uk + a[k] * z[k - 1]) / den;
+    }
+    for (int k = n - 2; k >= 0; k--) {
+        dp[k] = dp[k] - cp[k] * dp[k + 1];
+        z[k] = z[k] - cp[k] * z[k + 1];
+    }
+    /* v = (1, 0, .., 0, -a_0 / gam) */
+    double vy = dp[0] - a[0] / gam * dp[n - 1], vz = z[0] - a[0] / gam * z[n - 1];
+    double f = vy / (1.0 + vz);
+    for (int k = 0; k < n; k++) x[k] = dp[k] - f * z[k];
+}
+
+/* line-implicit ADI inner solve (no counterpart in the reference).  The
+ * matrix is the one du_LU_SGS_2D factorises approximately (sub_LU_SGS.f90:
+ * 26-111) with the flux differences of comput_DFn left out: diagonal alpha,
+ * neighbour couplings 0.5 Lc + Lv of the neighbour.  Every j line is solved
+ * exactly (scalar tridiagonal per variable), then every i line with the
+ * j-neighbour terms of the first half taken as known.  Band edges are
+ * Dirichlet (dU = 0 outside the band); lines along a periodic axis are
+ * cyclic. */
+static void ns_adi(orc *o, int ilo, int ihi, int jlo, int jhi)
+{
+    struct orc_ns *ns = o->ns;
+    const int perx = (o->bc[0] == HYB_BC_PERIODIC), pery = (o->bc[1] == HYB_BC_PERIODIC);
+    const int ni = ihi - ilo + 1, nj = jhi - jlo + 1, nm = ni > nj ? ni : nj;
+    double *a = malloc(nm * sizeof(double)), *b = malloc(nm * sizeof(double)), *c = malloc(nm * sizeof(double));
+    double *d = malloc(nm * sizeof(double)), *x = malloc(nm * sizeof(double)), *w = malloc(3 * nm * sizeof(double));
+    double *d1 = calloc(4 * ns->nc, sizeof(double)), *jt = calloc(4 * ns->nc, sizeof(double));
+#define ALFA(cc, ii, jj) (o->vol[MI(o, ii, jj)] / ns->dt[cc] + ns->Lci[cc] + ns->Lcj[cc] + 2.0 * (ns->Lvi[cc] + ns->Lvj[cc]))
+    for (int i = ilo; i <= ihi; i++) {
+        for (int k = 0; k < nj; k++) {
+            int j = jlo + k;
+            size_t cc = C2(o, i, j);
+            int jm = j - 1 < jlo ? jhi : j - 1, jp = j + 1 > jhi ? jlo : j + 1;
+            size_t cm = C2(o, i, jm), cq = C2(o, i, jp);
+            b[k] = ALFA(cc, i, j);
+            a[k] = (pery || j > jlo) ? 0.5 * ns->Lcj[cm] + ns->Lvj[cm] : 0.0;
+            c[k] = (pery || j < jhi) ? 0.5 * ns->Lcj[cq] + ns->Lvj[cq] : 0.0;
+        }
+        for (int m = 0; m < 4; m++) {
+            for (int k = 0; k < nj; k++) d[k] = A4(ns->Res, m, C2(o, i, jlo + k));
+            tri_solve(nj, a, b, c, d, x, pery, w);
+            for (int k = 0; k < nj; k++) A4(d1, m, C2(o, i, jlo + k)) = x[k];
+        }
+        for (int k = 0; k < nj; k++) {
+            int j = jlo + k;
+            int jm = j - 1 < jlo ? jhi : j - 1, jp = j + 1 > jhi ? jlo : j + 1;
+            for (int m = 0; m < 4; m++) {
+                double t = 0.0;
+                if (pery || j > jlo) t += a[k] * A4(d1, m, C2(o, i, jm));
+                if (pery || j < jhi) t += c[k] * A4(d1, m, C2(o, i, jp));
+                A4(jt, m, C2(o, i, j)) = t;
+            }
+        }
+    }
+    for (int j = jlo; j <= jhi; j++) {
+        for (int k = 0; k < ni; k++) {
+            int i = ilo + k;
+            size_t cc = C2(o, i, j);
+            int im = i - 1 < ilo ? ihi : i - 1, ip = i + 1 > ihi ? ilo : i + 1;
+            size_t cm = C2(o, im, j), cq = C2(o, ip, j);
+            b[k] = ALFA(cc, i, j);
+            a[k] = (perx || i > ilo) ? 0.5 * ns->Lci[cm] + ns->Lvi[cm] : 0.0;
+            c[k] = (perx || i < ihi) ? 0.5 * ns->Lci[cq] + ns->Lvi[cq] : 0.0;
+        }
+        for (int m = 0; m < 4; m++) {
+            for (int k = 0; k < ni; k++) d[k] = A4(ns->Res, m, C2(o, ilo + k, j)) + A4(jt, m, C2(o, ilo + k, j));
+            tri_solve(ni, a, b, c, d, x, perx, w);
+            for (int k = 0; k < ni; k++) A4(ns->dU, m, C2(o, ilo + k, j)) = x[k];
+        }
+    }
+#undef ALFA
+    free(a); free(b); free(c); free(d); free(x); free(w); free(d1); free(jt);
+}
+
 /* NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:4-40); returns the max
  * |Res(4)| over the band before the update (get_res, IO.f90:286-303) */
 static int ns_advance(orc *o, double *res4)
@@ -469,7 +589,8 @@ static int ns_advance(orc *o, double *res4)
         }
     *res4 = rmax;
     ns_lvc_dt(o);
-    ns_lusgs(o, ilo, ihi, jlo, jhi);
+    if (o->gsis.ns_solver == 1) ns_adi(o, ilo, ihi, jlo, jhi);
+    else ns_lusgs(o, ilo, ihi, jlo, jhi);
     for (int j = jlo; j <= jhi; j++)
         for (int i = ilo; i <= ihi; i++)
             for (int m = 0; m < 4; m++) A4(ns->U, m, C2(o, i, j)) += A4(ns->dU, m, C2(o, i, j));
@@ -555,6 +676,9 @@ int orc_gsis_solve(orc *o)
             double r, u, v, t, r2, u2, v2, t2;
             prim_ns(ns->U, ns->nc, c, cv, &r, &u, &v, &t);
             prim_ns(ns->U2, ns->nc, c, cv, &r2, &u2, &v2, &t2);
+            A4(ns->sk, 0, c) = SG(o, 1, i, j); A4(ns->sk, 1, c) = SG(o, 2, i, j);
+            A4(ns->sk, 2, c) = SG(o, 3, i, j); A4(ns->sk, 3, c) = SG(o, 4, i, j);
+            A4(ns->sk, 4, c) = SG(o, 8, i, j); A4(ns->sk, 5, c) = SG(o, 9, i, j);
             SG(o, 1, i, j) += r - r2 - lam;
             SG(o, 2, i, j) += (u - u2) / kin2ns;
             SG(o, 3, i, j) += (v - v2) / kin2ns;
@@ -582,6 +706,29 @@ int orc_gsis_solve(orc *o)
             SG(o, 8, i, j) += q[0];
             SG(o, 9, i, j) += q[1];
         }
+    /* optional distribution correction f += feq(S) - feq(S_k) on the band
+     * (the usual GSIS step; the reference corrects the moments only), with
+     * the sweep's floor */
+    if (o->gsis.reserved[2]) {
+#pragma omp parallel for schedule(static)
+        for (int v = 0; v < o->nv; v++) {
+            int iv = v % o->nvi, jv = v / o->nvi;
+            for (int j = jlo; j <= jhi; j++)
+                for (int i = ilo; i <= ihi; i++) {
+                    size_t c = C2(o, i, j);
+                    double s_new[6] = {SG(o, 1, i, j), SG(o, 2, i, j), SG(o, 3, i, j), SG(o, 4, i, j),
+                                       SG(o, 8, i, j), SG(o, 9, i, j)};
+                    double s_old[6];
+                    for (int k = 0; k < 6; k++) s_old[k] = A4(ns->sk, k, c);
+                    double g1, h1, g0, h0;
+                    orc_feq(o, s_new, iv, jv, &g1, &h1);
+                    orc_feq(o, s_old, iv, jv, &g0, &h0);
+                    double fg = FRD(o, 0, i, j, v) + (g1 - g0), fh = FRD(o, 1, i, j, v) + (h1 - h0);
+                    FRD(o, 0, i, j, v) = fg < F_FLOOR ? F_FLOOR : fg;
+                    FRD(o, 1, i, j, v) = fh < F_FLOOR ? F_FLOOR : fh;
+                }
+        }
+    }
     return HYB_OK;
 }
 

@@ -162,8 +162,10 @@ class Oracle:
         gp.flux = kw.get("flux", 5)
         gp.ns_scheme = kw.get("ns_scheme", 1)
         gp.use_mlp = kw.get("use_mlp", 0)
+        gp.ns_solver = kw.get("ns_solver", 0)
         gp.reserved[0] = kw.get("plane_order", 0)
         gp.reserved[1] = kw.get("no_mass_projection", 0)
+        gp.reserved[2] = kw.get("correct_f", 0)
         rc = self.L.orc_gsis_configure(self.h, C.byref(gp))
         if rc != 0:
             raise RuntimeError(f"orc_gsis_configure failed: {rc}")

@@ -36,19 +36,33 @@ def _pair(case, precision, **gk):
     return g, o
 
 
+@pytest.mark.parametrize("solver", [0, 1])
 @pytest.mark.parametrize("shape", ["small", "transposed", "stretched"])
-def test_gsis_fixed_inner_matches_oracle(cases_mod, shape):
+def test_gsis_fixed_inner_matches_oracle(cases_mod, shape, solver):
     if shape == "small":
         c = cases_mod.couette_small(ncy=32, nvx=16, nvy=16, dt=0.02)
     elif shape == "transposed":
         c = cases_mod.couette_small(ncx=40, ncy=8, nvx=12, nvy=12, dt=0.02)
     else:
         c = cases_mod.couette_small(ncy=32, nvx=12, nvy=12, dt=0.02, stretch=1.5)
-    g, o = _pair(c, 0, **FIXED)
+    g, o = _pair(c, 0, ns_solver=solver, **FIXED)
     for _ in range(3):
         g.step(1)
         o.step(1)
         assert g.gsis_last_inner() == o.gsis_last_inner() == FIXED["max_inner"]
+    _cmp_state(c, g, o, 1e-10)
+
+
+@pytest.mark.parametrize("shape", ["small", "stretched"])
+def test_gsis_distribution_correction_matches_oracle(cases_mod, shape):
+    if shape == "small":
+        c = cases_mod.couette_small(ncy=32, nvx=16, nvy=16, dt=0.02)
+    else:
+        c = cases_mod.couette_small(ncy=32, nvx=12, nvy=12, dt=0.02, stretch=1.5)
+    g, o = _pair(c, 0, correct_f=1, **FIXED)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
     _cmp_state(c, g, o, 1e-10)
 
 
@@ -81,9 +95,13 @@ def test_gsis_mixed_precision_error_is_bounded(cases_mod):
     assert err_rho < 5e-6 and err_t < 5e-6 and err_u < 5e-5, (err_rho, err_u, err_t)
 
 
-def test_gsis_converges_faster_than_plain(cases_mod):
+@pytest.mark.parametrize("solver,inner,corr,gain", [(0, 200, 0, 4), (1, 10, 0, 20), (0, 40, 1, 1000)])
+def test_gsis_converges_faster_than_plain(cases_mod, solver, inner, corr, gain):
     """Kn 0.1 channel, NND, dt 0.01: after 300 outer iterations the GSIS
-    residual is well below the plain one (oracle: 4.1e-4 against 3.5e-3)."""
+    residual is well below the plain one (oracle: plain 3.5e-3; LU-SGS
+    inner solve, 200 iterations: 4.1e-4; line-implicit inner solve, 10
+    iterations: 5.0e-5; LU-SGS, 40 iterations, with the distribution
+    correction: 6.9e-7)."""
     from hyb_gb300 import abi
     c = cases_mod.couette_small(dt=0.01)
     plain = abi.Solver(c, precision=0)
@@ -91,9 +109,10 @@ def test_gsis_converges_faster_than_plain(cases_mod):
     rp = plain.step(300)
     gs = abi.Solver(c, precision=0)
     gs.init_maxwellian()
-    gs.gsis(max_inner=200, inner_tol=0.0, inner_rtol=1e-2, cfl=20.0)
+    gs.gsis(max_inner=inner, inner_tol=0.0, inner_rtol=1e-2, cfl=20.0 if solver == 0 else 1000.0,
+            ns_solver=solver, correct_f=corr)
     rg = gs.step(300)
-    assert rg["max_rms"] < rp["max_rms"] / 4, (rg["max_rms"], rp["max_rms"])
+    assert rg["max_rms"] < rp["max_rms"] / gain, (rg["max_rms"], rp["max_rms"])
 
 
 def test_gsis_configure_errors(cases_mod):
