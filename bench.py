@@ -279,13 +279,89 @@ def run_gb300(args, world, rank, local):
     return 0
 
 
+def batch_cases():
+    """The seeded 256-instance manifest, FP32 distribution, dt scaled with the
+    cell size (kinetic CFL about 3 for the 64-cell channel at dt 0.01)."""
+    out = []
+    for d in cases.batch_manifest():
+        out.append(cases.Case(precision=1, dt=0.01 * 64.0 / d["ncy"], **d))
+    return out
+
+
+def run_batch(args, world, rank, local):
+    # one hardware queue per concurrent graph branch, up to the device limit;
+    # read when the CUDA context is created, so set before the first call
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    cl = batch_cases()
+    b = abi.Batch(cl, device=local)
+    b.init_maxwellian()
+    t_tune = time.perf_counter()
+    b.autotune(reps=2)
+    t_tune = time.perf_counter() - t_tune
+    b.step(args.warmup, residual=False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = b.launches()
+    dist_barrier(world)
+    b.step(args.steps, residual=False)
+    ms = b.last_ms()
+    launches = b.launches() - l0
+    dist_barrier(world)
+    clk = clocks.stop()
+    ms = dist_max(world, ms)
+    units = sum(c.cells * c.nv for c in cl) * args.steps
+    value = world * units / (ms / 1000.0)
+    # the same iterations issued instance by instance through hyb_step
+    views = [b.instance(k) for k in range(len(cl))]
+    t0 = time.perf_counter()
+    for v_ in views:
+        v_.step(args.steps, residual=False)
+    seq_ms = 1000.0 * (time.perf_counter() - t0)
+    # end to end: residuals of every instance read back each step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = b.step(1, residual=True)
+    e2e_s = dist_max(world, time.perf_counter() - t0)
+    peak, peak_kind = measured_peaks()
+    achieved = 16.0 * units / args.steps / (ms / args.steps / 1000.0) / 1e9
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded instance manifest, default_rng(20261203))",
+        "config": {"workload": "batched Couette, 256 instances", "instances": len(cl),
+                   "cell_velocities_per_step": units // args.steps,
+                   "precision": "fp32 f/fluxes/sweeps, fp64 moments", "scheme": "NND",
+                   "launch": "one CUDA graph launch per outer iteration, one branch per instance",
+                   "autotune_s": round(t_tune, 2), "parallelism": f"replicas x{world}",
+                   "l2": "per-step working set above L2 (sum of f over instances)"},
+        "e2e": {"value": world * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": len(cl) * 9 * 8,
+                "calls": "hyb_batch_step(1) with every instance's residual read back"},
+        "roofline": {"bound": "hbm", "kernel": "whole batched step (16 B per cell-velocity)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind},
+        "sequential_ms_per_step": seq_ms / args.steps,
+        "graph_speedup_vs_sequential": seq_ms / ms,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "last_residual_max": max(r["max_rms"] for r in res),
+    }
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="large", choices=["large", "small", "sine", "prof"])
+    ap.add_argument("--config", default="large", choices=["large", "small", "sine", "prof", "batch"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
@@ -294,6 +370,8 @@ def main():
     world, rank, local = dist_init()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.config == "batch":
+        return run_batch(args, world, rank, local)
     return run_gb300(args, world, rank, local)
 
 

@@ -20,7 +20,10 @@ EXPORTS = [
     "hyb_download_hot", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
     "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
     "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
-    "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc",
+    "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc", "hyb_autotune",
+    "hyb_batch_create", "hyb_batch_destroy", "hyb_batch_last_error", "hyb_batch_size",
+    "hyb_batch_instance", "hyb_batch_init_maxwellian", "hyb_batch_autotune", "hyb_batch_step",
+    "hyb_batch_last_step_ms", "hyb_batch_launch_count",
 ]
 STAGES = ["wall", "sweep", "moments", "sghost", "convert_ns", "gsis", "residual"]
 
@@ -63,6 +66,18 @@ def load(path=None):
     L.hyb_last_step_ms.argtypes = [vp, dp]
     L.hyb_stream.argtypes = [vp, C.POINTER(vp)]
     L.hyb_set_walls.argtypes = [vp, ip, dp, dp, dp]
+    L.hyb_autotune.argtypes = [vp, ip, C.POINTER(ip), C.POINTER(ip)]
+    L.hyb_batch_create.argtypes = [ip, vp, vp, vp, C.POINTER(vp)]
+    L.hyb_batch_destroy.argtypes = [vp]
+    L.hyb_batch_last_error.argtypes = [vp]
+    L.hyb_batch_last_error.restype = C.c_char_p
+    L.hyb_batch_size.argtypes = [vp, C.POINTER(ip)]
+    L.hyb_batch_instance.argtypes = [vp, ip, C.POINTER(vp)]
+    L.hyb_batch_init_maxwellian.argtypes = [vp] + [C.c_double] * 4
+    L.hyb_batch_autotune.argtypes = [vp, ip]
+    L.hyb_batch_step.argtypes = [vp, ip, vp]
+    L.hyb_batch_last_step_ms.argtypes = [vp, dp]
+    L.hyb_batch_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.hyb_profile_enable.argtypes = [vp, ip]
     L.hyb_profile_read.argtypes = [vp, dp, C.POINTER(C.c_longlong), ip]
     L.hyb_detfp_noalloc.argtypes = [ip, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -79,9 +94,15 @@ class Solver:
     subroutines (GKUA_Phy_boundary, Hybrid_GKUA_Comput_Block, DETFP,
     Convert_NS, DETFP_res, Hybrid_Time_advance_LU_SGS)."""
 
-    def __init__(self, case, precision=None, device=0):
+    def __init__(self, case, precision=None, device=0, handle=None):
         self.L = load()
         self.case = case
+        self.owned = handle is None
+        if handle is not None:      # an instance owned by a Batch
+            self.h = handle
+            self.nx, self.ny, self.nv = case.nx, case.ny, case.nv
+            self.P = (self.nx + 7) * (self.ny + 7)
+            return
         m, g, p, keep = case.c_structs()
         if precision is not None:
             p.precision = precision
@@ -101,9 +122,15 @@ class Solver:
             raise HybError(rc, f"{what}: {msg}")
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "owned", True):
             self.L.hyb_destroy(self.h)
-            self.h = None
+        self.h = None
+
+    def autotune(self, reps=3):
+        """Time every admissible sweep shape; returns the chosen (cpt, vpb)."""
+        c, v = C.c_int(0), C.c_int(0)
+        self._ck(self.L.hyb_autotune(self.h, reps, C.byref(c), C.byref(v)), "autotune")
+        return c.value, v.value
 
     def __del__(self):
         try:
@@ -204,4 +231,75 @@ class Solver:
     def last_ms(self):
         x = C.c_double()
         self._ck(self.L.hyb_last_step_ms(self.h, C.byref(x)), "last_step_ms")
+        return x.value
+
+
+class Batch:
+    """Many independent cases advanced together by one graph launch per outer
+    iteration (hyb_batch_*)."""
+
+    def __init__(self, case_list, precision=None, device=0):
+        self.L = load()
+        self.cases = list(case_list)
+        n = len(self.cases)
+        self._keep = []
+        M = (T.HybMesh * n)()
+        G = (T.HybVgrid * n)()
+        P = (T.HybParams * n)()
+        for k, c in enumerate(self.cases):
+            m, g, p, keep = c.c_structs()
+            if precision is not None:
+                p.precision = precision
+            p.device = device
+            M[k], G[k], P[k] = m, g, p
+            self._keep.append((m, g, p, keep))
+        self._arrays = (M, G, P)
+        h = C.c_void_p()
+        rc = self.L.hyb_batch_create(n, M, G, P, C.byref(h))
+        if rc != 0:
+            raise HybError(rc, "hyb_batch_create failed")
+        self.h = h
+        self.n = n
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = self.L.hyb_batch_last_error(self.h).decode() if self.h else ""
+            raise HybError(rc, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hyb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def instance(self, k):
+        """Non-owning Solver view of instance k."""
+        h = C.c_void_p()
+        self._ck(self.L.hyb_batch_instance(self.h, k, C.byref(h)), "batch_instance")
+        return Solver(self.cases[k], handle=h)
+
+    def init_maxwellian(self, rho=1.0, u=0.0, v=0.0, t=1.0):
+        self._ck(self.L.hyb_batch_init_maxwellian(self.h, rho, u, v, t), "batch_init_maxwellian")
+
+    def autotune(self, reps=3):
+        self._ck(self.L.hyb_batch_autotune(self.h, reps), "batch_autotune")
+
+    def step(self, n=1, residual=True):
+        res = (T.HybResidual * self.n)() if residual else None
+        self._ck(self.L.hyb_batch_step(self.h, n, res), "batch_step")
+        return [r.as_dict() for r in res] if residual else None
+
+    def last_ms(self):
+        x = C.c_double()
+        self._ck(self.L.hyb_batch_last_step_ms(self.h, C.byref(x)), "batch_last_step_ms")
+        return x.value
+
+    def launches(self):
+        x = C.c_longlong()
+        self._ck(self.L.hyb_batch_launch_count(self.h, C.byref(x)), "batch_launch_count")
         return x.value

@@ -135,6 +135,8 @@ __host__ __device__ inline size_t hyb_c2(int nx, int i, int j) {
 namespace hyb {
 int launch_wall(hyb_ctx *ctx);
 int launch_sweep(hyb_ctx *ctx, int store_rhs);
+int sweep_prepare(hyb_ctx *ctx);
+void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb);
 size_t sweep_smem_bytes(const hyb_ctx *ctx);
 int launch_moments(hyb_ctx *ctx);
 int moments_slices(const hyb_ctx *ctx);

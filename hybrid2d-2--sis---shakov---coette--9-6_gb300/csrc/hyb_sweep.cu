@@ -7,8 +7,8 @@
 
 namespace hyb {
 
-int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb);
-int sweep_launch_f64(hyb_ctx *ctx, const KinArgs<double> &A, int cpt, int vpb);
+int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb, bool launch);
+int sweep_launch_f64(hyb_ctx *ctx, const KinArgs<double> &A, int cpt, int vpb, bool launch);
 size_t sweep_group_bytes_f32(int PA, int tpv);
 size_t sweep_group_bytes_f64(int PA, int tpv);
 
@@ -75,19 +75,24 @@ static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.err = ctx->d_err;
 }
 
-// store_rhs: 0 no RHS store, 1 RHS to d_rhs with the update, 2 RHS only
-// (to d_rhs_gsis, f unchanged)
-int launch_sweep(hyb_ctx *ctx, int store_rhs) {
+static int sweep_dispatch(hyb_ctx *ctx, int store_rhs, bool launch) {
     int cpt, vpb;
     sweep_shape(ctx, &cpt, &vpb);
     if (ctx->precision == HYB_PREC_FP64) {
         KinArgs<double> A;
         fill_args<double>(ctx, store_rhs, A);
-        return sweep_launch_f64(ctx, A, cpt, vpb);
+        return sweep_launch_f64(ctx, A, cpt, vpb, launch);
     }
     KinArgs<float> A;
     fill_args<float>(ctx, store_rhs, A);
-    return sweep_launch_f32(ctx, A, cpt, vpb);
+    return sweep_launch_f32(ctx, A, cpt, vpb, launch);
 }
+
+// store_rhs: 0 no RHS store, 1 RHS to d_rhs with the update, 2 RHS only
+// (to d_rhs_gsis, f unchanged)
+int launch_sweep(hyb_ctx *ctx, int store_rhs) { return sweep_dispatch(ctx, store_rhs, true); }
+
+// sets the shared-memory attribute of the kernel the current shape selects
+int sweep_prepare(hyb_ctx *ctx) { return sweep_dispatch(ctx, 0, false); }
 
 }  // namespace hyb

@@ -522,8 +522,10 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
 }
 
 // ---- host side --------------------------------------------------------------
+// launch = false only sets the kernel's shared-memory attribute (done before
+// any stream capture of the launch)
 template <typename real, int CPT, bool UNI, int SCHEME>
-int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb) {
+int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, bool launch) {
     const int tpv = ctx->PA / CPT;
     const size_t smem = sweep_group_bytes<real>(ctx->PA, tpv) * vpb;
     static bool attr = false;
@@ -532,6 +534,7 @@ int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb) {
                              227 * 1024);
         attr = true;
     }
+    if (!launch) return HYB_OK;
     dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
     k_sweep<real, CPT, UNI, SCHEME><<<grd, blk, smem, ctx->stream>>>(A);
     ctx->launches++;
@@ -544,21 +547,24 @@ int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb) {
 }
 
 template <typename real, int CPT, bool UNI>
-int sweep_launch_scheme(hyb_ctx *ctx, const KinArgs<real> &A, int vpb) {
+int sweep_launch_scheme(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, bool launch) {
     switch (A.scheme) {
-        case HYB_SCHEME_UP1: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_UP1>(ctx, A, vpb);
-        case HYB_SCHEME_WENO3: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_WENO3>(ctx, A, vpb);
-        default: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_NND>(ctx, A, vpb);
+        case HYB_SCHEME_UP1: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_UP1>(ctx, A, vpb, launch);
+        case HYB_SCHEME_WENO3: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_WENO3>(ctx, A, vpb, launch);
+        default: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_NND>(ctx, A, vpb, launch);
     }
 }
 
 template <typename real>
-int sweep_launch_real(hyb_ctx *ctx, const KinArgs<real> &A, int cpt, int vpb) {
-    const bool uni = ctx->uniform != 0;
+int sweep_launch_real(hyb_ctx *ctx, const KinArgs<real> &A, int cpt, int vpb, bool launch) {
+    const bool u = ctx->uniform != 0;
     switch (cpt) {
-        case 4: return uni ? sweep_launch_scheme<real, 4, true>(ctx, A, vpb) : sweep_launch_scheme<real, 4, false>(ctx, A, vpb);
-        case 2: return uni ? sweep_launch_scheme<real, 2, true>(ctx, A, vpb) : sweep_launch_scheme<real, 2, false>(ctx, A, vpb);
-        default: return uni ? sweep_launch_scheme<real, 1, true>(ctx, A, vpb) : sweep_launch_scheme<real, 1, false>(ctx, A, vpb);
+        case 4: return u ? sweep_launch_scheme<real, 4, true>(ctx, A, vpb, launch)
+                         : sweep_launch_scheme<real, 4, false>(ctx, A, vpb, launch);
+        case 2: return u ? sweep_launch_scheme<real, 2, true>(ctx, A, vpb, launch)
+                         : sweep_launch_scheme<real, 2, false>(ctx, A, vpb, launch);
+        default: return u ? sweep_launch_scheme<real, 1, true>(ctx, A, vpb, launch)
+                          : sweep_launch_scheme<real, 1, false>(ctx, A, vpb, launch);
     }
 }
 

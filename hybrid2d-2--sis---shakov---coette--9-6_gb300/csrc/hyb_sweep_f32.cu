@@ -2,8 +2,8 @@
 #include "hyb_sweep.cuh"
 
 namespace hyb {
-int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb) {
-    return sweep_launch_real<float>(ctx, A, cpt, vpb);
+int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb, bool launch) {
+    return sweep_launch_real<float>(ctx, A, cpt, vpb, launch);
 }
 size_t sweep_group_bytes_f32(int PA, int tpv) { return sweep_group_bytes<float>(PA, tpv); }
 }  // namespace hyb

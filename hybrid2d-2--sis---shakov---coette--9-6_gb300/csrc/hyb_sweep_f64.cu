@@ -2,8 +2,8 @@
 #include "hyb_sweep.cuh"
 
 namespace hyb {
-int sweep_launch_f64(hyb_ctx *ctx, const KinArgs<double> &A, int cpt, int vpb) {
-    return sweep_launch_real<double>(ctx, A, cpt, vpb);
+int sweep_launch_f64(hyb_ctx *ctx, const KinArgs<double> &A, int cpt, int vpb, bool launch) {
+    return sweep_launch_real<double>(ctx, A, cpt, vpb, launch);
 }
 size_t sweep_group_bytes_f64(int PA, int tpv) { return sweep_group_bytes<double>(PA, tpv); }
 }  // namespace hyb

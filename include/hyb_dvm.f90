@@ -168,5 +168,64 @@ module hyb_dvm
        type(c_ptr), value :: ctx
        type(c_ptr), intent(out) :: stream
      end function
+     integer(c_int) function hyb_autotune(ctx, reps, cpt, vpb) bind(c, name="hyb_autotune")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: reps
+       integer(c_int), intent(out) :: cpt, vpb
+     end function
+     integer(c_int) function hyb_batch_create(n, meshes, vgrids, params, batch) bind(c, name="hyb_batch_create")
+       import :: c_int, c_ptr, hyb_mesh, hyb_vgrid, hyb_params
+       integer(c_int), value :: n
+       type(hyb_mesh), intent(in) :: meshes(*)
+       type(hyb_vgrid), intent(in) :: vgrids(*)
+       type(hyb_params), intent(in) :: params(*)
+       type(c_ptr), intent(out) :: batch
+     end function
+     integer(c_int) function hyb_batch_destroy(batch) bind(c, name="hyb_batch_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: batch
+     end function
+     type(c_ptr) function hyb_batch_last_error(batch) bind(c, name="hyb_batch_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: batch
+     end function
+     integer(c_int) function hyb_batch_size(batch, n) bind(c, name="hyb_batch_size")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: batch
+       integer(c_int), intent(out) :: n
+     end function
+     integer(c_int) function hyb_batch_instance(batch, k, ctx) bind(c, name="hyb_batch_instance")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: batch
+       integer(c_int), value :: k
+       type(c_ptr), intent(out) :: ctx
+     end function
+     integer(c_int) function hyb_batch_init_maxwellian(batch, rho, u, v, t) bind(c, name="hyb_batch_init_maxwellian")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: batch
+       real(c_double), value :: rho, u, v, t
+     end function
+     integer(c_int) function hyb_batch_autotune(batch, reps) bind(c, name="hyb_batch_autotune")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: batch
+       integer(c_int), value :: reps
+     end function
+     integer(c_int) function hyb_batch_step(batch, n_iter, res) bind(c, name="hyb_batch_step")
+       import :: c_int, c_ptr, hyb_residual
+       type(c_ptr), value :: batch
+       integer(c_int), value :: n_iter
+       type(hyb_residual), intent(out) :: res(*)
+     end function
+     integer(c_int) function hyb_batch_last_step_ms(batch, ms) bind(c, name="hyb_batch_last_step_ms")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: batch
+       real(c_double), intent(out) :: ms
+     end function
+     integer(c_int) function hyb_batch_launch_count(batch, count) bind(c, name="hyb_batch_launch_count")
+       import :: c_int, c_ptr, c_long_long
+       type(c_ptr), value :: batch
+       integer(c_long_long), intent(out) :: count
+     end function
   end interface
 end module hyb_dvm

@@ -236,6 +236,37 @@ int hyb_last_step_ms(const hyb_ctx *ctx, double *ms);
 /* Raw CUDA stream handle (cudaStream_t) the context launches on. */
 int hyb_stream(const hyb_ctx *ctx, void **stream);
 
+/* ---- sweep launch-shape autotuner (no counterpart in the reference) ------ */
+/* Times every admissible sweep shape (cells per thread, velocity groups per
+ * CTA) for `reps` sweeps on the context's own distribution, restores f after
+ * each candidate and keeps the fastest shape for later steps.  The chosen
+ * shape is returned through cpt/vpb when they are not NULL. */
+int hyb_autotune(hyb_ctx *ctx, int reps, int *cpt, int *vpb);
+
+/* ---- batched instances (no counterpart in the reference; the reference
+ * runs one case per process) ---------------------------------------------- */
+/* n independent cases of any mesh / velocity-grid size on one device and one
+ * precision.  One outer iteration of all instances is captured into one CUDA
+ * graph with an independent branch per instance; hyb_batch_step launches it
+ * once per iteration.  res (n entries, may be NULL) receives each instance's
+ * DETFP_res after the last iteration. */
+typedef struct hyb_batch hyb_batch;
+int hyb_batch_create(int n, const hyb_mesh *meshes, const hyb_vgrid *vgrids,
+                     const hyb_params *params, hyb_batch **out);
+int hyb_batch_destroy(hyb_batch *b);
+const char *hyb_batch_last_error(const hyb_batch *b);
+int hyb_batch_size(const hyb_batch *b, int *n);
+/* The context of instance k (for state transfer and moments). */
+int hyb_batch_instance(hyb_batch *b, int k, hyb_ctx **ctx);
+int hyb_batch_init_maxwellian(hyb_batch *b, double rho, double u, double v, double t);
+/* hyb_autotune on every instance; the captured graphs are rebuilt. */
+int hyb_batch_autotune(hyb_batch *b, int reps);
+int hyb_batch_step(hyb_batch *b, int n_iter, hyb_residual *res);
+/* Milliseconds of the last hyb_batch_step (CUDA events around the graph
+ * launches) and kernel launches issued by the batch's graphs. */
+int hyb_batch_last_step_ms(const hyb_batch *b, double *ms);
+int hyb_batch_launch_count(const hyb_batch *b, long long *count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,99 @@
+"""Batched instances and the sweep-shape autotuner on the GPU.
+
+A batch runs each instance's own kernels, captured into one graph: with the
+default launch shapes every instance's state must be bit-identical to a
+standalone context of the same case after the same iterations, and within
+1e-11 of the oracle.  The autotuner may change the sweep shape (and so the
+association of the scan), which keeps the FP64 state within 1e-11.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+from test_gpu_parity import _cmp_state, _interior_f
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cases_mod(pkg):
+    from hyb_gb300 import cases
+    return cases
+
+
+def _mixed_cases(cases_mod):
+    return [
+        cases_mod.couette_small(ncy=32, nvx=12, nvy=12, kn=0.5, uw=0.3, dt=0.02),
+        cases_mod.couette_small(ncy=64, nvx=16, nvy=16, kn=0.05, uw=0.1, dt=0.01),
+        cases_mod.couette_small(ncy=16, nvx=8, nvy=8, kn=2.0, uw=0.6, t_top=1.3, dt=0.04),
+        cases_mod.couette_small(ncy=128, nvx=12, nvy=12, kn=0.01, uw=0.4, dt=0.005),
+    ]
+
+
+def test_batch_matches_standalone_contexts(cases_mod):
+    from hyb_gb300 import abi
+    cl = _mixed_cases(cases_mod)
+    b = abi.Batch(cl, precision=0)
+    b.init_maxwellian()
+    rb = b.step(5)
+    for k, c in enumerate(cl):
+        s = abi.Solver(c, precision=0)
+        s.init_maxwellian()
+        rs = s.step(5)
+        inst = b.instance(k)
+        assert np.array_equal(inst.download_f(), s.download_f()), k
+        sb, cb = inst.moments()
+        ss, cs = s.moments()
+        assert np.array_equal(sb, ss) and np.array_equal(cb, cs), k
+        assert rb[k]["max_rms"] == rs["max_rms"], k
+    assert b.launches() > 0 and b.last_ms() > 0.0
+
+
+def test_batch_instance_matches_oracle(cases_mod):
+    from hyb_gb300 import abi
+    cl = _mixed_cases(cases_mod)
+    b = abi.Batch(cl, precision=0)
+    b.init_maxwellian()
+    b.step(3)
+    for k in (0, 3):
+        o = O.Oracle(cl[k], threads=0)
+        o.init_maxwellian()
+        o.convert_ns()
+        o.step(3)
+        _cmp_state(cl[k], b.instance(k), o, 1e-11)
+
+
+def test_autotune_keeps_results(cases_mod):
+    from hyb_gb300 import abi
+    c = cases_mod.couette_small(ncy=128, nvx=16, nvy=16, dt=0.01)
+    s = abi.Solver(c, precision=0)
+    s.init_maxwellian()
+    f0 = s.download_f()
+    cpt, vpb = s.autotune(reps=2)
+    assert cpt in (1, 2, 4) and vpb in (1, 2, 4, 8)
+    assert np.array_equal(s.download_f(), f0)      # f restored after timing
+    s.step(3)
+    o = O.Oracle(c, threads=0)
+    o.init_maxwellian()
+    o.convert_ns()
+    o.step(3)
+    _cmp_state(c, s, o, 1e-11)
+
+
+def test_batch_autotune_and_mixed_precision(cases_mod):
+    from hyb_gb300 import abi
+    cl = _mixed_cases(cases_mod)
+    b = abi.Batch(cl, precision=1)
+    b.init_maxwellian()
+    b.autotune(reps=2)
+    r = b.step(20)
+    for k, c in enumerate(cl):
+        o = O.Oracle(c, threads=0)
+        o.init_maxwellian()
+        o.convert_ns()
+        o.step(20)
+        fb = _interior_f(c, b.instance(k).download_f())
+        fo = _interior_f(c, o.frd())
+        assert np.abs(fb - fo).max() < 5e-5 * np.abs(fo).max(), k
+        assert np.isfinite(r[k]["max_rms"])
