@@ -24,6 +24,10 @@ EXPORTS = [
     "hyb_batch_create", "hyb_batch_destroy", "hyb_batch_last_error", "hyb_batch_size",
     "hyb_batch_instance", "hyb_batch_init_maxwellian", "hyb_batch_autotune", "hyb_batch_step",
     "hyb_batch_last_step_ms", "hyb_batch_launch_count",
+    "hyb_mlp_create", "hyb_mlp_destroy", "hyb_mlp_last_error", "hyb_mlp_param_count",
+    "hyb_mlp_get_params", "hyb_mlp_set_params", "hyb_mlp_set_norm", "hyb_mlp_set_data",
+    "hyb_mlp_train_epoch", "hyb_mlp_grad", "hyb_mlp_predict", "hyb_mlp_forward_dev",
+    "hyb_mlp_last_ms", "hyb_mlp_launch_count",
 ]
 STAGES = ["wall", "sweep", "moments", "sghost", "convert_ns", "gsis", "residual"]
 
@@ -78,6 +82,21 @@ def load(path=None):
     L.hyb_batch_step.argtypes = [vp, ip, vp]
     L.hyb_batch_last_step_ms.argtypes = [vp, dp]
     L.hyb_batch_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+    fp = C.POINTER(C.c_float)
+    L.hyb_mlp_create.argtypes = [ip, C.c_ulonglong, C.POINTER(vp)]
+    L.hyb_mlp_destroy.argtypes = [vp]
+    L.hyb_mlp_last_error.argtypes = [vp]
+    L.hyb_mlp_last_error.restype = C.c_char_p
+    L.hyb_mlp_get_params.argtypes = [vp, fp]
+    L.hyb_mlp_set_params.argtypes = [vp, fp]
+    L.hyb_mlp_set_norm.argtypes = [vp, fp, fp, fp, fp]
+    L.hyb_mlp_set_data.argtypes = [vp, fp, fp, ip]
+    L.hyb_mlp_train_epoch.argtypes = [vp, C.POINTER(ip), ip, C.c_float, fp]
+    L.hyb_mlp_grad.argtypes = [vp, fp, fp, ip, fp, fp]
+    L.hyb_mlp_predict.argtypes = [vp, fp, ip, fp]
+    L.hyb_mlp_forward_dev.argtypes = [vp, vp, ip, vp, vp]
+    L.hyb_mlp_last_ms.argtypes = [vp, dp]
+    L.hyb_mlp_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.hyb_profile_enable.argtypes = [vp, ip]
     L.hyb_profile_read.argtypes = [vp, dp, C.POINTER(C.c_longlong), ip]
     L.hyb_detfp_noalloc.argtypes = [ip, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -303,3 +322,91 @@ class Batch:
         x = C.c_longlong()
         self._ck(self.L.hyb_batch_launch_count(self.h, C.byref(x)), "batch_launch_count")
         return x.value
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp:
+    """The learned closure network on the GPU (hyb_mlp_*)."""
+
+    NPARAM = 9156
+
+    def __init__(self, seed=0, device=0):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.hyb_mlp_create(device, seed, C.byref(h))
+        if rc != 0:
+            raise HybError(rc, "hyb_mlp_create failed")
+        self.h = h
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = self.L.hyb_mlp_last_error(self.h).decode() if self.h else ""
+            raise HybError(rc, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.hyb_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        w = np.zeros(self.NPARAM, dtype=np.float32)
+        self._ck(self.L.hyb_mlp_get_params(self.h, _fp(w)), "get_params")
+        return w
+
+    def set_params(self, w):
+        w = _f32(w)
+        assert w.size == self.NPARAM
+        self._ck(self.L.hyb_mlp_set_params(self.h, _fp(w)), "set_params")
+
+    def set_norm(self, in_mean, in_std, out_mean, out_std):
+        a = [_f32(v) for v in (in_mean, in_std, out_mean, out_std)]
+        self._norm = a
+        self._ck(self.L.hyb_mlp_set_norm(self.h, *[_fp(v) for v in a]), "set_norm")
+
+    def set_data(self, x, y):
+        x, y = _f32(x), _f32(y)
+        self._ck(self.L.hyb_mlp_set_data(self.h, _fp(x), _fp(y), x.shape[0]), "set_data")
+        self.n = x.shape[0]
+
+    def train_epoch(self, perm, batch=8192, lr=1e-3):
+        perm = np.ascontiguousarray(perm, dtype=np.int32)
+        out = C.c_float(0.0)
+        self._ck(self.L.hyb_mlp_train_epoch(self.h, perm.ctypes.data_as(C.POINTER(C.c_int)), batch, lr,
+                                            C.byref(out)), "train_epoch")
+        return out.value
+
+    def grad(self, x, y):
+        x, y = _f32(x), _f32(y)
+        g = np.zeros(self.NPARAM, dtype=np.float32)
+        loss = C.c_float(0.0)
+        self._ck(self.L.hyb_mlp_grad(self.h, _fp(x), _fp(y), x.shape[0], _fp(g), C.byref(loss)), "grad")
+        return loss.value, g
+
+    def predict(self, x):
+        x = _f32(x)
+        y = np.zeros((x.shape[0], 4), dtype=np.float32)
+        self._ck(self.L.hyb_mlp_predict(self.h, _fp(x), x.shape[0], _fp(y)), "predict")
+        return y
+
+    def last_ms(self):
+        v = C.c_double()
+        self._ck(self.L.hyb_mlp_last_ms(self.h, C.byref(v)), "last_ms")
+        return v.value
+
+    def launches(self):
+        v = C.c_longlong()
+        self._ck(self.L.hyb_mlp_launch_count(self.h, C.byref(v)), "launch_count")
+        return v.value

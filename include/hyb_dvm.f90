@@ -227,5 +227,80 @@ module hyb_dvm
        type(c_ptr), value :: batch
        integer(c_long_long), intent(out) :: count
      end function
+     integer(c_int) function hyb_mlp_create(device, seed, net) bind(c, name="hyb_mlp_create")
+       import :: c_int, c_ptr, c_long_long
+       integer(c_int), value :: device
+       integer(c_long_long), value :: seed
+       type(c_ptr), intent(out) :: net
+     end function
+     integer(c_int) function hyb_mlp_destroy(net) bind(c, name="hyb_mlp_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: net
+     end function
+     type(c_ptr) function hyb_mlp_last_error(net) bind(c, name="hyb_mlp_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: net
+     end function
+     integer(c_int) function hyb_mlp_param_count() bind(c, name="hyb_mlp_param_count")
+       import :: c_int
+     end function
+     integer(c_int) function hyb_mlp_get_params(net, w) bind(c, name="hyb_mlp_get_params")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(out) :: w(*)
+     end function
+     integer(c_int) function hyb_mlp_set_params(net, w) bind(c, name="hyb_mlp_set_params")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(in) :: w(*)
+     end function
+     integer(c_int) function hyb_mlp_set_norm(net, in_mean, in_std, out_mean, out_std) bind(c, name="hyb_mlp_set_norm")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(in) :: in_mean(8), in_std(8), out_mean(4), out_std(4)
+     end function
+     integer(c_int) function hyb_mlp_set_data(net, x, y, n) bind(c, name="hyb_mlp_set_data")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(in) :: x(*), y(*)
+       integer(c_int), value :: n
+     end function
+     integer(c_int) function hyb_mlp_train_epoch(net, perm, batch, lr, mean_loss) bind(c, name="hyb_mlp_train_epoch")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       integer(c_int), intent(in) :: perm(*)
+       integer(c_int), value :: batch
+       real(c_float), value :: lr
+       real(c_float), intent(out) :: mean_loss
+     end function
+     integer(c_int) function hyb_mlp_grad(net, x, y, n, grad, loss) bind(c, name="hyb_mlp_grad")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(in) :: x(*), y(*)
+       integer(c_int), value :: n
+       real(c_float), intent(out) :: grad(*), loss
+     end function
+     integer(c_int) function hyb_mlp_predict(net, x, n, y) bind(c, name="hyb_mlp_predict")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: net
+       real(c_float), intent(in) :: x(*)
+       integer(c_int), value :: n
+       real(c_float), intent(out) :: y(*)
+     end function
+     integer(c_int) function hyb_mlp_forward_dev(net, x_dev, n, y_dev, stream) bind(c, name="hyb_mlp_forward_dev")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: net, x_dev, y_dev, stream
+       integer(c_int), value :: n
+     end function
+     integer(c_int) function hyb_mlp_last_ms(net, ms) bind(c, name="hyb_mlp_last_ms")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: net
+       real(c_double), intent(out) :: ms
+     end function
+     integer(c_int) function hyb_mlp_launch_count(net, count) bind(c, name="hyb_mlp_launch_count")
+       import :: c_int, c_ptr, c_long_long
+       type(c_ptr), value :: net
+       integer(c_long_long), intent(out) :: count
+     end function
   end interface
 end module hyb_dvm

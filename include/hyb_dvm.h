@@ -267,6 +267,41 @@ int hyb_batch_step(hyb_batch *b, int n_iter, hyb_residual *res);
 int hyb_batch_last_step_ms(const hyb_batch *b, double *ms);
 int hyb_batch_launch_count(const hyb_batch *b, long long *count);
 
+/* ---- learned closure (no counterpart in the reference) ------------------ */
+/* MLP 8 -> 64 -> 64 -> 64 -> 4, tanh hidden layers, 9,156 parameters; BF16
+ * weights/activations on the tensor cores with FP32 accumulation, FP32 master
+ * weights and Adam (beta 0.9 / 0.999, eps 1e-8).  Inputs (per face): log10
+ * local Kn, rho, T, du/dn, dT/dn, NSF shear stress, NSF normal heat flux,
+ * wall distance; outputs: the non-NSF shear stress, half normal-stress
+ * difference and heat-flux components.  Parameter layout (FP32): W1[64][8]
+ * b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[4][64] b4[4].  Inputs are
+ * normalised as (x - in_mean) / in_std and outputs returned as
+ * y_norm * out_std + out_mean; the loss is the mean squared error of the
+ * normalised outputs.  Host arrays unless the name says _dev. */
+typedef struct hyb_mlp hyb_mlp;
+int hyb_mlp_create(int device, unsigned long long seed, hyb_mlp **out);
+int hyb_mlp_destroy(hyb_mlp *m);
+const char *hyb_mlp_last_error(const hyb_mlp *m);
+int hyb_mlp_param_count(void);
+int hyb_mlp_get_params(hyb_mlp *m, float *w);
+/* Replaces the weights and resets the Adam state. */
+int hyb_mlp_set_params(hyb_mlp *m, const float *w);
+int hyb_mlp_set_norm(hyb_mlp *m, const float *in_mean, const float *in_std,
+                     const float *out_mean, const float *out_std);
+/* Training set x[n][8], y[n][4], kept on the device. */
+int hyb_mlp_set_data(hyb_mlp *m, const float *x, const float *y, int n);
+/* One epoch of Adam steps over minibatches perm[0:batch], perm[batch:2 batch],
+ * ... of the training set; mean_loss = mean loss over the epoch. */
+int hyb_mlp_train_epoch(hyb_mlp *m, const int *perm, int batch, float lr, float *mean_loss);
+/* Gradient of the mean loss over x[n], y[n] at the current weights (no
+ * update), in the parameter layout above. */
+int hyb_mlp_grad(hyb_mlp *m, const float *x, const float *y, int n, float *grad, float *loss);
+int hyb_mlp_predict(hyb_mlp *m, const float *x, int n, float *y);
+/* Device-pointer inference on a caller stream (NULL: the network's own). */
+int hyb_mlp_forward_dev(hyb_mlp *m, const float *x_dev, int n, float *y_dev, void *stream);
+int hyb_mlp_last_ms(const hyb_mlp *m, double *ms);
+int hyb_mlp_launch_count(const hyb_mlp *m, long long *count);
+
 #ifdef __cplusplus
 }
 #endif
