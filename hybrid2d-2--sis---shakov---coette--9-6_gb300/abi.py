@@ -189,16 +189,18 @@ class Solver:
         gp.max_inner = kw.get("max_inner", 2000)
         gp.inner_tol = kw.get("inner_tol", 1e-6)
         gp.inner_rtol = kw.get("inner_rtol", 0.0)
-        gp.reserved[0] = kw.get("plane_order", 0)
+        gp.lusgs_planes = kw.get("plane_order", 0)
         gp.cfl = kw.get("cfl", 20.0)
         gp.dtmax = kw.get("dtmax", 10.0)
         gp.dtmin = kw.get("dtmin", 1e-7)
         gp.flux = kw.get("flux", 5)
         gp.ns_scheme = kw.get("ns_scheme", 1)
-        gp.use_mlp = kw.get("use_mlp", 0)
+        gp.mlp_warm_after = kw.get("mlp_warm_after", 0)
+        gp.mlp_warm_inner = kw.get("mlp_warm_inner", 0)
+        gp.mlp_warm_rtol = kw.get("mlp_warm_rtol", 0.0)
         gp.ns_solver = kw.get("ns_solver", 0)
-        gp.reserved[1] = kw.get("no_mass_projection", 0)
-        gp.reserved[2] = kw.get("correct_f", 0)
+        gp.no_mass_projection = kw.get("no_mass_projection", 0)
+        gp.correct_f = kw.get("correct_f", 0)
         self._ck(self.L.hyb_gsis_configure(self.h, C.byref(gp)), "gsis_configure")
 
     def gsis_last_inner(self):

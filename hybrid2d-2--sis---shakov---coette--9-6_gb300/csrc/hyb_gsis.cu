@@ -782,9 +782,9 @@ int ns_create(hyb_ctx *ctx) {
         NsState *st = (NsState *)ctx->ns;
         if (st->have_graph) cudaGraphExecDestroy(st->graph);
         st->have_graph = false;
-        st->D.mass_proj = ctx->gsis.reserved[1] == 0;
+        st->D.mass_proj = ctx->gsis.no_mass_projection == 0;
         st->D.ns_scheme = ctx->gsis.ns_scheme;
-        st->D.correct_f = ctx->gsis.reserved[2] != 0;
+        st->D.correct_f = ctx->gsis.correct_f != 0;
         return HYB_OK;
     }
     if ((ctx->nx < 7 && ctx->bc[0] != HYB_BC_PERIODIC) || (ctx->ny < 7 && ctx->bc[1] != HYB_BC_PERIODIC)) {
@@ -863,9 +863,9 @@ int ns_create(hyb_ctx *ctx) {
     D.rk = st->rk;
     D.PA = ctx->PA;
     D.scan_is_j = ctx->scan_is_j;
-    D.mass_proj = ctx->gsis.reserved[1] == 0;
+    D.mass_proj = ctx->gsis.no_mass_projection == 0;
     D.ns_scheme = ctx->gsis.ns_scheme;
-    D.correct_f = ctx->gsis.reserved[2] != 0;
+    D.correct_f = ctx->gsis.correct_f != 0;
     D.src_on = 1;
     D.gamma = ctx->prm.gamma;
     D.ma = ctx->prm.ma;

@@ -72,8 +72,10 @@ class HybGsisParams(C.Structure):
     _fields_ = [
         ("enable", C.c_int), ("max_inner", C.c_int), ("inner_tol", C.c_double),
         ("inner_rtol", C.c_double), ("cfl", C.c_double), ("dtmax", C.c_double), ("dtmin", C.c_double),
-        ("flux", C.c_int), ("ns_scheme", C.c_int), ("use_mlp", C.c_int),
-        ("ns_solver", C.c_int), ("reserved", C.c_int * 4),
+        ("flux", C.c_int), ("ns_scheme", C.c_int), ("mlp_warm_after", C.c_int),
+        ("ns_solver", C.c_int), ("correct_f", C.c_int), ("no_mass_projection", C.c_int),
+        ("lusgs_planes", C.c_int), ("mlp_warm_inner", C.c_int), ("mlp_warm_rtol", C.c_double),
+        ("reserved", C.c_int * 2),
     ]
 
 

@@ -43,8 +43,10 @@ module hyb_dvm
   type, bind(c) :: hyb_gsis_params
      integer(c_int) :: enable, max_inner
      real(c_double) :: inner_tol, inner_rtol, cfl, dtmax, dtmin
-     integer(c_int) :: flux, ns_scheme, use_mlp, ns_solver
-     integer(c_int) :: reserved(4)
+     integer(c_int) :: flux, ns_scheme, mlp_warm_after, ns_solver
+     integer(c_int) :: correct_f, no_mass_projection, lusgs_planes, mlp_warm_inner
+     real(c_double) :: mlp_warm_rtol
+     integer(c_int) :: reserved(2)
   end type hyb_gsis_params
 
   interface

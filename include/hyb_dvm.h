@@ -127,14 +127,26 @@ typedef struct hyb_gsis_params {
                                value at the first inner iteration (0: off)   */
     double cfl, dtmax, dtmin;   /* local time step (sub_NS_singlegrid.f90:160-183) */
     int    flux;            /* NS flux splitting, Flux_* (COMMONDATA.f90:12) */
-    int    ns_scheme;       /* NS reconstruction scheme, Scheme_* (:11)      */
-    int    use_mlp;         /* use the learned closure as warm start         */
+    int    ns_scheme;       /* NS reconstruction: 1 NND2 (Scheme_*, :11), 0 first
+                               order, 2 NND2 stencil without the limiter      */
+    int    mlp_warm_after;  /* > 0: after this many outer iterations since
+                               configuration, hyb_step runs the learned warm
+                               start once (hyb_gsis_warm_start)              */
     int    ns_solver;       /* inner solver: 0 LU-SGS (du_LU_SGS_2D,
                                sub_LU_SGS.f90), 1 line-implicit ADI with the
                                LU-SGS diagonal and scalar couplings, exact
                                along each mesh line (no counterpart in the
                                reference)                                    */
-    int    reserved[4];
+    int    correct_f;       /* 1: after the moment correction also correct the
+                               distribution, f += feq(S) - feq(S_k) on the band
+                               (the reference corrects the moments only)     */
+    int    no_mass_projection;  /* 1: keep the band's mean density change   */
+    int    lusgs_planes;    /* oracle only: the reference's anti-diagonal
+                               LU-SGS order instead of two colours           */
+    int    mlp_warm_inner;  /* inner iterations of the warm start (0: 2000) */
+    double mlp_warm_rtol;   /* ... or until max|Res(4)| drops by this factor
+                               (0: 1e-3)                                     */
+    int    reserved[2];
 } hyb_gsis_params;
 
 typedef struct hyb_ctx hyb_ctx;

@@ -33,7 +33,7 @@
  *   - The inner LU-SGS uses the reference's algebra (alpha, comput_DFn,
  *     spectral radii) with a two-colour cell ordering: forward sweep red then
  *     black, backward sweep black then red, dU reset to 0 at each inner
- *     iteration.  HYB_ORC_LUSGS_PLANES=1 (gsis.reserved[0]) selects the
+ *     iteration.  lusgs_planes = 1 in hyb_gsis_params selects the
  *     reference's anti-diagonal order instead.
  */
 #include "hyb_oracle_impl.h"
@@ -431,7 +431,7 @@ static void lusgs_bwd_cell(orc *o, int i, int j, int ihi, int jhi)
 static void ns_lusgs(orc *o, int ilo, int ihi, int jlo, int jhi)
 {
     struct orc_ns *ns = o->ns;
-    if (o->gsis.reserved[0] == 1) {   /* reference anti-diagonal order */
+    if (o->gsis.lusgs_planes == 1) {   /* reference anti-diagonal order */
         for (int plane = ilo + jlo; plane <= ihi + jhi; plane++)
             for (int j = jlo; j <= jhi; j++) {
                 int i = plane - j;
@@ -658,7 +658,7 @@ int orc_gsis_solve(orc *o)
     /* the band's Dirichlet edges make the NS density change non-conservative;
      * its volume-weighted mean is removed so that the correction adds no mass */
     double lam = 0.0;
-    if (o->gsis.reserved[1] == 0) {
+    if (o->gsis.no_mass_projection == 0) {
         double num = 0.0, den = 0.0;
         for (int j = jlo; j <= jhi; j++)
             for (int i = ilo; i <= ihi; i++) {
@@ -709,7 +709,7 @@ int orc_gsis_solve(orc *o)
     /* optional distribution correction f += feq(S) - feq(S_k) on the band
      * (the usual GSIS step; the reference corrects the moments only), with
      * the sweep's floor */
-    if (o->gsis.reserved[2]) {
+    if (o->gsis.correct_f) {
 #pragma omp parallel for schedule(static)
         for (int v = 0; v < o->nv; v++) {
             int iv = v % o->nvi, jv = v / o->nvi;

@@ -161,11 +161,13 @@ class Oracle:
         gp.dtmin = kw.get("dtmin", 1e-7)
         gp.flux = kw.get("flux", 5)
         gp.ns_scheme = kw.get("ns_scheme", 1)
-        gp.use_mlp = kw.get("use_mlp", 0)
+        gp.mlp_warm_after = kw.get("mlp_warm_after", 0)
+        gp.mlp_warm_inner = kw.get("mlp_warm_inner", 0)
+        gp.mlp_warm_rtol = kw.get("mlp_warm_rtol", 0.0)
         gp.ns_solver = kw.get("ns_solver", 0)
-        gp.reserved[0] = kw.get("plane_order", 0)
-        gp.reserved[1] = kw.get("no_mass_projection", 0)
-        gp.reserved[2] = kw.get("correct_f", 0)
+        gp.lusgs_planes = kw.get("plane_order", 0)
+        gp.no_mass_projection = kw.get("no_mass_projection", 0)
+        gp.correct_f = kw.get("correct_f", 0)
         rc = self.L.orc_gsis_configure(self.h, C.byref(gp))
         if rc != 0:
             raise RuntimeError(f"orc_gsis_configure failed: {rc}")

@@ -47,7 +47,7 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu\n", sizeof(hyb_mesh), sizeof(hyb_vgrid), sizeof(hyb_params),
          sizeof(hyb_residual), sizeof(hyb_gsis_params));
   printf("%zu %zu %zu %zu\n", offsetof(hyb_mesh, wall_t), offsetof(hyb_params, omega_ns),
-         offsetof(hyb_params, device), offsetof(hyb_gsis_params, use_mlp));
+         offsetof(hyb_params, device), offsetof(hyb_gsis_params, mlp_warm_after));
   return 0;
 }
 '''
@@ -59,7 +59,7 @@ int main(void) {
     sizes = [C.sizeof(T.HybMesh), C.sizeof(T.HybVgrid), C.sizeof(T.HybParams), C.sizeof(T.HybResidual),
              C.sizeof(T.HybGsisParams)]
     offs = [T.HybMesh.wall_t.offset, T.HybParams.omega_ns.offset, T.HybParams.device.offset,
-            T.HybGsisParams.use_mlp.offset]
+            T.HybGsisParams.mlp_warm_after.offset]
     assert [int(x) for x in out] == sizes + offs
 
 
