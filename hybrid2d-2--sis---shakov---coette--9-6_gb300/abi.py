@@ -27,7 +27,8 @@ EXPORTS = [
     "hyb_mlp_create", "hyb_mlp_destroy", "hyb_mlp_last_error", "hyb_mlp_param_count",
     "hyb_mlp_get_params", "hyb_mlp_set_params", "hyb_mlp_set_norm", "hyb_mlp_set_data",
     "hyb_mlp_train_epoch", "hyb_mlp_grad", "hyb_mlp_predict", "hyb_mlp_forward_dev",
-    "hyb_mlp_last_ms", "hyb_mlp_launch_count",
+    "hyb_mlp_last_ms", "hyb_mlp_launch_count", "hyb_gsis_attach_mlp", "hyb_gsis_warm_start",
+    "hyb_closure_samples",
 ]
 STAGES = ["wall", "sweep", "moments", "sghost", "convert_ns", "gsis", "residual"]
 
@@ -97,6 +98,9 @@ def load(path=None):
     L.hyb_mlp_forward_dev.argtypes = [vp, vp, ip, vp, vp]
     L.hyb_mlp_last_ms.argtypes = [vp, dp]
     L.hyb_mlp_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.hyb_gsis_attach_mlp.argtypes = [vp, vp]
+    L.hyb_gsis_warm_start.argtypes = [vp]
+    L.hyb_closure_samples.argtypes = [vp, fp, fp, ip, C.POINTER(ip)]
     L.hyb_profile_enable.argtypes = [vp, ip]
     L.hyb_profile_read.argtypes = [vp, dp, C.POINTER(C.c_longlong), ip]
     L.hyb_detfp_noalloc.argtypes = [ip, ip, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -144,6 +148,25 @@ class Solver:
         if getattr(self, "h", None) and getattr(self, "owned", True):
             self.L.hyb_destroy(self.h)
         self.h = None
+
+    def attach_mlp(self, net):
+        self._mlp = net
+        self._ck(self.L.hyb_gsis_attach_mlp(self.h, net.h if net is not None else None), "gsis_attach_mlp")
+
+    def warm_start(self):
+        self._ck(self.L.hyb_gsis_warm_start(self.h), "gsis_warm_start")
+
+    def closure_samples(self):
+        """Closure-network inputs [n][8] and targets [n][4] of every j-face of
+        the current kinetic state."""
+        n = C.c_int(0)
+        self._ck(self.L.hyb_closure_samples(self.h, None, None, 0, C.byref(n)), "closure_samples")
+        x = np.zeros((n.value, 8), dtype=np.float32)
+        y = np.zeros((n.value, 4), dtype=np.float32)
+        self._ck(self.L.hyb_closure_samples(self.h, x.ctypes.data_as(C.POINTER(C.c_float)),
+                                            y.ctypes.data_as(C.POINTER(C.c_float)), n.value, C.byref(n)),
+                 "closure_samples")
+        return x, y
 
     def autotune(self, reps=3):
         """Time every admissible sweep shape; returns the chosen (cpt, vpb)."""

@@ -530,6 +530,19 @@ int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
         if (!rc) rc = staged(ctx, ST_SGHOST, &evi, [&] { return hyb::launch_sghost(ctx); });
         if (!rc) rc = staged(ctx, ST_CNS, &evi, [&] { return hyb::launch_convert_ns(ctx); });
         if (!rc && ctx->gsis.enable) rc = staged(ctx, ST_GSIS, &evi, [&] { return hyb::gsis_solve(ctx); });
+        if (!rc && ctx->gsis.enable) {
+            ctx->gsis_outer++;
+            if (ctx->gsis.mlp_warm_after > 0 && !ctx->warm_done && ctx->gsis_outer >= ctx->gsis.mlp_warm_after) {
+                ctx->warm_done = 1;
+                rc = staged(ctx, ST_GSIS, &evi, [&] { return hyb::gsis_warm_start(ctx); });
+                // a closure solve that left the physical range corrected nothing:
+                // the kinetic iteration goes on from its own state
+                if (rc == HYB_ERR_TEMPERATURE || rc == HYB_ERR_NONFINITE) {
+                    ctx->warm_done = 2;
+                    rc = HYB_OK;
+                }
+            }
+        }
         if (rc) return rc;
     }
     ctx->rhs_valid = 1;
@@ -688,6 +701,8 @@ int hyb_download_hot(hyb_ctx *ctx, double *tao_i, double *q_i, double *tao_j, do
 int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp) {
     if (!ctx || !gp) return HYB_ERR_INVALID;
     ctx->gsis = *gp;
+    ctx->gsis_outer = 0;
+    ctx->warm_done = 0;
     if (gp->enable) return hyb::ns_create(ctx);
     return HYB_OK;
 }

@@ -114,6 +114,9 @@ struct hyb_ctx {
     // GSIS
     hyb_gsis_params gsis;
     int gsis_last_inner;
+    hyb_mlp *mlp;                          // learned closure for the warm start (not owned)
+    int gsis_outer;                        // outer iterations since hyb_gsis_configure
+    int warm_done;                         // the scheduled warm start has run (2: fell back)
     void *ns;                              // NS solver state (hyb_ns.cu)
 };
 
@@ -148,4 +151,5 @@ int launch_convert_ns(hyb_ctx *ctx);
 int ns_create(hyb_ctx *ctx);
 void ns_destroy(hyb_ctx *ctx);
 int gsis_solve(hyb_ctx *ctx);
+int gsis_warm_start(hyb_ctx *ctx);
 }  // namespace hyb

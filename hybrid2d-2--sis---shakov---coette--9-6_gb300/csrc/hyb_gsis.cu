@@ -70,6 +70,10 @@ struct NsDev {
     const double *tin_i, *qin_i, *tin_j, *qin_j;            // NSF of the kinetic state
     double *S;                                               // [NSUM][nc]
     NsCtrl *ctrl;
+    // learned closure (warm start): j-face features and network outputs
+    int mlp_on;
+    double kn;                                               // reference Kn
+    float *mlp_x, *mlp_y;                                    // [(nx-1) ny][8] / [.][4]
 };
 
 struct NsState {
@@ -81,10 +85,96 @@ struct NsState {
     double *rk;             // [4][Nb*PA]
     cudaGraphExec_t graph;
     bool have_graph;
+    float *mlp_buf;         // closure features and outputs
 };
 
 __device__ __forceinline__ size_t c2(const NsDev &D, int i, int j) { return hyb_c2(D.nx, i, j); }
 __device__ __forceinline__ size_t mi(const NsDev &D, int i, int j) { return (size_t)(i - 1) + (size_t)D.nx * (j - 1); }
+
+// ---- learned-closure features of a j-face ------------------------------------
+// Face (i, j) between cells (i, j-1) and (i, j), the face of get_viscous in
+// Residual_FVM (sub_Residual.f90:278-342): 0 log10 of the local Knudsen
+// number Kn / rho (hard-sphere mean free path), 1 rho, 2 T, 3 du/dy,
+// 4 dT/dy, 5 NSF shear stress, 6 NSF heat flux q_y, 7 distance to the
+// nearer wall (1 without walls).  Primitive arrays on the C2 extents.
+struct Prims {
+    const double *d, *uu, *vv, *T, *amu, *x1, *y1;
+    int nx, ny, pery;
+    double cp, pr, kn;
+};
+
+__device__ void jface_features(const Prims &P, int i, int j, float *f) {
+    auto C = [&](int a, int b) { return hyb_c2(P.nx, a, b); };
+    const bool lo = (j == 1) && !P.pery, hi = (j == P.ny) && !P.pery;
+    double amu1, amk1;
+    if (lo) { amu1 = P.amu[C(i, j)]; amk1 = P.cp * (P.amu[C(i, j)] / P.pr); }
+    else if (hi) { amu1 = P.amu[C(i, j - 1)]; amk1 = P.cp * (P.amu[C(i, j - 1)] / P.pr); }
+    else { amu1 = (P.amu[C(i, j)] + P.amu[C(i, j - 1)]) * 0.5;
+           amk1 = P.cp * ((P.amu[C(i, j - 1)] + P.amu[C(i, j)]) / P.pr) * 0.5; }
+    const double *x1 = P.x1, *y1 = P.y1, *uu = P.uu, *vv = P.vv, *T = P.T;
+    const double dix = (x1[C(i + 1, j - 1)] + x1[C(i + 1, j)] - x1[C(i - 1, j - 1)] - x1[C(i - 1, j)]) * 0.25;
+    const double diy = (y1[C(i + 1, j - 1)] + y1[C(i + 1, j)] - y1[C(i - 1, j - 1)] - y1[C(i - 1, j)]) * 0.25;
+    const double djx = x1[C(i, j)] - x1[C(i, j - 1)], djy = y1[C(i, j)] - y1[C(i, j - 1)];
+    const double diu = (uu[C(i + 1, j - 1)] + uu[C(i + 1, j)] - uu[C(i - 1, j - 1)] - uu[C(i - 1, j)]) * 0.25;
+    const double div = (vv[C(i + 1, j - 1)] + vv[C(i + 1, j)] - vv[C(i - 1, j - 1)] - vv[C(i - 1, j)]) * 0.25;
+    const double dit = (T[C(i + 1, j - 1)] + T[C(i + 1, j)] - T[C(i - 1, j - 1)] - T[C(i - 1, j)]) * 0.25;
+    const double dju = uu[C(i, j)] - uu[C(i, j - 1)], djv = vv[C(i, j)] - vv[C(i, j - 1)];
+    const double djt = T[C(i, j)] - T[C(i, j - 1)];
+    const double ds = 1.0 / (dix * djy - djx * diy);
+    const double vx = (div * djy - djv * diy) * ds;
+    const double uy = (-diu * djx + dju * dix) * ds, ty = (-dit * djx + djt * dix) * ds;
+    const double rf = 0.5 * (P.d[C(i, j - 1)] + P.d[C(i, j)]);
+    const double tf = 0.5 * (T[C(i, j - 1)] + T[C(i, j)]);
+    double wd = 1.0;
+    if (!P.pery) {
+        const double yf = 0.5 * (y1[C(i, j - 1)] + y1[C(i, j)]);
+        const double ylo = 0.5 * (y1[C(i, 0)] + y1[C(i, 1)]), yhi = 0.5 * (y1[C(i, P.ny - 1)] + y1[C(i, P.ny)]);
+        wd = fmin(yf - ylo, yhi - yf);
+    }
+    f[0] = (float)log10(P.kn / rf);
+    f[1] = (float)rf;
+    f[2] = (float)tf;
+    f[3] = (float)uy;
+    f[4] = (float)ty;
+    f[5] = (float)((uy + vx) * amu1);
+    f[6] = (float)(amk1 * ty);
+    f[7] = (float)wd;
+}
+
+// closure targets of a j-face: the HoT of Convert_NS as (t12, t22, qx, qy),
+// the stress components a face normal to y carries
+__device__ void jface_targets(const double *tg_j, const double *qg_j, size_t nc, size_t c, float *y) {
+    y[0] = (float)tg_j[2 * nc + c];
+    y[1] = (float)tg_j[nc + c];
+    y[2] = (float)qg_j[c];
+    y[3] = (float)qg_j[nc + c];
+}
+
+// training samples of the kinetic state (Convert_NS arrays in d_hot)
+__global__ void k_closure_samples(Prims P, const double *tg_j, const double *qg_j, size_t nc, float *x, float *y) {
+    const int nf = (P.nx - 1) * P.ny;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int i = f % (P.nx - 1) + 1, j = f / (P.nx - 1) + 1;
+    jface_features(P, i, j, x + (size_t)f * 8);
+    jface_targets(tg_j, qg_j, nc, hyb_c2(P.nx, i, j), y + (size_t)f * 4);
+}
+
+__device__ __forceinline__ Prims ns_prims_of(const NsDev &D) {
+    Prims P;
+    P.d = D.d; P.uu = D.uu; P.vv = D.vv; P.T = D.T; P.amu = D.amu; P.x1 = D.x1; P.y1 = D.y1;
+    P.nx = D.nx; P.ny = D.ny; P.pery = D.pery; P.cp = D.cp; P.pr = D.pr; P.kn = D.kn;
+    return P;
+}
+
+// features of the current NS state for the network (every j-face)
+__global__ void k_ns_features(NsDev D) {
+    if (D.ctrl->done) return;
+    const int nf = (D.nx - 1) * D.ny;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    jface_features(ns_prims_of(D), f % (D.nx - 1) + 1, f / (D.nx - 1) + 1, D.mlp_x + (size_t)f * 8);
+}
 
 // ---- kernels of one inner iteration -----------------------------------------
 // comput_duvtpckw + get_viscous (sub_NS_singlegrid.f90:121-157, sub_Residual.f90:553-576)
@@ -247,12 +337,20 @@ __global__ void k_ns_faces(NsDev D, int dir) {
     to[3 * D.nc + cf] = t33;
     qo[cf] = qx;
     qo[D.nc + cf] = qy;
-    const double *tg = dir == 0 ? D.tg_i : D.tg_j, *qg = dir == 0 ? D.qg_i : D.qg_j;
-    t11 = t11 + tg[cf];
-    t22 = t22 + tg[D.nc + cf];
-    t12 = t12 + tg[2 * D.nc + cf];
-    qx = qx + qg[cf];
-    qy = qy + qg[D.nc + cf];
+    if (D.mlp_on && dir == 1) {   // warm start: the network's HoT of the current state
+        const float *y = D.mlp_y + 4 * ((size_t)(j - 1) * (nx - 1) + (i - 1));
+        t12 += (double)y[0];
+        t22 += (double)y[1];
+        qx += (double)y[2];
+        qy += (double)y[3];
+    } else {                      // the kinetic HoT of Convert_NS
+        const double *tg = dir == 0 ? D.tg_i : D.tg_j, *qg = dir == 0 ? D.qg_i : D.qg_j;
+        t11 = t11 + tg[cf];
+        t22 = t22 + tg[D.nc + cf];
+        t12 = t12 + tg[2 * D.nc + cf];
+        qx = qx + qg[cf];
+        qy = qy + qg[D.nc + cf];
+    }
     double E1 = u1 * t11 + v1 * t12 + qx, E2 = u1 * t12 + v1 * t22 + qy;
     Fx[cf] = f0;
     Fx[D.nc + cf] = f1 + (t11 * n1 + t12 * n2) * s;
@@ -771,6 +869,7 @@ void ns_destroy(hyb_ctx *ctx) {
     if (st->ctrl) cudaFree(st->ctrl);
     if (st->h_ctrl) cudaFreeHost(st->h_ctrl);
     if (st->rk) cudaFree(st->rk);
+    if (st->mlp_buf) cudaFree(st->mlp_buf);
     if (ctx->d_rhs_gsis) cudaFree(ctx->d_rhs_gsis);
     ctx->d_rhs_gsis = nullptr;
     delete st;
@@ -867,6 +966,19 @@ int ns_create(hyb_ctx *ctx) {
     D.ns_scheme = ctx->gsis.ns_scheme;
     D.correct_f = ctx->gsis.correct_f != 0;
     D.src_on = 1;
+    D.mlp_on = 0;
+    D.kn = sqrt(HYB_PI) / (2.0 * ctx->prm.cfc);
+    {
+        const size_t nf = (size_t)(ctx->nx - 1) * ctx->ny;
+        if (cudaMalloc((void **)&st->mlp_buf, nf * 12 * sizeof(float)) != cudaSuccess) {
+            cudaFree(st->buf); cudaFree(st->geo); cudaFree(st->rk); cudaFree(ctx->d_rhs_gsis);
+            ctx->d_rhs_gsis = nullptr;
+            delete st;
+            return HYB_ERR_NOMEM;
+        }
+        D.mlp_x = st->mlp_buf;
+        D.mlp_y = st->mlp_buf + 8 * nf;
+    }
     D.gamma = ctx->prm.gamma;
     D.ma = ctx->prm.ma;
     D.pr = ctx->prm.pr;
@@ -897,6 +1009,10 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
     cudaStream_t s = ctx->stream;
     k_ns_prims<<<gc, bs, 0, s>>>(D);
+    if (D.mlp_on) {
+        k_ns_features<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D);
+        hyb_mlp_forward_dev(ctx->mlp, D.mlp_x, nfj, D.mlp_y, (void *)s);
+    }
     k_ns_faces<<<(nfi + bs - 1) / bs, bs, 0, s>>>(D, 0);
     k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D, 1);
     k_ns_res<<<(ncell + bs - 1) / bs, bs, 0, s>>>(D);
@@ -914,7 +1030,40 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     k_ns_close<<<1, 256, 0, s>>>(D);
 }
 
-static int inner_launches(const hyb_ctx *ctx) { return ctx->gsis.ns_solver == 1 ? 8 : 10; }
+static int inner_launches(const hyb_ctx *ctx, const NsDev &D) {
+    return (ctx->gsis.ns_solver == 1 ? 8 : 10) + (D.mlp_on ? 2 : 0);
+}
+
+// after the inner iterations: mass projection, moment correction with getNSF,
+// optional distribution correction, Shakhov parameters of the next step
+static int finish_correction(hyb_ctx *ctx, NsDev &D, bool correct_f) {
+    const int bs = 256;
+    const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
+    cudaStream_t s = ctx->stream;
+    k_gsis_mass<<<1, 256, 0, s>>>(D);
+    k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    if (correct_f) {
+        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)(ctx->nvj < 16 ? ctx->nvj : 16));
+        if (ctx->precision == HYB_PREC_FP64)
+            k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
+                                                     ctx->Na, ctx->Nb, ctx->prm.cpr);
+        else
+            k_gsis_fcorr<float><<<grd, 256, 0, s>>>(D, (float *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
+                                                    ctx->Na, ctx->Nb, ctx->prm.cpr);
+        ctx->launches++;
+    }
+    if (ctx->precision == HYB_PREC_FP64)
+        k_gsis_eqp<double><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (double *)ctx->d_eqp,
+                                                                          ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
+                                                                          ctx->prm.cpr);
+    else
+        k_gsis_eqp<float><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (float *)ctx->d_eqp,
+                                                                        ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
+                                                                        ctx->prm.cpr);
+    ctx->launches += 3;
+    return ck(ctx, "gsis_finish");
+}
 
 int gsis_solve(hyb_ctx *ctx) {
     NsState *st = (NsState *)ctx->ns;
@@ -970,7 +1119,7 @@ int gsis_solve(hyb_ctx *ctx) {
     int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
     for (int b = 0; b < nbatch; b++) {
         HYB_CK(cudaGraphLaunch(st->graph, s));
-        ctx->launches += NS_BATCH * inner_launches(ctx);
+        ctx->launches += NS_BATCH * inner_launches(ctx, D);
         HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
         HYB_CK(cudaStreamSynchronize(s));
         if (st->h_ctrl->done) break;
@@ -980,29 +1129,107 @@ int gsis_solve(hyb_ctx *ctx) {
         ctx->last_error = "synthetic solve: temperature below 0.1 or non-finite residual";
         return st->h_ctrl->err;
     }
-    k_gsis_mass<<<1, 256, 0, s>>>(D);
-    k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
-    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
-    if (D.correct_f) {
-        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)(ctx->nvj < 16 ? ctx->nvj : 16));
-        if (ctx->precision == HYB_PREC_FP64)
-            k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
-                                                     ctx->Na, ctx->Nb, ctx->prm.cpr);
-        else
-            k_gsis_fcorr<float><<<grd, 256, 0, s>>>(D, (float *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
-                                                    ctx->Na, ctx->Nb, ctx->prm.cpr);
-        ctx->launches++;
+    return finish_correction(ctx, D, D.correct_f != 0);
+}
+
+// learned warm start: NS closed with the network's HoT, iterated from the
+// kinetic state (no kinetic source) towards a steady state on the band, then
+// the moments and f are corrected to it
+int gsis_warm_start(hyb_ctx *ctx) {
+    NsState *st = (NsState *)ctx->ns;
+    if (!st || !ctx->gsis.enable) {
+        ctx->last_error = "warm start: the synthetic solve is not configured";
+        return HYB_ERR_INVALID;
     }
-    if (ctx->precision == HYB_PREC_FP64)
-        k_gsis_eqp<double><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (double *)ctx->d_eqp,
-                                                                          ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
-                                                                          ctx->prm.cpr);
-    else
-        k_gsis_eqp<float><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (float *)ctx->d_eqp,
-                                                                        ctx->Na, ctx->Nb, ctx->PA, ctx->scan_is_j,
-                                                                        ctx->prm.cpr);
+    if (!ctx->mlp) {
+        ctx->last_error = "warm start: no network attached (hyb_gsis_attach_mlp)";
+        return HYB_ERR_INVALID;
+    }
+    NsDev W = st->D;
+    W.cfl = ctx->gsis.cfl > 0 ? ctx->gsis.cfl : 20.0;
+    W.dtmax = ctx->gsis.dtmax > 0 ? ctx->gsis.dtmax : 10.0;
+    W.dtmin = ctx->gsis.dtmin > 0 ? ctx->gsis.dtmin : 1e-7;
+    W.src_on = 0;
+    W.mlp_on = 1;
+    const int bs = 256;
+    cudaStream_t s = ctx->stream;
+    k_gsis_start<<<(unsigned)((4 * W.nc + bs - 1) / bs), bs, 0, s>>>(W, ctx->d_hot);
+    k_ns_ghosts<<<1, 256, 0, s>>>(W);
+    k_gsis_copy<<<(unsigned)((4 * W.nc + bs - 1) / bs), bs, 0, s>>>(W.U2, W.U, 4 * W.nc);
     ctx->launches += 3;
-    return ck(ctx, "gsis_finish");
+    NsCtrl c0;
+    memset(&c0, 0, sizeof(c0));
+    c0.max_it = ctx->gsis.mlp_warm_inner > 0 ? ctx->gsis.mlp_warm_inner : 2000;
+    c0.tol = 0.0;
+    c0.rtol = ctx->gsis.mlp_warm_rtol > 0 ? ctx->gsis.mlp_warm_rtol : 1e-3;
+    *st->h_ctrl = c0;
+    HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
+    const int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
+    for (int b = 0; b < nbatch; b++) {
+        for (int k = 0; k < NS_BATCH; k++) inner_iteration(ctx, W);
+        ctx->launches += NS_BATCH * inner_launches(ctx, W);
+        HYB_CK(cudaGetLastError());
+        HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
+        HYB_CK(cudaStreamSynchronize(s));
+        if (st->h_ctrl->done) break;
+    }
+    ctx->gsis_last_inner = st->h_ctrl->it;
+    if (st->h_ctrl->err) {
+        ctx->last_error = "warm start: temperature below 0.1 or non-finite residual";
+        return st->h_ctrl->err;
+    }
+    return finish_correction(ctx, W, true);
 }
 
 }  // namespace hyb
+
+extern "C" {
+
+int hyb_gsis_attach_mlp(hyb_ctx *ctx, hyb_mlp *net) {
+    if (!ctx) return HYB_ERR_INVALID;
+    ctx->mlp = net;
+    return HYB_OK;
+}
+
+int hyb_gsis_warm_start(hyb_ctx *ctx) {
+    if (!ctx) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    return hyb::gsis_warm_start(ctx);
+}
+
+int hyb_closure_samples(hyb_ctx *ctx, float *x, float *y, int cap, int *n) {
+    if (!ctx || !n) return HYB_ERR_INVALID;
+    const int nf = (ctx->nx - 1) * ctx->ny;
+    *n = nf;
+    if (!x || !y) return HYB_OK;   // size query
+    if (cap < nf) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const size_t nc = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
+    const double *hot = ctx->d_hot;
+    hyb::Prims P;
+    P.d = hot + 4 * nc; P.uu = hot + 5 * nc; P.vv = hot + 6 * nc; P.T = hot + 7 * nc; P.amu = hot + 8 * nc;
+    P.x1 = ctx->d_x1; P.y1 = ctx->d_y1;
+    P.nx = ctx->nx; P.ny = ctx->ny; P.pery = ctx->bc[1] == HYB_BC_PERIODIC;
+    const double g = ctx->prm.gamma, ma = ctx->prm.ma;
+    P.cp = g / (g * (g - 1.0) * ma * ma);
+    P.pr = ctx->prm.pr;
+    P.kn = sqrt(HYB_PI) / (2.0 * ctx->prm.cfc);
+    float *dx = nullptr;
+    HYB_CK(cudaMalloc((void **)&dx, (size_t)nf * 12 * sizeof(float)));
+    float *dy = dx + (size_t)nf * 8;
+    hyb::k_closure_samples<<<(nf + 255) / 256, 256, 0, ctx->stream>>>(P, hot + 27 * nc, hot + 31 * nc, nc, dx, dy);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(x, dx, (size_t)nf * 8 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)nf * 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dx);
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("closure samples: ") + cudaGetErrorString(e);
+        return HYB_ERR_CUDA;
+    }
+    return HYB_OK;
+}
+
+}  // extern "C"
+

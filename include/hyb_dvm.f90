@@ -304,5 +304,20 @@ module hyb_dvm
        type(c_ptr), value :: net
        integer(c_long_long), intent(out) :: count
      end function
+     integer(c_int) function hyb_gsis_attach_mlp(ctx, net) bind(c, name="hyb_gsis_attach_mlp")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, net
+     end function
+     integer(c_int) function hyb_gsis_warm_start(ctx) bind(c, name="hyb_gsis_warm_start")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function hyb_closure_samples(ctx, x, y, cap, n) bind(c, name="hyb_closure_samples")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: ctx
+       real(c_float), intent(out) :: x(*), y(*)
+       integer(c_int), value :: cap
+       integer(c_int), intent(out) :: n
+     end function
   end interface
 end module hyb_dvm

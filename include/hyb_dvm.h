@@ -131,7 +131,9 @@ typedef struct hyb_gsis_params {
                                order, 2 NND2 stencil without the limiter      */
     int    mlp_warm_after;  /* > 0: after this many outer iterations since
                                configuration, hyb_step runs the learned warm
-                               start once (hyb_gsis_warm_start)              */
+                               start once (hyb_gsis_warm_start); if its closure
+                               solve leaves the physical range the state is
+                               left as it was and the iteration goes on      */
     int    ns_solver;       /* inner solver: 0 LU-SGS (du_LU_SGS_2D,
                                sub_LU_SGS.f90), 1 line-implicit ADI with the
                                LU-SGS diagonal and scalar couplings, exact
@@ -284,8 +286,8 @@ int hyb_batch_launch_count(const hyb_batch *b, long long *count);
  * weights/activations on the tensor cores with FP32 accumulation, FP32 master
  * weights and Adam (beta 0.9 / 0.999, eps 1e-8).  Inputs (per face): log10
  * local Kn, rho, T, du/dn, dT/dn, NSF shear stress, NSF normal heat flux,
- * wall distance; outputs: the non-NSF shear stress, half normal-stress
- * difference and heat-flux components.  Parameter layout (FP32): W1[64][8]
+ * wall distance; outputs: the non-NSF shear stress t_xy, wall-normal
+ * normal stress t_yy and heat-flux components q_x, q_y.  Parameter layout (FP32): W1[64][8]
  * b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[4][64] b4[4].  Inputs are
  * normalised as (x - in_mean) / in_std and outputs returned as
  * y_norm * out_std + out_mean; the loss is the mean squared error of the
@@ -313,6 +315,23 @@ int hyb_mlp_predict(hyb_mlp *m, const float *x, int n, float *y);
 int hyb_mlp_forward_dev(hyb_mlp *m, const float *x_dev, int n, float *y_dev, void *stream);
 int hyb_mlp_last_ms(const hyb_mlp *m, double *ms);
 int hyb_mlp_launch_count(const hyb_mlp *m, long long *count);
+
+/* Use of the network by a context.  hyb_gsis_attach_mlp gives the synthetic
+ * solve a network (not owned; NULL detaches).  hyb_gsis_warm_start runs the
+ * learned warm start once: the NS equations closed with the network's HoT
+ * (its predicted non-NSF t_xy, t_yy, q_x, q_y on the j-faces, in place of
+ * the kinetic HoT) are iterated from the kinetic state towards a steady
+ * state on the band, then the moments and f are corrected to that state as
+ * in the synthetic solve.  The kinetic GSIS iteration that follows converges
+ * to the kinetic solution whatever the network's error, and its residual
+ * judges it.  hyb_closure_samples writes the network's inputs x[n][8] and
+ * targets y[n][4] (the Convert_NS HoT t_xy, t_yy, q_x, q_y) of every j-face,
+ * n = (nx-1)*ny, face (i, j) at (j-1)*(nx-1) + i-1, for the current kinetic
+ * state: training data from the solver's own runs.  With x or y NULL it
+ * only returns n. */
+int hyb_gsis_attach_mlp(hyb_ctx *ctx, hyb_mlp *net);
+int hyb_gsis_warm_start(hyb_ctx *ctx);
+int hyb_closure_samples(hyb_ctx *ctx, float *x, float *y, int cap, int *n);
 
 #ifdef __cplusplus
 }
