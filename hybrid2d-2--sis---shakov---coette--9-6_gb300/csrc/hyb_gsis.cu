@@ -40,6 +40,8 @@
 namespace hyb {
 
 constexpr int NS_BATCH = 8;
+// local-Kn gate of the learned HoT in the warm start: log10(0.02), log10(0.05)
+constexpr double MLP_GATE_LO = -1.6989700043360187, MLP_GATE_HI = -1.3010299956639813;
 
 struct NsCtrl {
     unsigned long long res_bits;   // max |Res(4)| of the current inner iteration (bit pattern)
@@ -338,11 +340,17 @@ __global__ void k_ns_faces(NsDev D, int dir) {
     qo[cf] = qx;
     qo[D.nc + cf] = qy;
     if (D.mlp_on && dir == 1) {   // warm start: the network's HoT of the current state
-        const float *y = D.mlp_y + 4 * ((size_t)(j - 1) * (nx - 1) + (i - 1));
-        t12 += (double)y[0];
-        t22 += (double)y[1];
-        qx += (double)y[2];
-        qy += (double)y[3];
+        const size_t f = (size_t)(j - 1) * (nx - 1) + (i - 1);
+        const float *y = D.mlp_y + 4 * f;
+        // Kn gate: the network's absolute error (about 5e-4 in these units)
+        // exceeds the HoT itself below a local Kn of a few 1e-2, where the
+        // NSF closure alone is the better model; ramp from 0.02 to 0.05
+        const double lk = (double)D.mlp_x[8 * f];   // log10(Kn / rho)
+        const double w = fmin(1.0, fmax(0.0, (lk - MLP_GATE_LO) / (MLP_GATE_HI - MLP_GATE_LO)));
+        t12 += w * (double)y[0];
+        t22 += w * (double)y[1];
+        qx += w * (double)y[2];
+        qy += w * (double)y[3];
     } else {                      // the kinetic HoT of Convert_NS
         const double *tg = dir == 0 ? D.tg_i : D.tg_j, *qg = dir == 0 ? D.qg_i : D.qg_j;
         t11 = t11 + tg[cf];

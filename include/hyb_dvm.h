@@ -320,7 +320,9 @@ int hyb_mlp_launch_count(const hyb_mlp *m, long long *count);
  * solve a network (not owned; NULL detaches).  hyb_gsis_warm_start runs the
  * learned warm start once: the NS equations closed with the network's HoT
  * (its predicted non-NSF t_xy, t_yy, q_x, q_y on the j-faces, in place of
- * the kinetic HoT) are iterated from the kinetic state towards a steady
+ * the kinetic HoT, weighted by a local-Kn gate that ramps from 0 at
+ * Kn/rho = 0.02 to 1 at 0.05: below that the NSF closure is the better
+ * model and the network's error exceeds the HoT) are iterated from the kinetic state towards a steady
  * state on the band, then the moments and f are corrected to that state as
  * in the synthetic solve.  The kinetic GSIS iteration that follows converges
  * to the kinetic solution whatever the network's error, and its residual
