@@ -194,6 +194,42 @@ def run_reference(args, world, rank):
     return 0
 
 
+def time_to_residual(tol=1e-8, max_iters=8000, chunk=50):
+    """Wall time and outer iterations to max RMS residual <= tol on the Kn 0.1
+    channel (4x64 cells, 32x32 NC, NND, dt 0.01), for the plain kinetic
+    iteration and the synthetic-solve variants; device-synchronised wall
+    clock around the hyb_step calls (residual read every `chunk` steps)."""
+    from hyb_gb300 import closure
+    gs = dict(max_inner=40, inner_tol=0.0, inner_rtol=1e-2, cfl=20.0, ns_solver=0, correct_f=1)
+    variants = [("plain_fp64", 0, None), ("gsis_fp64", 0, gs), ("gsis_mixed", 1, gs),
+                ("gsis_mixed_learned", 1, dict(gs, mlp_warm_after=20))]
+    net = closure.load()
+    out = {}
+    for name, prec, g in variants:
+        c = cases.couette_small(dt=0.01)
+        s = abi.Solver(c, precision=prec)
+        s.init_maxwellian()
+        if g is not None:
+            s.attach_mlp(net)
+            s.gsis(**g)
+        it, r = 0, None
+        t0 = time.perf_counter()
+        while it < max_iters:
+            r = s.step(chunk)
+            it += chunk
+            if r["max_rms"] <= tol:
+                break
+        el = time.perf_counter() - t0
+        u = s.moments()[0].reshape(c.ny + 7, c.nx + 7, 11)[4:4 + c.ny - 1, 4:4 + c.nx - 1, 1]
+        out[name] = {"seconds": round(el, 3), "iterations": it, "residual": r["max_rms"],
+                     "reached": bool(r["max_rms"] <= tol), "u_mid_wall": float(u[-1].mean())}
+        s.close()
+    ref = out["plain_fp64"]["u_mid_wall"]
+    for v in out.values():
+        v["u_wall_rel_diff_vs_plain"] = abs(v["u_mid_wall"] - ref) / abs(ref)
+    return {"workload": "couette-4x64-nv32-kn0.1, NND, dt 0.01", "tol": tol, "chunk": chunk, "runs": out}
+
+
 def run_gb300(args, world, rank, local):
     case = make_case(args.config)
     s = abi.Solver(case, device=local)
@@ -272,6 +308,8 @@ def run_gb300(args, world, rank, local):
         "clocks": clk,
         "last_residual": res["max_rms"],
     }
+    if not args.no_ttr and rank == 0:
+        line["time_to_residual"] = time_to_residual()
     if not args.no_cpu:
         cv, cores, sample = cpu_sample(case, seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
@@ -363,6 +401,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="large", choices=["large", "small", "sine", "prof", "batch"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ttr", action="store_true", help="skip the time-to-residual runs")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:
