@@ -70,6 +70,15 @@ template <typename real> __device__ __forceinline__ real dexp(real x);
 template <> __device__ __forceinline__ float dexp<float>(float x) { return expf(x); }
 template <> __device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
 
+// the sweep's FP32 path uses the hardware approximations of exp and 1/x
+// (a few ulp); the FP64 path keeps the correctly rounded forms
+template <typename real> __device__ __forceinline__ real sweep_exp(real x);
+template <> __device__ __forceinline__ float sweep_exp<float>(float x) { return __expf(x); }
+template <> __device__ __forceinline__ double sweep_exp<double>(double x) { return exp(x); }
+template <typename real> __device__ __forceinline__ real sweep_rcp(real x);
+template <> __device__ __forceinline__ float sweep_rcp<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double sweep_rcp<double>(double x) { return 1.0 / x; }
+
 template <typename real> struct Consts {
     static __device__ __forceinline__ real eps_weno() { return real(HYB_EPSWENO_D); }
     static __device__ __forceinline__ real c1() { return real(HYB_CWENO1_D); }

@@ -378,11 +378,11 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
                 const real viu = vx - e_u[k], vjv = vy - e_v[k];
                 const real vij2 = (viu * viu + vjv * vjv) * e_it[k];
                 const real fvx = e_qx[k] * viu + e_qy[k] * vjv;
-                const real gdv = e_crt[k] * dexp<real>(-vij2);
+                const real gdv = e_crt[k] * sweep_exp<real>(-vij2);
                 const real geq = gdv * (real(1) + fvx * (real(2) * vij2 - real(4)));
                 const real heq = (e_ht[k] * gdv) * (real(1) + fvx * (real(2) * vij2 - real(2)));
                 const real vol = UNI ? vol_u : vl[k];
-                const real ivol = UNI ? ivol_u : real(1) / vol;
+                const real ivol = UNI ? ivol_u : sweep_rcp<real>(vol);
                 rG[k] = -divG * ivol + e_cf[k] * (geq - f0[k]);
                 rH[k] = -divH * ivol + e_cf[k] * (heq - f1[k]);
                 // LU-SGS forward element (GKUA_Residual.f90:39-57)
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
                 else
                     alfa = vol / dt + (posp(sAf[k + 1]) - negp(sAf[k]) + posp(sBh[k]) - negp(sBl[k])) +
                            vol * e_cf[k];
-                ia[k] = real(1) / alfa;
+                ia[k] = sweep_rcp<real>(alfa);
                 pc[k] = posp(sAf[k]) * ia[k];
                 const real pb = posp(sBl[k]);
                 cG[k] = (vol * rG[k] + pb * dG[k]) * ia[k];
