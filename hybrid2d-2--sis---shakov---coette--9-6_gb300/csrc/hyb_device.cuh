@@ -60,10 +60,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 template <typename real> __device__ __forceinline__ real posp(real a) { return (a + fabs(a)) * real(0.5); }
 template <typename real> __device__ __forceinline__ real negp(real a) { return (a - fabs(a)) * real(0.5); }
 
-// FMINMD, Functions.f90:10-25
+// FMINMD, Functions.f90:10-25: the smaller-magnitude argument when both have
+// the same strict sign, else 0.  Branch-free form: t = sign(x) y is > 0
+// exactly when y has x's sign, and min(|x|, t) is then |x| or |y|; the
+// result can differ from the reference only in the sign of a zero
 template <typename real> __device__ __forceinline__ real fminmd(real x, real y) {
-    if ((x > real(0) && y > real(0)) || (x < real(0) && y < real(0))) return (fabs(x) <= fabs(y)) ? x : y;
-    return real(0);
+    const real t = copysign(real(1), x) * y;
+    return copysign(fmax(real(0), fmin(fabs(x), t)), x);
 }
 
 template <typename real> __device__ __forceinline__ real dexp(real x);
