@@ -99,8 +99,10 @@ __global__ void k_wall(const real *__restrict__ f, real *__restrict__ fw, const 
 // moments.  k_moments_part: one CTA per (march row b, velocity slice); the
 // slice's velocity rows stream through an NST-stage shared-memory ring filled
 // by cp.async.bulk (full/empty mbarrier pairs), each thread accumulates MC
-// cells.  Mixed mode sums each velocity row in FP32 with Kahan compensation
-// and folds it into FP64; FP64 mode accumulates in FP64.  k_moments_finish
+// cells.  Mixed mode sums blocks of 8 velocities in plain FP32, adds the block
+// sums with Kahan compensation and folds the result into FP64 (the block
+// rounding is of the order of the FP32 inputs' own); FP64 mode accumulates in
+// FP64.  k_moments_finish
 // adds the slices in fixed order and applies DETFP's primitive conversion.
 // ---------------------------------------------------------------------------
 struct MomArgs {
@@ -171,11 +173,16 @@ __global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
     };
     if (t == 0)
         for (int n = 0; n < MOM_NST - 1 && n < nloc; n++) issue(n);
+    // plain sums over blocks of 8 velocities, compensated sums of the blocks
     KahanAcc<real> ks[10][MC];
+    real blk[10][MC];
 #pragma unroll
     for (int q = 0; q < 10; q++)
 #pragma unroll
-        for (int c = 0; c < MC; c++) ks[q][c].zero();
+        for (int c = 0; c < MC; c++) {
+            ks[q][c].zero();
+            blk[q][c] = real(0);
+        }
     bool ok = true;
     int n = 0;
     for (int jv = jv0; jv < jv1 && ok; jv++) {
@@ -202,16 +209,25 @@ __global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
                 for (int c = 0; c < MC; c++) {
                     const real wg = wv * gg[c];
                     const real b4 = hh[c] + (vx * vx + vy * vy) * gg[c];
-                    ks[0][c].add(wg);
-                    ks[1][c].add(wx * gg[c]);
-                    ks[2][c].add(wy * gg[c]);
-                    ks[3][c].add(wv * b4);
-                    ks[4][c].add(wx * (vx * gg[c]));
-                    ks[5][c].add(wy * (vy * gg[c]));
-                    ks[6][c].add(wxy * gg[c]);
-                    ks[7][c].add(wx * b4);
-                    ks[8][c].add(wy * b4);
-                    ks[9][c].add(wv * hh[c]);
+                    blk[0][c] += wg;
+                    blk[1][c] += wx * gg[c];
+                    blk[2][c] += wy * gg[c];
+                    blk[3][c] += wv * b4;
+                    blk[4][c] += wx * (vx * gg[c]);
+                    blk[5][c] += wy * (vy * gg[c]);
+                    blk[6][c] += wxy * gg[c];
+                    blk[7][c] += wx * b4;
+                    blk[8][c] += wy * b4;
+                    blk[9][c] += wv * hh[c];
+                }
+                if ((iv & 7) == 7 || iv == nvi - 1) {
+#pragma unroll
+                    for (int q = 0; q < 10; q++)
+#pragma unroll
+                        for (int c = 0; c < MC; c++) {
+                            ks[q][c].add(blk[q][c]);
+                            blk[q][c] = real(0);
+                        }
                 }
             }
             __syncwarp();
