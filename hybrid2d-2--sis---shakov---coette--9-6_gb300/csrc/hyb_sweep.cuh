@@ -278,11 +278,10 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
     }
 
     for (int b = 1; b <= Nb; b++) {
+        // each thread waits on the row's mbarrier itself (that wait makes the
+        // bulk copy visible); a timed-out wait is acted on at the row's one
+        // block barrier below, before anything is written to f
         wait_row(b + 2);
-        if (__syncthreads_or(timeout)) {
-            if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
-            return;
-        }
         real pc[CPT], cG[CPT], cH[CPT], ia[CPT], sAh[CPT], sBh[CPT], FBh_G[CPT], FBh_H[CPT];
         real fo0[CPT], fo1[CPT];           // f of row b-1 (for the backward update)
         real P = real(1), CGt = real(0), CHt = real(0);
@@ -439,7 +438,11 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
                 aggb[warp * 3 + 2] = Hi;
             }
         }
-        __syncthreads();
+        if (__syncthreads_or(timeout)) {
+            if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
+            return;
+        }
+        // every thread is past this row's reads, so the slot of row b-3 is free
         if (producer) issue_row(b + RING - 3);
         real xG = Ge, xH = He;                              // dF just before cell a0
         if (need_scan && warp > 0) {
