@@ -201,28 +201,43 @@ def time_to_residual(tol=1e-8, max_iters=8000, chunk=50):
     clock around the hyb_step calls (residual read every `chunk` steps)."""
     from hyb_gb300 import closure
     gs = dict(max_inner=40, inner_tol=0.0, inner_rtol=1e-2, cfl=20.0, ns_solver=0, correct_f=1)
-    variants = [("plain_fp64", 0, None), ("gsis_fp64", 0, gs), ("gsis_mixed", 1, gs),
-                ("gsis_mixed_learned", 1, dict(gs, mlp_warm_after=20))]
+    # "switch" variants run FP32 f until the residual reaches `switch_at`
+    # (or stops falling) and continue the same state in an FP64 context
+    variants = [("plain_fp64", 0, None, False), ("gsis_fp64", 0, gs, False), ("gsis_mixed", 1, gs, False),
+                ("gsis_mixed_learned", 1, dict(gs, mlp_warm_after=20), False),
+                ("gsis_mixed_then_fp64", 1, gs, True), ("gsis_mixed_learned_then_fp64", 1, dict(gs, mlp_warm_after=20), True)]
     net = closure.load()
     out = {}
-    for name, prec, g in variants:
+    switch_at = 3e-6
+    for name, prec, g, switch in variants:
         c = cases.couette_small(dt=0.01)
         s = abi.Solver(c, precision=prec)
         s.init_maxwellian()
         if g is not None:
             s.attach_mlp(net)
             s.gsis(**g)
-        it, r = 0, None
+        it, r, prev, switched_at = 0, None, None, None
         t0 = time.perf_counter()
         while it < max_iters:
             r = s.step(chunk)
             it += chunk
             if r["max_rms"] <= tol:
                 break
+            if switch and switched_at is None and (r["max_rms"] <= switch_at or (
+                    r["max_rms"] < 1e-4 and prev is not None and r["max_rms"] > 0.9 * prev)):
+                f = s.download_f()
+                s.close()
+                s = abi.Solver(c, precision=0)
+                s.upload_f(f)
+                s.gsis(**{k: v for k, v in g.items() if k != "mlp_warm_after"})
+                switched_at = it
+            prev = r["max_rms"]
         el = time.perf_counter() - t0
         u = s.moments()[0].reshape(c.ny + 7, c.nx + 7, 11)[4:4 + c.ny - 1, 4:4 + c.nx - 1, 1]
         out[name] = {"seconds": round(el, 3), "iterations": it, "residual": r["max_rms"],
                      "reached": bool(r["max_rms"] <= tol), "u_mid_wall": float(u[-1].mean())}
+        if switch:
+            out[name]["fp64_from_iteration"] = switched_at
         s.close()
     ref = out["plain_fp64"]["u_mid_wall"]
     for v in out.values():
