@@ -180,9 +180,7 @@ __global__ void k_ns_features(NsDev D) {
 
 // ---- kernels of one inner iteration -----------------------------------------
 // comput_duvtpckw + get_viscous (sub_NS_singlegrid.f90:121-157, sub_Residual.f90:553-576)
-__global__ void k_ns_prims(NsDev D) {
-    if (D.ctrl->done) return;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void ns_prims_body(const NsDev &D, size_t idx) {
     if (idx == 0) D.ctrl->res_bits = 0ull;
     if (idx >= D.nc) return;
     int i = (int)(idx % (D.nx + 3)) - 1, j = (int)(idx / (D.nx + 3)) - 1;
@@ -199,6 +197,11 @@ __global__ void k_ns_prims(NsDev D) {
         D.cc[idx] = sqrt(t) / D.ma;
     }
     if (i >= 0 && i <= D.nx && j >= 0 && j <= D.ny) D.amu[idx] = 1.0 / D.re * pow(t, D.omega);
+}
+
+__global__ void k_ns_prims(NsDev D) {
+    if (D.ctrl->done) return;
+    ns_prims_body(D, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 __device__ __forceinline__ double minmod_ns(double a, double b) {
@@ -241,11 +244,9 @@ __device__ void van_leer(const double *QL, const double *QR, double *F, double g
 }
 
 // Residual_FVM face fluxes (sub_Residual.f90:66-342), dir 0: i-faces, 1: j-faces
-__global__ void k_ns_faces(NsDev D, int dir) {
-    if (D.ctrl->done) return;
+__device__ __forceinline__ void ns_faces_body(const NsDev &D, int dir, int idx) {
     const int nx = D.nx, ny = D.ny;
     int ni = dir == 0 ? nx : nx - 1, nj = dir == 0 ? ny - 1 : ny;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ni * nj) return;
     int i = idx % ni + 1, j = idx / ni + 1;
     double s, n1, n2;
@@ -366,11 +367,15 @@ __global__ void k_ns_faces(NsDev D, int dir) {
     Fx[3 * D.nc + cf] = f3 + (E1 * n1 + E2 * n2) * s;
 }
 
-// residual, spectral radii, local dt, band max of |Res(4)|; dU reset
-__global__ void k_ns_res(NsDev D) {
+__global__ void k_ns_faces(NsDev D, int dir) {
     if (D.ctrl->done) return;
+    ns_faces_body(D, dir, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// residual, spectral radii, local dt, band max of |Res(4)|; dU reset
+// returns |Res(4)| of a band cell (0 elsewhere)
+__device__ __forceinline__ double ns_res_body(const NsDev &D, int idx) {
     const int nx = D.nx, ny = D.ny;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     double r4 = 0.0;
     if (idx < (nx - 1) * (ny - 1)) {
         int i = idx % (nx - 1) + 1, j = idx / (nx - 1) + 1;
@@ -408,6 +413,12 @@ __global__ void k_ns_res(NsDev D) {
             if (r4 != r4) atomicExch(&D.ctrl->err, HYB_ERR_NONFINITE);
         }
     }
+    return r4;
+}
+
+__global__ void k_ns_res(NsDev D) {
+    if (D.ctrl->done) return;
+    const double r4 = ns_res_body(D, blockIdx.x * blockDim.x + threadIdx.x);
     // block max, then one atomic per block (max is order independent)
     __shared__ double sm[256];
     sm[threadIdx.x] = r4;
@@ -435,10 +446,8 @@ __device__ __forceinline__ void dfn(const double *U, const double *dU, double n1
 
 // one colour of the forward (bwd = 0) or backward (bwd = 1) LU-SGS sweep
 // (du_LU_SGS_2D, sub_LU_SGS.f90:26-111)
-__global__ void k_ns_lusgs(NsDev D, int color, int bwd) {
-    if (D.ctrl->done) return;
+__device__ __forceinline__ void ns_lusgs_body(const NsDev &D, int color, int bwd, int idx) {
     const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= bw * bh) return;
     int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
     if (((i + j) & 1) != color) return;
@@ -480,6 +489,11 @@ __global__ void k_ns_lusgs(NsDev D, int color, int bwd) {
         }
         for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = D.dU[m * D.nc + c] + (dui[m] + duj[m]) / alfa;
     }
+}
+
+__global__ void k_ns_lusgs(NsDev D, int color, int bwd) {
+    if (D.ctrl->done) return;
+    ns_lusgs_body(D, color, bwd, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---- line-implicit ADI inner solve (no counterpart in the reference) -----
@@ -625,14 +639,17 @@ __global__ void k_ns_ilines(NsDev D) {
 }
 
 // U += dU on the band
-__global__ void k_ns_update(NsDev D) {
-    if (D.ctrl->done) return;
+__device__ __forceinline__ void ns_update_body(const NsDev &D, int idx) {
     const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= bw * bh) return;
     int i = idx % bw + D.ilo, j = idx / bw + D.jlo;
     size_t c = c2(D, i, j);
     for (int m = 0; m < 4; m++) D.U[m * D.nc + c] += D.dU[m * D.nc + c];
+}
+
+__global__ void k_ns_update(NsDev D) {
+    if (D.ctrl->done) return;
+    ns_update_body(D, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // periodic ghost U from the band (the NS solver's inner-boundary exchange)
@@ -671,6 +688,66 @@ __global__ void k_ns_close(NsDev D) {
         double res = __longlong_as_double((long long)C->res_bits);
         if (C->it == 1 && C->rtol * res > C->tol) C->tol = C->rtol * res;
         if (!(res > C->tol) || C->it >= C->max_it || C->err) C->done = 1;
+    }
+}
+
+// The whole LU-SGS inner loop of a small mesh in one CTA: the phases of an
+// iteration (primitives, face fluxes, residual, the four colour passes,
+// update, periodic ghosts, stop test) are separated by block barriers and the
+// loop runs at most max_it times, so one launch replaces the graph batches.
+// Same arithmetic per cell as the multi-kernel path.
+constexpr int NS_FUSED_THREADS = 512;
+constexpr size_t NS_FUSED_MAX_CELLS = 16384;
+
+__global__ void __launch_bounds__(NS_FUSED_THREADS) k_ns_fused(NsDev D) {
+    __shared__ double red[NS_FUSED_THREADS / 32];
+    __shared__ int stop;
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    NsCtrl *C = D.ctrl;
+    const int nfi = D.nx * (D.ny - 1), nfj = (D.nx - 1) * D.ny, ncl = (D.nx - 1) * (D.ny - 1);
+    const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
+    const int max_it = C->max_it;
+    for (int it = 0; it < max_it; it++) {
+        for (size_t idx = tid; idx < D.nc; idx += T) ns_prims_body(D, idx);
+        __syncthreads();
+        for (int idx = tid; idx < nfi; idx += T) ns_faces_body(D, 0, idx);
+        for (int idx = tid; idx < nfj; idx += T) ns_faces_body(D, 1, idx);
+        __syncthreads();
+        double r4 = 0.0;
+        for (int idx = tid; idx < ncl; idx += T) {
+            const double r = ns_res_body(D, idx);
+            if (r > r4) r4 = r;
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const double o = __shfl_xor_sync(0xffffffffu, r4, off);
+            if (o > r4) r4 = o;
+        }
+        if (lane == 0) red[warp] = r4;
+        __syncthreads();
+        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 0, 0, idx);
+        __syncthreads();
+        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 1, 0, idx);
+        __syncthreads();
+        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 1, 1, idx);
+        __syncthreads();
+        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 0, 1, idx);
+        __syncthreads();
+        for (int idx = tid; idx < nband; idx += T) ns_update_body(D, idx);
+        __syncthreads();
+        ns_ghosts(D);
+        __syncthreads();
+        if (tid == 0) {
+            double res = 0.0;
+            for (int w = 0; w < T / 32; w++)
+                if (red[w] > res) res = red[w];
+            C->res_bits = (unsigned long long)__double_as_longlong(res);
+            C->it += 1;
+            if (C->it == 1 && C->rtol * res > C->tol) C->tol = C->rtol * res;
+            stop = (!(res > C->tol) || C->it >= C->max_it || C->err) ? 1 : 0;
+            if (stop) C->done = 1;
+        }
+        __syncthreads();
+        if (stop) break;
     }
 }
 
@@ -1115,22 +1192,31 @@ int gsis_solve(hyb_ctx *ctx) {
     }
     ctx->launches += 8;
     HYB_CK(cudaGetLastError());
-    if (!st->have_graph) {
-        cudaGraph_t g;
-        HYB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < NS_BATCH; k++) inner_iteration(ctx, D);
-        HYB_CK(cudaStreamEndCapture(s, &g));
-        HYB_CK(cudaGraphInstantiate(&st->graph, g, 0));
-        cudaGraphDestroy(g);
-        st->have_graph = true;
-    }
-    int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
-    for (int b = 0; b < nbatch; b++) {
-        HYB_CK(cudaGraphLaunch(st->graph, s));
-        ctx->launches += NS_BATCH * inner_launches(ctx, D);
+    if (ctx->gsis.ns_solver == 0 && D.nc <= NS_FUSED_MAX_CELLS) {
+        // small mesh: the whole inner loop in one CTA
+        k_ns_fused<<<1, NS_FUSED_THREADS, 0, s>>>(D);
+        ctx->launches++;
+        HYB_CK(cudaGetLastError());
         HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
         HYB_CK(cudaStreamSynchronize(s));
-        if (st->h_ctrl->done) break;
+    } else {
+        if (!st->have_graph) {
+            cudaGraph_t g;
+            HYB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < NS_BATCH; k++) inner_iteration(ctx, D);
+            HYB_CK(cudaStreamEndCapture(s, &g));
+            HYB_CK(cudaGraphInstantiate(&st->graph, g, 0));
+            cudaGraphDestroy(g);
+            st->have_graph = true;
+        }
+        int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
+        for (int b = 0; b < nbatch; b++) {
+            HYB_CK(cudaGraphLaunch(st->graph, s));
+            ctx->launches += NS_BATCH * inner_launches(ctx, D);
+            HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
+            HYB_CK(cudaStreamSynchronize(s));
+            if (st->h_ctrl->done) break;
+        }
     }
     ctx->gsis_last_inner = st->h_ctrl->it;
     if (st->h_ctrl->err) {

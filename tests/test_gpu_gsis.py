@@ -37,9 +37,13 @@ def _pair(case, precision, **gk):
 
 
 @pytest.mark.parametrize("solver", [0, 1])
-@pytest.mark.parametrize("shape", ["small", "transposed", "stretched"])
+@pytest.mark.parametrize("shape", ["small", "transposed", "stretched", "wide"])
 def test_gsis_fixed_inner_matches_oracle(cases_mod, shape, solver):
-    if shape == "small":
+    """Meshes up to 16384 cells (with ghosts) run the LU-SGS inner loop in
+    one fused CTA; the "wide" mesh (44 x 404) runs the graph-batched kernels."""
+    if shape == "wide":
+        c = cases_mod.couette_small(ncx=40, ncy=400, nvx=8, nvy=8, dt=0.005)
+    elif shape == "small":
         c = cases_mod.couette_small(ncy=32, nvx=16, nvy=16, dt=0.02)
     elif shape == "transposed":
         c = cases_mod.couette_small(ncx=40, ncy=8, nvx=12, nvy=12, dt=0.02)
