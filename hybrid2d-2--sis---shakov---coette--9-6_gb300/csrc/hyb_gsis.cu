@@ -52,6 +52,8 @@ struct NsCtrl {
     double tol;                    // absolute stop; raised to rtol * first residual
     double rtol;
     double lam;                    // volume mean of the band's density change
+    unsigned bar_count;            // grid barrier of the cooperative inner loop: arrivals
+    unsigned bar_gen;              // and completed barriers
 };
 
 struct NsDev {
@@ -88,6 +90,7 @@ struct NsState {
     cudaGraphExec_t graph;
     bool have_graph;
     float *mlp_buf;         // closure features and outputs
+    int coop_blocks;        // blocks of the cooperative inner loop (0: not available)
 };
 
 __device__ __forceinline__ size_t c2(const NsDev &D, int i, int j) { return hyb_c2(D.nx, i, j); }
@@ -691,30 +694,70 @@ __global__ void k_ns_close(NsDev D) {
     }
 }
 
-// The whole LU-SGS inner loop of a small mesh in one CTA: the phases of an
-// iteration (primitives, face fluxes, residual, the four colour passes,
-// update, periodic ghosts, stop test) are separated by block barriers and the
-// loop runs at most max_it times, so one launch replaces the graph batches.
-// Same arithmetic per cell as the multi-kernel path.
-constexpr int NS_FUSED_THREADS = 512;
-constexpr size_t NS_FUSED_MAX_CELLS = 16384;
+// The LU-SGS inner loop of a small mesh in one cooperative launch.  The
+// phases of an iteration (primitives, face fluxes, residual, the four colour
+// passes, update, periodic ghosts, stop test) are separated by grid-wide
+// barriers (the launch guarantees that all blocks are resident) and the loop
+// runs at most max_it times, so one launch replaces the graph batches.  The
+// arithmetic per cell is that of the multi-kernel path.  GB300's FP64 rate
+// per SM is small, so the mesh is spread one warp per SM over as many SMs as
+// it has warps of cells.
+constexpr int NS_COOP_THREADS = 32;
+constexpr size_t NS_COOP_MAX_CELLS = 65536;
 
-__global__ void __launch_bounds__(NS_FUSED_THREADS) k_ns_fused(NsDev D) {
-    __shared__ double red[NS_FUSED_THREADS / 32];
-    __shared__ int stop;
-    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// grid barrier: counter + generation in the control block; the wait is
+// bounded and a block that gives up sets HYB_ERR_TIMEOUT, which ends the
+// waits of the others
+__device__ bool ns_grid_sync(NsCtrl *C) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &C->bar_gen;
+        volatile int *err = &C->err;
+        const unsigned g = *gen;
+        __threadfence();
+        int good = 1;
+        if (atomicAdd(&C->bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(&C->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&C->bar_gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                if (*err == HYB_ERR_TIMEOUT || clock64() - t0 > HYB_SPIN_CYCLES) {
+                    atomicExch(&C->err, HYB_ERR_TIMEOUT);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__global__ void __launch_bounds__(NS_COOP_THREADS) k_ns_coop(NsDev D) {
+    __shared__ double red[NS_COOP_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g0 = blockIdx.x * blockDim.x + tid, G = gridDim.x * blockDim.x;
     NsCtrl *C = D.ctrl;
+    volatile NsCtrl *V = D.ctrl;
     const int nfi = D.nx * (D.ny - 1), nfj = (D.nx - 1) * D.ny, ncl = (D.nx - 1) * (D.ny - 1);
     const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
-    const int max_it = C->max_it;
+    const int max_it = V->max_it;
     for (int it = 0; it < max_it; it++) {
-        for (size_t idx = tid; idx < D.nc; idx += T) ns_prims_body(D, idx);
-        __syncthreads();
-        for (int idx = tid; idx < nfi; idx += T) ns_faces_body(D, 0, idx);
-        for (int idx = tid; idx < nfj; idx += T) ns_faces_body(D, 1, idx);
-        __syncthreads();
+        for (size_t idx = g0; idx < D.nc; idx += G) ns_prims_body(D, idx);   // idx 0 clears res_bits
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nfi + nfj; idx += G) {
+            if (idx < nfi) ns_faces_body(D, 0, idx);
+            else ns_faces_body(D, 1, idx - nfi);
+        }
+        if (!ns_grid_sync(C)) return;
         double r4 = 0.0;
-        for (int idx = tid; idx < ncl; idx += T) {
+        for (int idx = g0; idx < ncl; idx += G) {
             const double r = ns_res_body(D, idx);
             if (r > r4) r4 = r;
         }
@@ -724,30 +767,38 @@ __global__ void __launch_bounds__(NS_FUSED_THREADS) k_ns_fused(NsDev D) {
         }
         if (lane == 0) red[warp] = r4;
         __syncthreads();
-        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 0, 0, idx);
-        __syncthreads();
-        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 1, 0, idx);
-        __syncthreads();
-        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 1, 1, idx);
-        __syncthreads();
-        for (int idx = tid; idx < nband; idx += T) ns_lusgs_body(D, 0, 1, idx);
-        __syncthreads();
-        for (int idx = tid; idx < nband; idx += T) ns_update_body(D, idx);
-        __syncthreads();
-        ns_ghosts(D);
-        __syncthreads();
         if (tid == 0) {
-            double res = 0.0;
-            for (int w = 0; w < T / 32; w++)
-                if (red[w] > res) res = red[w];
-            C->res_bits = (unsigned long long)__double_as_longlong(res);
-            C->it += 1;
-            if (C->it == 1 && C->rtol * res > C->tol) C->tol = C->rtol * res;
-            stop = (!(res > C->tol) || C->it >= C->max_it || C->err) ? 1 : 0;
-            if (stop) C->done = 1;
+            double m = 0.0;
+            for (int w = 0; w < NS_COOP_THREADS / 32; w++)
+                if (red[w] > m) m = red[w];
+            atomicMax(&C->res_bits, (unsigned long long)__double_as_longlong(m));
         }
-        __syncthreads();
-        if (stop) break;
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 0, 0, idx);
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 1, 0, idx);
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 1, 1, idx);
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 0, 1, idx);
+        if (!ns_grid_sync(C)) return;
+        for (int idx = g0; idx < nband; idx += G) ns_update_body(D, idx);
+        if (!ns_grid_sync(C)) return;
+        if (blockIdx.x == 0) {
+            ns_ghosts(D);
+            __syncthreads();
+            if (tid == 0) {
+                const double res = __longlong_as_double((long long)V->res_bits);
+                const int itn = V->it + 1;
+                V->it = itn;
+                double tol = V->tol;
+                if (itn == 1 && V->rtol * res > tol) tol = V->rtol * res;
+                V->tol = tol;
+                if (!(res > tol) || itn >= V->max_it || V->err) V->done = 1;
+            }
+        }
+        if (!ns_grid_sync(C)) return;
+        if (V->done) break;
     }
 }
 
@@ -1081,6 +1132,21 @@ int ns_create(hyb_ctx *ctx) {
     }
     D.ctrl = st->ctrl;
     st->have_graph = false;
+    {
+        // enough blocks for one cell per thread, within what is co-resident
+        int dev = 0, coop = 0, per_sm = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ns_coop, NS_COOP_THREADS, 0);
+        // one thread per item of the largest phase (cells or faces), at most
+        // four blocks per SM so that the barrier's arrivals stay few
+        const size_t nf = (size_t)D.nx * (D.ny - 1) + (size_t)(D.nx - 1) * D.ny;
+        const size_t items = nc > nf ? nc : nf;
+        const int want = (int)((items + NS_COOP_THREADS - 1) / NS_COOP_THREADS);
+        const int cap = per_sm < 4 ? per_sm * nsm : 4 * nsm;
+        st->coop_blocks = (coop && cap > 0) ? (want < cap ? want : cap) : 0;
+    }
     ctx->ns = st;
     return ck(ctx, "ns_create");
 }
@@ -1129,7 +1195,11 @@ static int finish_correction(hyb_ctx *ctx, NsDev &D, bool correct_f) {
     k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     if (correct_f) {
-        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)(ctx->nvj < 16 ? ctx->nvj : 16));
+        // about four velocities per thread: the two Shakhov evaluations per
+        // velocity are FP64 exponentials, and small meshes need the velocity
+        // axis for parallelism
+        const int nsl = ctx->nv / 4 < 1 ? 1 : (ctx->nv / 4 > 4096 ? 4096 : ctx->nv / 4);
+        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)nsl);
         if (ctx->precision == HYB_PREC_FP64)
             k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
                                                      ctx->Na, ctx->Nb, ctx->prm.cpr);
@@ -1192,11 +1262,12 @@ int gsis_solve(hyb_ctx *ctx) {
     }
     ctx->launches += 8;
     HYB_CK(cudaGetLastError());
-    if (ctx->gsis.ns_solver == 0 && D.nc <= NS_FUSED_MAX_CELLS) {
-        // small mesh: the whole inner loop in one CTA
-        k_ns_fused<<<1, NS_FUSED_THREADS, 0, s>>>(D);
+    if (ctx->gsis.ns_solver == 0 && D.nc <= NS_COOP_MAX_CELLS && st->coop_blocks > 0) {
+        // small mesh: the whole inner loop in one cooperative launch
+        void *kargs[] = {(void *)&D};
+        HYB_CK(cudaLaunchCooperativeKernel((const void *)k_ns_coop, dim3(st->coop_blocks), dim3(NS_COOP_THREADS),
+                                           kargs, 0, s));
         ctx->launches++;
-        HYB_CK(cudaGetLastError());
         HYB_CK(cudaMemcpyAsync(st->h_ctrl, st->ctrl, sizeof(NsCtrl), cudaMemcpyDeviceToHost, s));
         HYB_CK(cudaStreamSynchronize(s));
     } else {
