@@ -168,6 +168,25 @@ inline size_t dev_cell(const hyb_ctx *c, int i, int j) {
     return (size_t)(b - 1) * c->PA + (a - 1);
 }
 
+// Sweep layout of a mesh: the scan axis is the longer one that fits one CTA
+// row (<= 1024 cells); cells per sweep thread (cpt) tile the scan axis
+// exactly; the padded row PA holds 32 * cpt-cell chunks and a thread group
+// (PA / cpt threads) fits one 256-thread CTA, so scan axes above 256 cells
+// need an even count and above 512 a multiple of 4.
+struct SweepLayout {
+    int scan_is_j, Na, Nb, cpt, PA;
+};
+static bool sweep_layout(int ncx, int ncy, SweepLayout *L) {
+    if (ncy >= ncx && ncy <= 1024) L->scan_is_j = 1;
+    else if (ncx <= 1024) L->scan_is_j = 0;
+    else return false;
+    L->Na = L->scan_is_j ? ncy : ncx;
+    L->Nb = L->scan_is_j ? ncx : ncy;
+    L->cpt = (L->Na % 4 == 0 && L->Na >= 128) ? 4 : ((L->Na % 2 == 0 && L->Na >= 64) ? 2 : 1);
+    L->PA = (L->Na + 32 * L->cpt - 1) / (32 * L->cpt) * (32 * L->cpt);
+    return L->PA / L->cpt <= 256;
+}
+
 }  // namespace
 
 extern "C" {
@@ -194,6 +213,8 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     }
     if ((m->bc[0] == HYB_BC_PERIODIC) != (m->bc[2] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
     if ((m->bc[1] == HYB_BC_PERIODIC) != (m->bc[3] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
+    SweepLayout lay;
+    if (!sweep_layout(m->nx - 1, m->ny - 1, &lay)) return HYB_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYB_ERR_NODEVICE;
     if (p->device < 0 || p->device >= ndev) return HYB_ERR_INVALID;
@@ -207,16 +228,12 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     c->nx = m->nx; c->ny = m->ny; c->ncx = m->nx - 1; c->ncy = m->ny - 1;
     c->nvi = vg->nvi; c->nvj = vg->nvj; c->nv = vg->nvi * vg->nvj;
     for (int f = 0; f < 4; f++) c->bc[f] = m->bc[f];
-    // the scan axis is the longer one that fits one CTA row (<= 1024 cells)
     int ncx = c->ncx, ncy = c->ncy;
-    if (ncy >= ncx && ncy <= 1024) c->scan_is_j = 1;
-    else if (ncx <= 1024) c->scan_is_j = 0;
-    else { delete c; return HYB_ERR_UNSUPPORTED; }
-    c->Na = c->scan_is_j ? ncy : ncx;
-    c->Nb = c->scan_is_j ? ncx : ncy;
-    // cells per sweep thread: chunks must tile the scan axis exactly
-    c->cpt = (c->Na % 4 == 0 && c->Na >= 128) ? 4 : ((c->Na % 2 == 0 && c->Na >= 64) ? 2 : 1);
-    c->PA = (c->Na + 32 * c->cpt - 1) / (32 * c->cpt) * (32 * c->cpt);
+    c->scan_is_j = lay.scan_is_j;
+    c->Na = lay.Na;
+    c->Nb = lay.Nb;
+    c->cpt = lay.cpt;
+    c->PA = lay.PA;
     // wall stencils need at least three cells along the wall-normal axis,
     // a periodic march axis at least two
     for (int f = 0; f < 4; f++)

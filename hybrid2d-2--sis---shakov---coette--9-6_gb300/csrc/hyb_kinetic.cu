@@ -112,11 +112,11 @@ struct MomArgs {
     double *CF;         // [(nx+3)(ny+3)]
     void *eqp;          // [8][Nb*PA] real
     const double *vx, *vy, *w;
-    int nvi, nv, Na, Nb, PA, nx, ny, scan_is_j, vs, *err;
+    int nvi, nv, Na, Nb, PA, nx, ny, scan_is_j, vs, nloc_max, *err;
     double cfc, cpr, x1s, r00, t00;
 };
 
-constexpr int MOM_NST = 8;
+constexpr int MOM_NST = 4;
 
 template <typename real> struct KahanAcc;
 template <> struct KahanAcc<double> {
@@ -137,9 +137,24 @@ template <> struct KahanAcc<float> {
     __device__ double fold() { double r = (double)s - (double)c; s = 0.f; c = 0.f; return r; }
 };
 
+// velocities per stage slot: one mbarrier wait, one refill and one empty
+// arrival per slot; 16 KB slots at PA = 512 in both precisions
+template <typename real> struct MomVps { static constexpr int v = 4; };
+template <> struct MomVps<double> { static constexpr int v = 2; };
+
+template <typename real>
+__host__ __device__ inline size_t mom_smem_bytes(int PA, int nloc_max) {
+    size_t b = 256;                                                   // mbarriers
+    b += ((size_t)3 * nloc_max * sizeof(real) + 127) / 128 * 128;     // vx, vy, w per velocity
+    b += (size_t)MOM_NST * MomVps<real>::v * 2 * PA * sizeof(real);   // stage ring
+    return b;
+}
+
 template <typename real, int MC>
-__global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
+__global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int VPS = MomVps<real>::v;
+    constexpr int FLUSH = 8 / VPS;                  // slots per block of 8 velocities
     const int PA = M.PA, t = threadIdx.x, TPV = blockDim.x;
     const int b = blockIdx.x + 1, slice = blockIdx.y;
     const int a0 = t * MC + 1;
@@ -147,15 +162,20 @@ __global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
     const int nvi = M.nvi, nvj = M.nv / M.nvi;
     const int jv0 = (int)((long long)nvj * slice / M.vs), jv1 = (int)((long long)nvj * (slice + 1) / M.vs);
     const int v0 = jv0 * nvi, nloc = (jv1 - jv0) * nvi;
+    const int nslot = (nloc + VPS - 1) / VPS;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
     uint64_t *empty = full + MOM_NST;
-    real *svx = reinterpret_cast<real *>(smem_raw + 256);          // nvi nodes
-    real *stage = reinterpret_cast<real *>(smem_raw + 256 + ((nvi * sizeof(real) + 127) / 128) * 128);
+    real *sv = reinterpret_cast<real *>(smem_raw + 256);             // [3][nloc]
+    real *stage = reinterpret_cast<real *>(smem_raw + 256 + ((size_t)3 * M.nloc_max * sizeof(real) + 127) / 128 * 128);
     const size_t rs = (size_t)M.Nb * PA;
     const real *f = (const real *)M.f;
     const uint32_t row_bytes = (uint32_t)(PA * sizeof(real));
     const int nwarp = TPV >> 5, lane = t & 31;
-    for (int k = t; k < nvi; k += TPV) svx[k] = (real)M.vx[k];
+    for (int k = t; k < nloc; k += TPV) {
+        sv[k] = (real)M.vx[k % nvi];
+        sv[nloc + k] = (real)M.vy[jv0 + k / nvi];
+        sv[2 * nloc + k] = (real)M.w[(size_t)v0 + k];
+    }
     if (t == 0) {
         for (int k = 0; k < MOM_NST; k++) {
             mbar_init(&full[k], 1);
@@ -166,13 +186,17 @@ __global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
     __syncthreads();
     auto issue = [&](int n) {
         const int k = n % MOM_NST;
-        const real *src = f + (size_t)(v0 + n) * 2 * rs + (size_t)(b - 1) * PA;
-        mbar_arrive_expect_tx(&full[k], 2 * row_bytes);
-        bulk_g2s(stage + (size_t)k * 2 * PA, src, row_bytes, &full[k]);
-        bulk_g2s(stage + (size_t)k * 2 * PA + PA, src + rs, row_bytes, &full[k]);
+        const int cnt = min(VPS, nloc - n * VPS);
+        mbar_arrive_expect_tx(&full[k], 2 * row_bytes * cnt);
+        for (int u = 0; u < cnt; u++) {
+            const real *src = f + (size_t)(v0 + n * VPS + u) * 2 * rs + (size_t)(b - 1) * PA;
+            real *dst = stage + ((size_t)k * VPS + u) * 2 * PA;
+            bulk_g2s(dst, src, row_bytes, &full[k]);
+            bulk_g2s(dst + PA, src + rs, row_bytes, &full[k]);
+        }
     };
     if (t == 0)
-        for (int n = 0; n < MOM_NST - 1 && n < nloc; n++) issue(n);
+        for (int n = 0; n < MOM_NST - 1 && n < nslot; n++) issue(n);
     // plain sums over blocks of 8 velocities, compensated sums of the blocks
     KahanAcc<real> ks[10][MC];
     real blk[10][MC];
@@ -184,55 +208,58 @@ __global__ void __launch_bounds__(256, 2) k_moments_part(MomArgs M) {
             blk[q][c] = real(0);
         }
     bool ok = true;
-    int n = 0;
-    for (int jv = jv0; jv < jv1 && ok; jv++) {
-        const real vy = (real)M.vy[jv];
-        const double *wrow = M.w + (size_t)jv * nvi;
-        for (int iv = 0; iv < nvi && ok; iv++, n++) {
-            const int k = n % MOM_NST;
-            // refill the slot freed by velocity n-1 with velocity n+NST-1
-            if (t == 0 && n + MOM_NST - 1 < nloc) {
-                if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
-                    ok = false;
-                else
-                    issue(n + MOM_NST - 1);
-            }
-            if (!mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
-            if (act && ok) {
-                const real vx = svx[iv], wv = (real)__ldg(wrow + iv);
-                const real *g = stage + (size_t)k * 2 * PA + (a0 - 1);
-                real gg[MC], hh[MC];
-#pragma unroll
-                for (int c = 0; c < MC; c++) { gg[c] = g[c]; hh[c] = g[PA + c]; }
-                const real wx = wv * vx, wy = wv * vy, wxy = wx * vy;
-#pragma unroll
-                for (int c = 0; c < MC; c++) {
-                    const real wg = wv * gg[c];
-                    const real b4 = hh[c] + (vx * vx + vy * vy) * gg[c];
-                    blk[0][c] += wg;
-                    blk[1][c] += wx * gg[c];
-                    blk[2][c] += wy * gg[c];
-                    blk[3][c] += wv * b4;
-                    blk[4][c] += wx * (vx * gg[c]);
-                    blk[5][c] += wy * (vy * gg[c]);
-                    blk[6][c] += wxy * gg[c];
-                    blk[7][c] += wx * b4;
-                    blk[8][c] += wy * b4;
-                    blk[9][c] += wv * hh[c];
-                }
-                if ((iv & 7) == 7 || iv == nvi - 1) {
-#pragma unroll
-                    for (int q = 0; q < 10; q++)
-#pragma unroll
-                        for (int c = 0; c < MC; c++) {
-                            ks[q][c].add(blk[q][c]);
-                            blk[q][c] = real(0);
-                        }
-                }
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[k]);
+    for (int n = 0; n < nslot && ok; n++) {
+        const int k = n % MOM_NST;
+        // refill the slot freed by slot n-1 with slot n+NST-1
+        if (t == 0 && n + MOM_NST - 1 < nslot) {
+            if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
+                ok = false;
+            else
+                issue(n + MOM_NST - 1);
         }
+        if (!mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
+        if (act && ok) {
+            const int cnt = min(VPS, nloc - n * VPS);
+            const real *gs = stage + (size_t)k * VPS * 2 * PA + (a0 - 1);
+#pragma unroll
+            for (int u = 0; u < VPS; u++) {
+                if (u < cnt) {
+                    const int lv = n * VPS + u;
+                    const real vx = sv[lv], vy = sv[nloc + lv], wv = sv[2 * nloc + lv];
+                    const real *g = gs + (size_t)u * 2 * PA;
+                    real gg[MC], hh[MC];
+#pragma unroll
+                    for (int c = 0; c < MC; c++) { gg[c] = g[c]; hh[c] = g[PA + c]; }
+                    const real wx = wv * vx, wy = wv * vy, wxy = wx * vy, c2 = vx * vx + vy * vy;
+#pragma unroll
+                    for (int c = 0; c < MC; c++) {
+                        const real wg = wv * gg[c];
+                        const real b4 = hh[c] + c2 * gg[c];
+                        blk[0][c] += wg;
+                        blk[1][c] += wx * gg[c];
+                        blk[2][c] += wy * gg[c];
+                        blk[3][c] += wv * b4;
+                        blk[4][c] += wx * (vx * gg[c]);
+                        blk[5][c] += wy * (vy * gg[c]);
+                        blk[6][c] += wxy * gg[c];
+                        blk[7][c] += wx * b4;
+                        blk[8][c] += wy * b4;
+                        blk[9][c] += wv * hh[c];
+                    }
+                }
+            }
+            if ((n % FLUSH) == FLUSH - 1 || n == nslot - 1) {
+#pragma unroll
+                for (int q = 0; q < 10; q++)
+#pragma unroll
+                    for (int c = 0; c < MC; c++) {
+                        ks[q][c].add(blk[q][c]);
+                        blk[q][c] = real(0);
+                    }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[k]);
     }
     if (__syncthreads_or(!ok)) {
         if (t == 0) atomicExch(M.err, HYB_ERR_TIMEOUT);
@@ -505,26 +532,30 @@ int launch_moments(hyb_ctx *ctx) {
     M.ny = ctx->ny;
     M.scan_is_j = ctx->scan_is_j;
     M.vs = moments_slices(ctx);
+    M.nloc_max = (ctx->nvj + M.vs - 1) / M.vs * ctx->nvi;
     M.err = ctx->d_err;
     M.cfc = ctx->prm.cfc;
     M.cpr = ctx->prm.cpr;
     M.x1s = ctx->prm.x1s;
     M.r00 = ctx->prm.r00;
     M.t00 = ctx->prm.t00;
-    // cells per thread: FP64 sums need one register pair per moment, the
-    // compensated FP32 sums two floats; both stay below 128 registers
-    const int mc = (ctx->precision == HYB_PREC_FP64 && ctx->cpt >= 4) ? 4 : (ctx->cpt >= 2 ? 2 : 1);
+    // cells per thread: two where the chunk allows it (both precisions stay
+    // below 128 registers without spills), one on FP64 rows of <= 256 cells
+    // so that more threads share them; a CTA has at most 512 threads
+    const int mc = (ctx->cpt >= 2 && (ctx->precision != HYB_PREC_FP64 || ctx->PA > 256)) ? 2 : 1;
     const int tpv = ctx->PA / mc;
-    const size_t smem = 256 + ((ctx->nvi * ctx->real_size + 127) / 128) * 128 +
-                        (size_t)MOM_NST * 2 * ctx->PA * ctx->real_size;
+    const size_t smem = ctx->precision == HYB_PREC_FP64 ? mom_smem_bytes<double>(ctx->PA, M.nloc_max)
+                                                        : mom_smem_bytes<float>(ctx->PA, M.nloc_max);
+    if (smem > (size_t)227 * 1024) {
+        ctx->last_error = "moments: velocity slice too large for shared memory";
+        return HYB_ERR_UNSUPPORTED;
+    }
     dim3 grd(ctx->Nb, M.vs);
     if (ctx->precision == HYB_PREC_FP64) {
-        if (mc == 4) launch_mom<double, 4>(ctx, M, grd, tpv, smem);
-        else if (mc == 2) launch_mom<double, 2>(ctx, M, grd, tpv, smem);
+        if (mc == 2) launch_mom<double, 2>(ctx, M, grd, tpv, smem);
         else launch_mom<double, 1>(ctx, M, grd, tpv, smem);
     } else {
-        if (mc == 4) launch_mom<float, 4>(ctx, M, grd, tpv, smem);
-        else if (mc == 2) launch_mom<float, 2>(ctx, M, grd, tpv, smem);
+        if (mc == 2) launch_mom<float, 2>(ctx, M, grd, tpv, smem);
         else launch_mom<float, 1>(ctx, M, grd, tpv, smem);
     }
     ctx->launches++;

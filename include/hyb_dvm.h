@@ -154,7 +154,10 @@ typedef struct hyb_gsis_params {
 typedef struct hyb_ctx hyb_ctx;
 
 /* ---- lifecycle ---------------------------------------------------------- */
-/* Replaces init / Alloc_GKUA_FRD (sub_init.f90:6-79, 329-386). */
+/* Replaces init / Alloc_GKUA_FRD (sub_init.f90:6-79, 329-386).
+ * Size limits (HYB_ERR_UNSUPPORTED otherwise): the sweep's scan axis is the
+ * longer cell count that is <= 1024; above 256 cells it must be even and
+ * above 512 a multiple of 4; a wall-normal axis has >= 4 cells. */
 int hyb_create(const hyb_mesh *mesh, const hyb_vgrid *vgrid,
                const hyb_params *params, hyb_ctx **out);
 int hyb_destroy(hyb_ctx *ctx);

@@ -90,3 +90,21 @@ def test_invalid_arguments_are_rejected_without_a_device(lib, pkg):
     assert lib.hyb_step(None, 1, None) == T.HYB_ERR_INVALID
     assert lib.hyb_destroy(None) == T.HYB_ERR_INVALID
     assert lib.hyb_last_error(None) == b"null context"
+
+
+@pytest.mark.parametrize("ncy,ok", [(600, True), (602, False), (601, False), (256, True), (257, False), (255, True)])
+def test_scan_axis_size_limits(lib, pkg, ncy, ok):
+    """A sweep thread group must fit one 256-thread CTA: scan axes above 256
+    cells need an even count, above 512 a multiple of 4 (checked before any
+    device call)."""
+    from hyb_gb300 import cases, hyb_types as T
+    c = cases.couette_small(ncy=ncy, nvx=8, nvy=8)
+    m, g, p, keep = c.c_structs()
+    h = C.c_void_p()
+    rc = lib.hyb_create(C.byref(m), C.byref(g), C.byref(p), C.byref(h))
+    if ok:
+        assert rc in (T.HYB_OK, T.HYB_ERR_NODEVICE)
+        if rc == T.HYB_OK:
+            lib.hyb_destroy(h)
+    else:
+        assert rc == T.HYB_ERR_UNSUPPORTED

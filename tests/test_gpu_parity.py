@@ -112,6 +112,24 @@ def test_fp64_stretched_mesh(cases_mod):
     _cmp_state(c, g, o, 1e-11)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_odd_velocity_counts(cases_mod, precision):
+    """Velocity counts that are not multiples of the moment kernel's stage
+    slot (4 FP32 / 2 FP64 velocities) or of its 8-velocity sum blocks."""
+    c = cases_mod.couette_small(ncy=32, nvx=13, nvy=11, dt=0.05)
+    g, o = _pair(c, precision)
+    if precision == 0:
+        _cmp_state(c, g, o, 1e-12)
+        g.step(2)
+        o.step(2)
+        _cmp_state(c, g, o, 1e-11)
+    else:
+        g.step(2)
+        o.step(2)
+        Sg, So = _s_ring(c, g.moments()[0]), _s_ring(c, o.s_gkua())
+        assert _rel(Sg[..., 0], So[..., 0]) < 5e-6 and _rel(Sg[..., 3], So[..., 3]) < 5e-6
+
+
 def test_mixed_precision_error_is_bounded(cases_mod):
     c = cases_mod.couette_small(ncy=32, nvx=16, nvy=16, dt=0.05)
     g, o = _pair(c, 1)
