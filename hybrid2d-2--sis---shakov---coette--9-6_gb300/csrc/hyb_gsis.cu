@@ -377,19 +377,24 @@ __global__ void k_ns_faces(NsDev D, int dir) {
 
 // residual, spectral radii, local dt, band max of |Res(4)|; dU reset
 // returns |Res(4)| of a band cell (0 elsewhere)
-__device__ __forceinline__ double ns_res_body(const NsDev &D, int idx) {
+// fwd0: also the first LU-SGS pass (forward, colour 0) of the cell: its
+// neighbours in that pass are of colour 1 with dU = 0, so
+// du_LU_SGS_2D reduces to dU = Res / alpha there
+__device__ __forceinline__ double ns_res_body(const NsDev &D, int idx, bool fwd0 = false) {
     const int nx = D.nx, ny = D.ny;
     double r4 = 0.0;
     if (idx < (nx - 1) * (ny - 1)) {
         int i = idx % (nx - 1) + 1, j = idx / (nx - 1) + 1;
         size_t c = c2(D, i, j), ci = c2(D, i + 1, j), cj = c2(D, i, j + 1);
         const bool in_band = i >= D.ilo && i <= D.ihi && j >= D.jlo && j <= D.jhi;
+        double rm[4];
         for (int m = 0; m < 4; m++) {
             size_t o = (size_t)m * D.nc;
             double r = D.fluxi[o + ci] - D.fluxi[o + c] + D.fluxj[o + cj] - D.fluxj[o + c];
             if (D.src_on && in_band) r += D.src[o + c];
             D.Res[o + c] = r;
             D.dU[o + c] = 0.0;
+            rm[m] = r;
         }
         // comput_Lvc / comput_dt (sub_NS_singlegrid.f90:160-221)
         double s0 = D.vol[mi(D, i, j)];
@@ -412,8 +417,14 @@ __device__ __forceinline__ double ns_res_body(const NsDev &D, int idx) {
         if (dt < D.dtmin) dt = D.dtmin;
         D.dt[c] = dt;
         if (in_band) {
-            r4 = fabs(D.Res[3 * D.nc + c]);
+            r4 = fabs(rm[3]);
             if (r4 != r4) atomicExch(&D.ctrl->err, HYB_ERR_NONFINITE);
+            if (fwd0 && ((i + j) & 1) == 0) {
+                double alfa = s0 / dt + 1.0 * (lci + lcj);
+                alfa = alfa + 2.0 * (lvi + lvj);
+                const double ra = 1.0 / alfa;
+                for (int m = 0; m < 4; m++) D.dU[(size_t)m * D.nc + c] = (rm[m] + 0.0 + 0.0) * ra;
+            }
         }
     }
     return r4;
@@ -437,10 +448,12 @@ __global__ void k_ns_res(NsDev D) {
 __device__ __forceinline__ void dfn(const double *U, const double *dU, double n1, double n2, double g, double *DF) {
     double U2[4];
     for (int m = 0; m < 4; m++) U2[m] = U[m] + dU[m];
-    double un1 = (U[1] * n1 + U[2] * n2) / U[0];
-    double p1 = (g - 1.0) * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]);
-    double un2 = (U2[1] * n1 + U2[2] * n2) / U2[0];
-    double p2 = (g - 1.0) * (U2[3] - 0.5 * (U2[1] * U2[1] + U2[2] * U2[2]) / U2[0]);
+    // one reciprocal per state (FP64 division is a long dependent sequence)
+    const double r1 = 1.0 / U[0], r2 = 1.0 / U2[0];
+    double un1 = (U[1] * n1 + U[2] * n2) * r1;
+    double p1 = (g - 1.0) * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) * r1);
+    double un2 = (U2[1] * n1 + U2[2] * n2) * r2;
+    double p2 = (g - 1.0) * (U2[3] - 0.5 * (U2[1] * U2[1] + U2[2] * U2[2]) * r2);
     DF[0] = U2[0] * un2 - U[0] * un1;
     DF[1] = (U2[1] * un2 + p2 * n1) - (U[1] * un1 + p1 * n1);
     DF[2] = (U2[2] * un2 + p2 * n2) - (U[2] * un1 + p1 * n2);
@@ -474,7 +487,8 @@ __device__ __forceinline__ void ns_lusgs_body(const NsDev &D, int color, int bwd
             for (int m = 0; m < 4; m++)
                 duj[m] = 0.5 * (DF[m] * D.sj[mi(D, i, j)] + w * D.Lcj[cn] * dUn[m]) + D.Lvj[cn] * dUn[m];
         }
-        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = (D.Res[m * D.nc + c] + dui[m] + duj[m]) / alfa;
+        const double ra = 1.0 / alfa;
+        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = (D.Res[m * D.nc + c] + dui[m] + duj[m]) * ra;
     } else {
         if (i != D.ihi) {
             size_t cn = c2(D, i + 1, j);
@@ -490,7 +504,8 @@ __device__ __forceinline__ void ns_lusgs_body(const NsDev &D, int color, int bwd
             for (int m = 0; m < 4; m++)
                 duj[m] = -0.5 * (DF[m] * D.sj[mi(D, i, j + 1)] - w * D.Lcj[cn] * dUn[m]) + D.Lvj[cn] * dUn[m];
         }
-        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = D.dU[m * D.nc + c] + (dui[m] + duj[m]) / alfa;
+        const double ra = 1.0 / alfa;
+        for (int m = 0; m < 4; m++) D.dU[m * D.nc + c] = D.dU[m * D.nc + c] + (dui[m] + duj[m]) * ra;
     }
 }
 
@@ -694,14 +709,17 @@ __global__ void k_ns_close(NsDev D) {
     }
 }
 
-// The LU-SGS inner loop of a small mesh in one cooperative launch.  The
-// phases of an iteration (primitives, face fluxes, residual, the four colour
-// passes, update, periodic ghosts, stop test) are separated by grid-wide
-// barriers (the launch guarantees that all blocks are resident) and the loop
-// runs at most max_it times, so one launch replaces the graph batches.  The
-// arithmetic per cell is that of the multi-kernel path.  GB300's FP64 rate
-// per SM is small, so the mesh is spread one warp per SM over as many SMs as
-// it has warps of cells.
+// The LU-SGS inner loop of a small mesh in one cooperative launch.  An
+// iteration has five phases separated by grid-wide barriers (the launch
+// guarantees that all blocks are resident): face fluxes; residual with the
+// first colour pass and the stop test; the three other colour passes; update
+// with the periodic ghost images and the primitives of the changed cells.
+// The loop runs at most max_it times, so one launch replaces the graph
+// batches, and the arithmetic per cell is that of the multi-kernel path.
+// Each phase is a chain of dependent FP64 operations and L2 accesses per
+// cell; GB300 issues FP64 at 2 lanes per clock per SM, so one warp per SM
+// spread over as many SMs as the mesh has warps of cells keeps that chain
+// short.
 constexpr int NS_COOP_THREADS = 32;
 constexpr size_t NS_COOP_MAX_CELLS = 65536;
 
@@ -739,6 +757,47 @@ __device__ bool ns_grid_sync(NsCtrl *C) {
     return ok != 0;
 }
 
+// U += dU of one band cell, its periodic ghost images (the copies
+// ns_ghosts makes) and the primitives of the cell and of its images; the
+// images' primitives are those of the cell (the same function of the same U)
+__device__ __forceinline__ void ns_update_prims_body(const NsDev &D, int idx) {
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    if (idx >= bw * bh) return;
+    const int i = idx % bw + D.ilo, j = idx / bw + D.jlo, nx = D.nx, ny = D.ny;
+    const size_t c = c2(D, i, j);
+    double u4[4];
+    for (int m = 0; m < 4; m++) {
+        u4[m] = D.U[m * D.nc + c] + D.dU[m * D.nc + c];
+        D.U[m * D.nc + c] = u4[m];
+    }
+    ns_prims_body(D, c);
+    int gi[2] = {i, i}, gj[2] = {j, j}, ni = 1, nj = 1;
+    if (D.perx) {
+        if (i == nx - 1) gi[ni++] = 0;
+        else if (i == nx - 2) gi[ni++] = -1;
+        else if (i == 1) gi[ni++] = nx;
+        else if (i == 2) gi[ni++] = nx + 1;
+    }
+    if (D.pery) {
+        if (j == ny - 1) gj[nj++] = 0;
+        else if (j == ny - 2) gj[nj++] = -1;
+        else if (j == 1) gj[nj++] = ny;
+        else if (j == 2) gj[nj++] = ny + 1;
+    }
+    for (int a = 0; a < ni; a++)
+        for (int b = 0; b < nj; b++) {
+            if (a == 0 && b == 0) continue;
+            const size_t g = c2(D, gi[a], gj[b]);
+            for (int m = 0; m < 4; m++) D.U[m * D.nc + g] = u4[m];
+            D.d[g] = D.d[c];
+            D.uu[g] = D.uu[c];
+            D.vv[g] = D.vv[c];
+            D.T[g] = D.T[c];
+            D.p[g] = D.p[c];
+            if (gi[a] >= 0 && gi[a] <= nx && gj[b] >= 0 && gj[b] <= ny) D.amu[g] = D.amu[c];
+        }
+}
+
 __global__ void __launch_bounds__(NS_COOP_THREADS) k_ns_coop(NsDev D) {
     __shared__ double red[NS_COOP_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -748,9 +807,13 @@ __global__ void __launch_bounds__(NS_COOP_THREADS) k_ns_coop(NsDev D) {
     const int nfi = D.nx * (D.ny - 1), nfj = (D.nx - 1) * D.ny, ncl = (D.nx - 1) * (D.ny - 1);
     const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
     const int max_it = V->max_it;
+    const double rtol = V->rtol;
+    double tol = V->tol;
+    // primitives of every cell; afterwards only the band and its ghost
+    // images change, and the update phase recomputes theirs
+    for (size_t idx = g0; idx < D.nc; idx += G) ns_prims_body(D, idx);   // idx 0 clears res_bits
+    if (!ns_grid_sync(C)) return;
     for (int it = 0; it < max_it; it++) {
-        for (size_t idx = g0; idx < D.nc; idx += G) ns_prims_body(D, idx);   // idx 0 clears res_bits
-        if (!ns_grid_sync(C)) return;
         for (int idx = g0; idx < nfi + nfj; idx += G) {
             if (idx < nfi) ns_faces_body(D, 0, idx);
             else ns_faces_body(D, 1, idx - nfi);
@@ -758,7 +821,7 @@ __global__ void __launch_bounds__(NS_COOP_THREADS) k_ns_coop(NsDev D) {
         if (!ns_grid_sync(C)) return;
         double r4 = 0.0;
         for (int idx = g0; idx < ncl; idx += G) {
-            const double r = ns_res_body(D, idx);
+            const double r = ns_res_body(D, idx, true);     // with the first LU-SGS pass
             if (r > r4) r4 = r;
         }
         for (int off = 16; off > 0; off >>= 1) {
@@ -774,31 +837,27 @@ __global__ void __launch_bounds__(NS_COOP_THREADS) k_ns_coop(NsDev D) {
             atomicMax(&C->res_bits, (unsigned long long)__double_as_longlong(m));
         }
         if (!ns_grid_sync(C)) return;
-        for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 0, 0, idx);
-        if (!ns_grid_sync(C)) return;
+        // the stop test of this iteration, taken by every thread on the same
+        // values; the iteration's update is still applied
+        const double res = __longlong_as_double((long long)V->res_bits);
+        const int itn = it + 1;
+        if (itn == 1 && rtol * res > tol) tol = rtol * res;
+        const bool last = !(res > tol) || itn >= max_it || V->err != 0;
         for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 1, 0, idx);
         if (!ns_grid_sync(C)) return;
         for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 1, 1, idx);
         if (!ns_grid_sync(C)) return;
         for (int idx = g0; idx < nband; idx += G) ns_lusgs_body(D, 0, 1, idx);
         if (!ns_grid_sync(C)) return;
-        for (int idx = g0; idx < nband; idx += G) ns_update_body(D, idx);
-        if (!ns_grid_sync(C)) return;
-        if (blockIdx.x == 0) {
-            ns_ghosts(D);
-            __syncthreads();
-            if (tid == 0) {
-                const double res = __longlong_as_double((long long)V->res_bits);
-                const int itn = V->it + 1;
-                V->it = itn;
-                double tol = V->tol;
-                if (itn == 1 && V->rtol * res > tol) tol = V->rtol * res;
-                V->tol = tol;
-                if (!(res > tol) || itn >= V->max_it || V->err) V->done = 1;
-            }
+        for (int idx = g0; idx < nband; idx += G) ns_update_prims_body(D, idx);
+        if (g0 == 0) {
+            V->res_bits = 0ull;
+            V->it = itn;
+            V->tol = tol;
+            if (last) V->done = 1;
         }
         if (!ns_grid_sync(C)) return;
-        if (V->done) break;
+        if (last) break;
     }
 }
 
