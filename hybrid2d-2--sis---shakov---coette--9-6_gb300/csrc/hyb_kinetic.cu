@@ -13,14 +13,20 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <cooperative_groups.h>
+
 #include "hyb_common.cuh"
 #include "hyb_device.cuh"
 
 namespace hyb {
 
 // ---------------------------------------------------------------------------
-// diffuse wall: one CTA per wall face cell
+// diffuse wall: one cluster of WALL_CL CTAs per wall face cell; each CTA
+// takes a contiguous share of the velocities, the n_w flux balance adds the
+// CTAs' partial sums in rank order through distributed shared memory
 // ---------------------------------------------------------------------------
+constexpr int WALL_CL = 8;
+
 struct WallFace {
     // position of the face cells in the (a,b) layout
     int on_scan;      // 1: wall at a scan-axis end (cells along b), 0: march end
@@ -29,10 +35,15 @@ struct WallFace {
 };
 
 template <typename real>
-__global__ void k_wall(const real *__restrict__ f, real *__restrict__ fw, const double *__restrict__ wd,
-                       const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ w,
-                       int nvi, int nv, int Na, int Nb, int PA, int on_scan, int hi) {
-    const int k = blockIdx.x;   // face cell (0-based, face order)
+__global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
+    k_wall(const real *__restrict__ f, real *__restrict__ fw, const double *__restrict__ wd,
+           const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ w, int nvi,
+           int nv, int Na, int Nb, int PA, int on_scan, int hi) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int k = blockIdx.x / WALL_CL;   // face cell (0-based, face order)
+    const int per = (nv + WALL_CL - 1) / WALL_CL, vb = rank * per, ve = min(nv, vb + per);
     // wall data: [k][6] = u, v, t, swnx, swny, step
     const double uw = wd[k * 6 + 0], vw = wd[k * 6 + 1], tw = wd[k * 6 + 2];
     const double swnx = wd[k * 6 + 3], swny = wd[k * 6 + 4], step = wd[k * 6 + 5];
@@ -51,7 +62,7 @@ __global__ void k_wall(const real *__restrict__ f, real *__restrict__ fw, const 
     }
     const size_t rs = (size_t)Nb * PA;
     double s0 = 0.0, s1 = 0.0;
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) {
         const real *fv = f + (size_t)v * 2 * rs;
         double vxx = vx[v % nvi], vyy = vy[v / nvi];
         double wt = w[v];
@@ -72,6 +83,7 @@ __global__ void k_wall(const real *__restrict__ f, real *__restrict__ fw, const 
         s1 += wt * fb;
     }
     __shared__ double r0[256], r1[256];
+    __shared__ double part[2], nw_sh;
     r0[threadIdx.x] = s0;
     r1[threadIdx.x] = s1;
     __syncthreads();
@@ -82,8 +94,23 @@ __global__ void k_wall(const real *__restrict__ f, real *__restrict__ fw, const 
         }
         __syncthreads();
     }
-    const double nwall = -r0[0] / r1[0];
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    if (threadIdx.x == 0) {
+        part[0] = r0[0];
+        part[1] = r1[0];
+    }
+    cl.sync();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int q = 0; q < WALL_CL; q++) {
+            const double *pq = cl.map_shared_rank(part, q);
+            t0 += pq[0];
+            t1 += pq[1];
+        }
+        nw_sh = -t0 / t1;
+    }
+    cl.sync();   // every CTA has read the partials before any exits
+    const double nwall = nw_sh;
+    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) {
         double vxx = vx[v % nvi], vyy = vy[v / nvi];
         double vnw = ((vxx - uw) * swnx + (vyy - vw) * swny) * step;
         if (vnw >= 0.0) {
@@ -274,20 +301,28 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
         for (int c = 0; c < MC; c++) M.part[((size_t)slice * 10 + q) * ncell + cell0 + c] = ks[q][c].fold();
 }
 
+// lpc lanes per cell (a power of two <= 32): lane l of a cell's group adds
+// the slices l, l+lpc, ... in order, then the group folds by xor shuffles
+// (a fixed order); small meshes spread the slice sums over the lanes
 template <typename real>
-__global__ void k_moments_finish(MomArgs M) {
+__global__ void k_moments_finish(MomArgs M, int lpc) {
     const size_t ncell = (size_t)M.Nb * M.PA;
-    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= ncell) return;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t cell = tid / lpc;
+    const int sub = (int)(tid % lpc);
     const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
-    if (a > M.Na) return;
+    const bool ok = cell < ncell && a <= M.Na;
     double s[10];
 #pragma unroll
-    for (int q = 0; q < 10; q++) {
-        double x = 0.0;
-        for (int sl = 0; sl < M.vs; sl++) x += M.part[((size_t)sl * 10 + q) * ncell + cell];
-        s[q] = x;
-    }
+    for (int q = 0; q < 10; q++) s[q] = 0.0;
+    if (ok)
+        for (int sl = sub; sl < M.vs; sl += lpc)
+#pragma unroll
+            for (int q = 0; q < 10; q++) s[q] += M.part[((size_t)sl * 10 + q) * ncell + cell];
+    for (int off = lpc >> 1; off > 0; off >>= 1)
+#pragma unroll
+        for (int q = 0; q < 10; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
+    if (!ok || sub != 0) return;
     // primitive conversion, GKUA_DETFP.f90:59-92
     double S1 = s[0], S4 = s[3], S5 = s[4], S6 = s[5], S7 = s[6];
     double ron = S1;
@@ -480,11 +515,11 @@ int launch_wall(hyb_ctx *ctx) {
         int nfc = (face == 1 || face == 3) ? ctx->ncy : ctx->ncx;
         const double *wd = ctx->d_wall + (size_t)(face - 1) * 6 * 4096;
         if (ctx->precision == HYB_PREC_FP64)
-            k_wall<double><<<nfc, 256, 0, ctx->stream>>>((const double *)ctx->d_f, (double *)ctx->d_fw[face - 1], wd,
+            k_wall<double><<<nfc * WALL_CL, 256, 0, ctx->stream>>>((const double *)ctx->d_f, (double *)ctx->d_fw[face - 1], wd,
                                                           ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
                                                           ctx->Nb, ctx->PA, on_scan, hi);
         else
-            k_wall<float><<<nfc, 256, 0, ctx->stream>>>((const float *)ctx->d_f, (float *)ctx->d_fw[face - 1], wd,
+            k_wall<float><<<nfc * WALL_CL, 256, 0, ctx->stream>>>((const float *)ctx->d_f, (float *)ctx->d_fw[face - 1], wd,
                                                          ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
                                                          ctx->Nb, ctx->PA, on_scan, hi);
         ctx->launches++;
@@ -562,9 +597,13 @@ int launch_moments(hyb_ctx *ctx) {
     int rc = check_err(ctx, "k_moments_part");
     if (rc) return rc;
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
-    const unsigned nb = (unsigned)((ncell + 255) / 256);
-    if (ctx->precision == HYB_PREC_FP64) k_moments_finish<double><<<nb, 256, 0, ctx->stream>>>(M);
-    else k_moments_finish<float><<<nb, 256, 0, ctx->stream>>>(M);
+    // lanes per cell: enough for the slices, while the grid keeps about
+    // 64K threads (one lane per cell on large meshes)
+    int lpc = 1;
+    while (lpc < 32 && lpc < M.vs && ncell * (size_t)(lpc * 2) <= 65536) lpc *= 2;
+    const unsigned nb = (unsigned)((ncell * lpc + 255) / 256);
+    if (ctx->precision == HYB_PREC_FP64) k_moments_finish<double><<<nb, 256, 0, ctx->stream>>>(M, lpc);
+    else k_moments_finish<float><<<nb, 256, 0, ctx->stream>>>(M, lpc);
     ctx->launches++;
     return check_err(ctx, "k_moments_finish");
 }
