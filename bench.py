@@ -217,11 +217,19 @@ def time_to_residual(tol=1e-8, max_iters=8000, chunk=50):
             s.attach_mlp(net)
             s.gsis(**g)
         it, r, prev, switched_at = 0, None, None, None
+        best, best_it, stalled = None, 0, False
         t0 = time.perf_counter()
         while it < max_iters:
             r = s.step(chunk)
             it += chunk
             if r["max_rms"] <= tol:
+                break
+            # an FP32 run that has stopped falling below 1e-4 for 1000
+            # iterations sits on its rounding floor: stop and report it
+            if best is None or r["max_rms"] < 0.9 * best:
+                best, best_it = r["max_rms"], it
+            elif prec == 1 and not switch and r["max_rms"] < 1e-4 and it - best_it >= 1000:
+                stalled = True
                 break
             if switch and switched_at is None and (r["max_rms"] <= switch_at or (
                     r["max_rms"] < 1e-4 and prev is not None and r["max_rms"] > 0.9 * prev)):
@@ -238,6 +246,8 @@ def time_to_residual(tol=1e-8, max_iters=8000, chunk=50):
                      "reached": bool(r["max_rms"] <= tol), "u_mid_wall": float(u[-1].mean())}
         if switch:
             out[name]["fp64_from_iteration"] = switched_at
+        if stalled:
+            out[name]["stalled_on_fp32_floor"] = True
         s.close()
     ref = out["plain_fp64"]["u_mid_wall"]
     for v in out.values():

@@ -297,7 +297,7 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     if (rc == HYB_OK) ALLOC(c->d_x1, nc2 * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_y1, nc2 * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_hot, hyb::hot_doubles(c->nx, c->ny) * sizeof(double));
-    size_t nblk = (size_t)((c->Na + 31) / 32) * c->Nb;
+    const size_t nblk = (size_t)hyb::residual_blocks(c);
     if (rc == HYB_OK) ALLOC(c->d_resid, (16 + 8 * nblk) * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_err, sizeof(int));
     if (rc == HYB_OK) ALLOC(c->d_mpart, (size_t)hyb::moments_slices(c) * 10 * ncell * sizeof(double));

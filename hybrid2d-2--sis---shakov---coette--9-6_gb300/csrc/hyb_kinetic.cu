@@ -177,7 +177,9 @@ __host__ __device__ inline size_t mom_smem_bytes(int PA, int nloc_max) {
     return b;
 }
 
-template <typename real, int MC>
+// NM = 10: the DETFP moments; NM = 4: moments 1-4 only (the residual of a
+// stored RHS, DETFP_res)
+template <typename real, int MC, int NM>
 __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int VPS = MomVps<real>::v;
@@ -225,10 +227,10 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     if (t == 0)
         for (int n = 0; n < MOM_NST - 1 && n < nslot; n++) issue(n);
     // plain sums over blocks of 8 velocities, compensated sums of the blocks
-    KahanAcc<real> ks[10][MC];
-    real blk[10][MC];
+    KahanAcc<real> ks[NM][MC];
+    real blk[NM][MC];
 #pragma unroll
-    for (int q = 0; q < 10; q++)
+    for (int q = 0; q < NM; q++)
 #pragma unroll
         for (int c = 0; c < MC; c++) {
             ks[q][c].zero();
@@ -266,18 +268,20 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
                         blk[1][c] += wx * gg[c];
                         blk[2][c] += wy * gg[c];
                         blk[3][c] += wv * b4;
-                        blk[4][c] += wx * (vx * gg[c]);
-                        blk[5][c] += wy * (vy * gg[c]);
-                        blk[6][c] += wxy * gg[c];
-                        blk[7][c] += wx * b4;
-                        blk[8][c] += wy * b4;
-                        blk[9][c] += wv * hh[c];
+                        if constexpr (NM > 4) {
+                            blk[4][c] += wx * (vx * gg[c]);
+                            blk[5][c] += wy * (vy * gg[c]);
+                            blk[6][c] += wxy * gg[c];
+                            blk[7][c] += wx * b4;
+                            blk[8][c] += wy * b4;
+                            blk[9][c] += wv * hh[c];
+                        }
                     }
                 }
             }
             if ((n % FLUSH) == FLUSH - 1 || n == nslot - 1) {
 #pragma unroll
-                for (int q = 0; q < 10; q++)
+                for (int q = 0; q < NM; q++)
 #pragma unroll
                     for (int c = 0; c < MC; c++) {
                         ks[q][c].add(blk[q][c]);
@@ -296,9 +300,9 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     const size_t ncell = (size_t)M.Nb * PA;
     const size_t cell0 = (size_t)(b - 1) * PA + (a0 - 1);
 #pragma unroll
-    for (int q = 0; q < 10; q++)
+    for (int q = 0; q < NM; q++)
 #pragma unroll
-        for (int c = 0; c < MC; c++) M.part[((size_t)slice * 10 + q) * ncell + cell0 + c] = ks[q][c].fold();
+        for (int c = 0; c < MC; c++) M.part[((size_t)slice * NM + q) * ncell + cell0 + c] = ks[q][c].fold();
 }
 
 // lpc lanes per cell (a power of two <= 32): lane l of a cell's group adds
@@ -365,66 +369,68 @@ __global__ void k_moments_finish(MomArgs M, int lpc) {
 }
 
 // ---------------------------------------------------------------------------
-// residual: moments 1..4 of the stored RHS per cell, then rms / max
+// residual (DETFP_res): moments 1..4 of the stored RHS per cell by
+// k_moments_part<., ., 4> over velocity slices, then per cell the slice sums
+// (lanes per cell as in k_moments_finish), and per block the max |x| and the
+// sum of x^2 of the block's cells; k_residual_final folds the blocks
 // ---------------------------------------------------------------------------
-template <typename real, int VS>
-__global__ void __launch_bounds__(32 * VS) k_residual(const real *__restrict__ rhs, const double *__restrict__ vx,
-                                                       const double *__restrict__ vy, const double *__restrict__ w,
-                                                       int nvi, int nv, int Na, int Nb, int PA,
-                                                       double *__restrict__ part, double *__restrict__ cellm) {
-    const int tx = threadIdx.x, sl = threadIdx.y;
-    const int a = blockIdx.x * 32 + tx + 1, b = blockIdx.y + 1;
-    const bool act = a <= Na;
-    const size_t cell = (size_t)(b - 1) * PA + (a - 1);
-    const size_t rs = (size_t)Nb * PA;
-    double acc[4] = {0, 0, 0, 0};
-    const int nvj = nv / nvi;
-    if (act) {
-        for (int jv = sl; jv < nvj; jv += VS) {
-            KahanAcc<real> s[4];
+__device__ __forceinline__ double nanmax(double a, double b) {
+    if (a != a) return a;
+    if (b != b) return b;
+    return b > a ? b : a;
+}
+
+__global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, double *__restrict__ part,
+                                                         double *__restrict__ cellm) {
+    const size_t ncell = (size_t)M.Nb * M.PA;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t cell = tid / lpc;
+    const int sub = (int)(tid % lpc);
+    const int a = (int)(cell % M.PA) + 1;
+    const bool ok = cell < ncell && a <= M.Na;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ok)
+        for (int sl = sub; sl < M.vs; sl += lpc)
 #pragma unroll
-            for (int k = 0; k < 4; k++) s[k].zero();
-            const real vyy = (real)vy[jv];
-            for (int iv = 0; iv < nvi; iv++) {
-                int v = iv + nvi * jv;
-                const real vxx = (real)vx[iv];
-                const real wv = (real)w[v];
-                real gg = rhs[(size_t)v * 2 * rs + cell], hh = rhs[(size_t)v * 2 * rs + rs + cell];
-                real vxg = vxx * gg, vyg = vyy * gg;
-                s[0].add(wv * gg);
-                s[1].add(wv * vxg);
-                s[2].add(wv * vyg);
-                s[3].add(wv * (hh + vxx * vxg + vyy * vyg));
-            }
+            for (int q = 0; q < 4; q++) s[q] += M.part[((size_t)sl * 4 + q) * ncell + cell];
+    for (int off = lpc >> 1; off > 0; off >>= 1)
 #pragma unroll
-            for (int k = 0; k < 4; k++) acc[k] += s[k].fold();
-        }
+        for (int q = 0; q < 4; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
+    const bool own = ok && sub == 0;
+    if (own && cellm)
+#pragma unroll
+        for (int q = 0; q < 4; q++) cellm[(size_t)q * ncell + cell] = s[q];
+    double mx[4], sq[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double x = own ? s[q] : 0.0;
+        mx[q] = fabs(x);
+        sq[q] = x * x;
     }
-    __shared__ double red[VS][4][33];
+    for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-    for (int k = 0; k < 4; k++) red[sl][k][tx] = acc[k];
-    __syncthreads();
-    // per-cell value, then block max and sum of squares (deterministic)
-    __shared__ double cellv[4][32];
-    if (sl == 0) {
-        for (int k = 0; k < 4; k++) {
-            double x = 0.0;
-            for (int q = 0; q < VS; q++) x += red[q][k][tx];
-            cellv[k][tx] = act ? x : 0.0;
-            if (cellm && act) cellm[(size_t)k * Nb * PA + cell] = x;
+        for (int q = 0; q < 4; q++) {
+            mx[q] = nanmax(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], off));
+            sq[q] += __shfl_xor_sync(0xffffffffu, sq[q], off);
         }
-    }
-    __syncthreads();
-    if (sl == 0 && tx < 4) {
-        double mx = 0.0, ss = 0.0;
-        for (int q = 0; q < 32; q++) {
-            double x = cellv[tx][q];
-            if (fabs(x) > mx || x != x) mx = fabs(x);
-            ss += x * x;
+    __shared__ double wm[8][4], ws[8][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            wm[warp][q] = mx[q];
+            ws[warp][q] = sq[q];
         }
-        size_t blk = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
-        part[blk * 8 + tx] = mx;
-        part[blk * 8 + 4 + tx] = ss;
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        const int q = threadIdx.x;
+        double m = 0.0, t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            m = nanmax(m, wm[w][q]);
+            t += ws[w][q];
+        }
+        part[(size_t)blockIdx.x * 8 + q] = m;
+        part[(size_t)blockIdx.x * 8 + 4 + q] = t;
     }
 }
 
@@ -538,19 +544,34 @@ int moments_slices(const hyb_ctx *ctx) {
     return vs;
 }
 
-template <typename real, int MC>
+template <typename real, int MC, int NM>
 static void launch_mom(hyb_ctx *ctx, const MomArgs &M, dim3 grd, int tpv, size_t smem) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_moments_part<real, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_moments_part<real, MC, NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024);
         attr = true;
     }
-    k_moments_part<real, MC><<<grd, tpv, smem, ctx->stream>>>(M);
+    k_moments_part<real, MC, NM><<<grd, tpv, smem, ctx->stream>>>(M);
 }
 
-int launch_moments(hyb_ctx *ctx) {
+// lanes per cell of the slice sums: enough for the slices, while the grid
+// keeps about 64K threads (one lane per cell on large meshes)
+static int finish_lpc(size_t ncell, int vs) {
+    int lpc = 1;
+    while (lpc < 32 && lpc < vs && ncell * (size_t)(lpc * 2) <= 65536) lpc *= 2;
+    return lpc;
+}
+
+int residual_blocks(const hyb_ctx *ctx) {
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    return (int)((ncell * finish_lpc(ncell, moments_slices(ctx)) + 255) / 256);
+}
+
+// MomArgs of the moment pass over the velocity slices of distribution `f`
+static MomArgs mom_args(hyb_ctx *ctx, const void *f, size_t *smem, int *mc) {
     MomArgs M;
-    M.f = ctx->d_f;
+    M.f = f;
     M.part = ctx->d_mpart;
     M.S = ctx->d_S;
     M.CF = ctx->d_CF;
@@ -577,30 +598,39 @@ int launch_moments(hyb_ctx *ctx) {
     // cells per thread: two where the chunk allows it (both precisions stay
     // below 128 registers without spills), one on FP64 rows of <= 256 cells
     // so that more threads share them; a CTA has at most 512 threads
-    const int mc = (ctx->cpt >= 2 && (ctx->precision != HYB_PREC_FP64 || ctx->PA > 256)) ? 2 : 1;
-    const int tpv = ctx->PA / mc;
-    const size_t smem = ctx->precision == HYB_PREC_FP64 ? mom_smem_bytes<double>(ctx->PA, M.nloc_max)
-                                                        : mom_smem_bytes<float>(ctx->PA, M.nloc_max);
+    *mc = (ctx->cpt >= 2 && (ctx->precision != HYB_PREC_FP64 || ctx->PA > 256)) ? 2 : 1;
+    *smem = ctx->precision == HYB_PREC_FP64 ? mom_smem_bytes<double>(ctx->PA, M.nloc_max)
+                                            : mom_smem_bytes<float>(ctx->PA, M.nloc_max);
+    return M;
+}
+
+template <int NM>
+static int launch_mom_pass(hyb_ctx *ctx, const MomArgs &M, int mc, size_t smem) {
     if (smem > (size_t)227 * 1024) {
         ctx->last_error = "moments: velocity slice too large for shared memory";
         return HYB_ERR_UNSUPPORTED;
     }
+    const int tpv = ctx->PA / mc;
     dim3 grd(ctx->Nb, M.vs);
     if (ctx->precision == HYB_PREC_FP64) {
-        if (mc == 2) launch_mom<double, 2>(ctx, M, grd, tpv, smem);
-        else launch_mom<double, 1>(ctx, M, grd, tpv, smem);
+        if (mc == 2) launch_mom<double, 2, NM>(ctx, M, grd, tpv, smem);
+        else launch_mom<double, 1, NM>(ctx, M, grd, tpv, smem);
     } else {
-        if (mc == 2) launch_mom<float, 2>(ctx, M, grd, tpv, smem);
-        else launch_mom<float, 1>(ctx, M, grd, tpv, smem);
+        if (mc == 2) launch_mom<float, 2, NM>(ctx, M, grd, tpv, smem);
+        else launch_mom<float, 1, NM>(ctx, M, grd, tpv, smem);
     }
     ctx->launches++;
-    int rc = check_err(ctx, "k_moments_part");
+    return check_err(ctx, "k_moments_part");
+}
+
+int launch_moments(hyb_ctx *ctx) {
+    size_t smem;
+    int mc;
+    MomArgs M = mom_args(ctx, ctx->d_f, &smem, &mc);
+    int rc = launch_mom_pass<10>(ctx, M, mc, smem);
     if (rc) return rc;
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
-    // lanes per cell: enough for the slices, while the grid keeps about
-    // 64K threads (one lane per cell on large meshes)
-    int lpc = 1;
-    while (lpc < 32 && lpc < M.vs && ncell * (size_t)(lpc * 2) <= 65536) lpc *= 2;
+    const int lpc = finish_lpc(ncell, M.vs);
     const unsigned nb = (unsigned)((ncell * lpc + 255) / 256);
     if (ctx->precision == HYB_PREC_FP64) k_moments_finish<double><<<nb, 256, 0, ctx->stream>>>(M, lpc);
     else k_moments_finish<float><<<nb, 256, 0, ctx->stream>>>(M, lpc);
@@ -608,21 +638,21 @@ int launch_moments(hyb_ctx *ctx) {
     return check_err(ctx, "k_moments_finish");
 }
 
+// moments 1-4 of a stored RHS: per-cell values to cellm (if given) and the
+// per-block max / sum of squares to the residual partials
 static int residual_part(hyb_ctx *ctx, const void *rhs, double *cellm, int *nblk_out) {
-    constexpr int VS = 8;
-    dim3 blk(32, VS), grd((ctx->Na + 31) / 32, ctx->Nb);
-    *nblk_out = grd.x * grd.y;
-    double *part = ctx->d_resid + 16;
-    if (ctx->precision == HYB_PREC_FP64)
-        k_residual<double, VS><<<grd, blk, 0, ctx->stream>>>((const double *)rhs, ctx->d_vx, ctx->d_vy, ctx->d_w,
-                                                              ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA, part,
-                                                              cellm);
-    else
-        k_residual<float, VS><<<grd, blk, 0, ctx->stream>>>((const float *)rhs, ctx->d_vx, ctx->d_vy, ctx->d_w,
-                                                             ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA, part,
-                                                             cellm);
+    size_t smem;
+    int mc;
+    MomArgs M = mom_args(ctx, rhs, &smem, &mc);
+    int rc = launch_mom_pass<4>(ctx, M, mc, smem);
+    if (rc) return rc;
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    const int lpc = finish_lpc(ncell, M.vs);
+    const unsigned nb = (unsigned)((ncell * lpc + 255) / 256);
+    *nblk_out = (int)nb;
+    k_residual_finish<<<nb, 256, 0, ctx->stream>>>(M, lpc, ctx->d_resid + 16, cellm);
     ctx->launches++;
-    return check_err(ctx, "k_residual");
+    return check_err(ctx, "k_residual_finish");
 }
 
 // per-cell moments 1-4 of the RHS-only sweep's output, [4][Nb*PA]
