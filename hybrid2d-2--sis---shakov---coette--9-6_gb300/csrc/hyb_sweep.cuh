@@ -340,6 +340,13 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
             Vec<real, CPT>::ld(ep + 6 * ncell + cell0, e_qy);
             Vec<real, CPT>::ld(ep + 7 * ncell + cell0, e_cf);
             if (!UNI) Vec<real, CPT>::ld(A.vol + cell0, vl);
+            // the next row's Shakhov parameters towards L1 while this row
+            // computes (one prefetch per 128-byte line)
+            if (b < Nb && ((a0 - 1) * (int)sizeof(real)) % 128 == 0) {
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(ep + q * ncell + cell0 + PA));
+            }
             if (stdB) {
                 real p0[CPT], p1[CPT], q0[CPT], q1[CPT];
                 Vec<real, CPT>::ld(rp + (a0 - 1), p0);
