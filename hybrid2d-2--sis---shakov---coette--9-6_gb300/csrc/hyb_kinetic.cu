@@ -61,6 +61,7 @@ __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
         nslot = PA;
     }
     const size_t rs = (size_t)Nb * PA;
+    extern __shared__ double emax[];   // exp(-c^2/Tw)/(pi Tw) of this CTA's velocities
     double s0 = 0.0, s1 = 0.0;
     for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) {
         const real *fv = f + (size_t)v * 2 * rs;
@@ -78,8 +79,10 @@ __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
         double vnw = ((vxx - uw) * swnx + (vyy - vw) * swny) * step;
         double vnn = (vnw - fabs(vnw)) / 2.0;
         s0 += wt * (vnn * tG);
-        double fb = (vnw + fabs(vnw)) / 2.0 * exp(-((vxx - uw) * (vxx - uw) + (vyy - vw) * (vyy - vw)) / tw) /
-                    (HYB_PI * tw);
+        const double cv = (vxx - uw) * (vxx - uw) + (vyy - vw) * (vyy - vw);
+        const double em = exp(-cv / tw) / (HYB_PI * tw);
+        emax[v - vb] = em;
+        double fb = (vnw + fabs(vnw)) / 2.0 * em;
         s1 += wt * fb;
     }
     __shared__ double r0[256], r1[256];
@@ -114,8 +117,7 @@ __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
         double vxx = vx[v % nvi], vyy = vy[v / nvi];
         double vnw = ((vxx - uw) * swnx + (vyy - vw) * swny) * step;
         if (vnw >= 0.0) {
-            double cv = (vxx - uw) * (vxx - uw) + (vyy - vw) * (vyy - vw);
-            double gg = nwall * exp(-cv / tw) / (HYB_PI * tw);
+            double gg = nwall * emax[v - vb];   // each thread reads its own entries
             fw[((size_t)v * 2 + 0) * nslot + k] = (real)gg;
             fw[((size_t)v * 2 + 1) * nslot + k] = (real)(tw * gg / 2.0);
         }
@@ -126,15 +128,15 @@ __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
 // moments.  k_moments_part: one CTA per (march row b, velocity slice); the
 // slice's velocity rows stream through an NST-stage shared-memory ring filled
 // by cp.async.bulk (full/empty mbarrier pairs), each thread accumulates MC
-// cells.  Mixed mode sums blocks of 8 velocities in plain FP32, adds the block
-// sums with Kahan compensation and folds the result into FP64 (the block
-// rounding is of the order of the FP32 inputs' own); FP64 mode accumulates in
-// FP64.  k_moments_finish
-// adds the slices in fixed order and applies DETFP's primitive conversion.
+// cells.  Mixed mode sums blocks of 8 velocities in plain FP32 and adds the
+// block sums with Kahan compensation (the block rounding is of the order of
+// the FP32 inputs' own); FP64 mode accumulates in FP64.  k_moments_finish
+// adds the slices in fixed order (float-float in mixed mode, converted to
+// FP64 once per cell) and applies DETFP's primitive conversion.
 // ---------------------------------------------------------------------------
 struct MomArgs {
     const void *f;
-    double *part;       // [VS][10][Nb*PA]
+    double *part;       // [VS][10][Nb*PA]: double (FP64), float2 Kahan pair (mixed)
     double *S;          // [NSUM][(nx+3)(ny+3)]
     double *CF;         // [(nx+3)(ny+3)]
     void *eqp;          // [8][Nb*PA] real
@@ -150,7 +152,6 @@ template <> struct KahanAcc<double> {
     double s;
     __device__ void zero() { s = 0; }
     __device__ void add(double x) { s += x; }
-    __device__ double fold() { double r = s; s = 0; return r; }
 };
 template <> struct KahanAcc<float> {
     float s, c;
@@ -161,8 +162,49 @@ template <> struct KahanAcc<float> {
         c = (t - s) - y;
         s = t;
     }
-    __device__ double fold() { double r = (double)s - (double)c; s = 0.f; c = 0.f; return r; }
 };
+
+// Per-slice partial sums.  FP64 mode stores a double per (slice, moment,
+// cell).  FP32 mode stores the slice's Kahan pair as a float2 (s, -c) whose
+// value is x + y: the slices are then added in float-float arithmetic and
+// converted to double once per cell, which keeps float-to-double conversions
+// (2 lanes per clock per SM on GB300) out of the per-slice work.
+template <typename real> struct SliceSum;
+template <> struct SliceSum<double> {
+    double a;
+    __device__ void zero() { a = 0.0; }
+    __device__ void add_part(const double *part, size_t i) { a += part[i]; }
+    __device__ void shfl_xor(int off) { a += __shfl_xor_sync(0xffffffffu, a, off); }
+    __device__ double value() const { return a; }
+};
+template <> struct SliceSum<float> {
+    float hi, lo;
+    __device__ void zero() { hi = lo = 0.f; }
+    // (hi, lo) += (x + y): two-sum of the leading parts, then renormalise
+    __device__ void add2(float x, float y) {
+        const float t = hi + x, bp = t - hi;
+        float e = (hi - (t - bp)) + (x - bp);
+        e += lo + y;
+        hi = t + e;
+        lo = e - (hi - t);
+    }
+    __device__ void add_part(const double *part, size_t i) {
+        const float2 p = reinterpret_cast<const float2 *>(part)[i];
+        add2(p.x, p.y);
+    }
+    __device__ void shfl_xor(int off) {
+        const float x = __shfl_xor_sync(0xffffffffu, hi, off), y = __shfl_xor_sync(0xffffffffu, lo, off);
+        add2(x, y);
+    }
+    __device__ double value() const { return (double)hi + (double)lo; }
+};
+template <typename real> __device__ __forceinline__ void store_part(double *part, size_t i, KahanAcc<real> &k);
+template <> __device__ __forceinline__ void store_part<double>(double *part, size_t i, KahanAcc<double> &k) {
+    part[i] = k.s;
+}
+template <> __device__ __forceinline__ void store_part<float>(double *part, size_t i, KahanAcc<float> &k) {
+    reinterpret_cast<float2 *>(part)[i] = make_float2(k.s, -k.c);
+}
 
 // velocities per stage slot: one mbarrier wait, one refill and one empty
 // arrival per slot; 16 KB slots at PA = 512 in both precisions
@@ -302,7 +344,7 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
 #pragma unroll
     for (int q = 0; q < NM; q++)
 #pragma unroll
-        for (int c = 0; c < MC; c++) M.part[((size_t)slice * NM + q) * ncell + cell0 + c] = ks[q][c].fold();
+        for (int c = 0; c < MC; c++) store_part<real>(M.part, ((size_t)slice * NM + q) * ncell + cell0 + c, ks[q][c]);
 }
 
 // lpc lanes per cell (a power of two <= 32): lane l of a cell's group adds
@@ -316,17 +358,20 @@ __global__ void k_moments_finish(MomArgs M, int lpc) {
     const int sub = (int)(tid % lpc);
     const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
     const bool ok = cell < ncell && a <= M.Na;
-    double s[10];
+    SliceSum<real> acc[10];
 #pragma unroll
-    for (int q = 0; q < 10; q++) s[q] = 0.0;
+    for (int q = 0; q < 10; q++) acc[q].zero();
     if (ok)
         for (int sl = sub; sl < M.vs; sl += lpc)
 #pragma unroll
-            for (int q = 0; q < 10; q++) s[q] += M.part[((size_t)sl * 10 + q) * ncell + cell];
+            for (int q = 0; q < 10; q++) acc[q].add_part(M.part, ((size_t)sl * 10 + q) * ncell + cell);
     for (int off = lpc >> 1; off > 0; off >>= 1)
 #pragma unroll
-        for (int q = 0; q < 10; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
+        for (int q = 0; q < 10; q++) acc[q].shfl_xor(off);
     if (!ok || sub != 0) return;
+    double s[10];
+#pragma unroll
+    for (int q = 0; q < 10; q++) s[q] = acc[q].value();
     // primitive conversion, GKUA_DETFP.f90:59-92
     double S1 = s[0], S4 = s[3], S5 = s[4], S6 = s[5], S7 = s[6];
     double ron = S1;
@@ -380,6 +425,7 @@ __device__ __forceinline__ double nanmax(double a, double b) {
     return b > a ? b : a;
 }
 
+template <typename real>
 __global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, double *__restrict__ part,
                                                          double *__restrict__ cellm) {
     const size_t ncell = (size_t)M.Nb * M.PA;
@@ -388,15 +434,20 @@ __global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, dou
     const int sub = (int)(tid % lpc);
     const int a = (int)(cell % M.PA) + 1;
     const bool ok = cell < ncell && a <= M.Na;
-    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    SliceSum<real> acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[q].zero();
     if (ok)
         for (int sl = sub; sl < M.vs; sl += lpc)
 #pragma unroll
-            for (int q = 0; q < 4; q++) s[q] += M.part[((size_t)sl * 4 + q) * ncell + cell];
+            for (int q = 0; q < 4; q++) acc[q].add_part(M.part, ((size_t)sl * 4 + q) * ncell + cell);
     for (int off = lpc >> 1; off > 0; off >>= 1)
 #pragma unroll
-        for (int q = 0; q < 4; q++) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
+        for (int q = 0; q < 4; q++) acc[q].shfl_xor(off);
     const bool own = ok && sub == 0;
+    double s[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) s[q] = acc[q].value();
     if (own && cellm)
 #pragma unroll
         for (int q = 0; q < 4; q++) cellm[(size_t)q * ncell + cell] = s[q];
@@ -520,12 +571,23 @@ int launch_wall(hyb_ctx *ctx) {
         face_role(ctx, face, &on_scan, &hi);
         int nfc = (face == 1 || face == 3) ? ctx->ncy : ctx->ncx;
         const double *wd = ctx->d_wall + (size_t)(face - 1) * 6 * 4096;
+        const size_t wall_smem = (size_t)((ctx->nv + WALL_CL - 1) / WALL_CL) * sizeof(double);
+        if (wall_smem > (size_t)200 * 1024) {
+            ctx->last_error = "wall: velocity grid too large for one cluster's shared memory";
+            return HYB_ERR_UNSUPPORTED;
+        }
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_wall<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_wall<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
         if (ctx->precision == HYB_PREC_FP64)
-            k_wall<double><<<nfc * WALL_CL, 256, 0, ctx->stream>>>((const double *)ctx->d_f, (double *)ctx->d_fw[face - 1], wd,
+            k_wall<double><<<nfc * WALL_CL, 256, wall_smem, ctx->stream>>>((const double *)ctx->d_f, (double *)ctx->d_fw[face - 1], wd,
                                                           ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
                                                           ctx->Nb, ctx->PA, on_scan, hi);
         else
-            k_wall<float><<<nfc * WALL_CL, 256, 0, ctx->stream>>>((const float *)ctx->d_f, (float *)ctx->d_fw[face - 1], wd,
+            k_wall<float><<<nfc * WALL_CL, 256, wall_smem, ctx->stream>>>((const float *)ctx->d_f, (float *)ctx->d_fw[face - 1], wd,
                                                          ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
                                                          ctx->Nb, ctx->PA, on_scan, hi);
         ctx->launches++;
@@ -650,7 +712,10 @@ static int residual_part(hyb_ctx *ctx, const void *rhs, double *cellm, int *nblk
     const int lpc = finish_lpc(ncell, M.vs);
     const unsigned nb = (unsigned)((ncell * lpc + 255) / 256);
     *nblk_out = (int)nb;
-    k_residual_finish<<<nb, 256, 0, ctx->stream>>>(M, lpc, ctx->d_resid + 16, cellm);
+    if (ctx->precision == HYB_PREC_FP64)
+        k_residual_finish<double><<<nb, 256, 0, ctx->stream>>>(M, lpc, ctx->d_resid + 16, cellm);
+    else
+        k_residual_finish<float><<<nb, 256, 0, ctx->stream>>>(M, lpc, ctx->d_resid + 16, cellm);
     ctx->launches++;
     return check_err(ctx, "k_residual_finish");
 }
