@@ -21,28 +21,44 @@
 namespace hyb {
 
 // ---------------------------------------------------------------------------
-// diffuse wall: one cluster of WALL_CL CTAs per wall face cell; each CTA
-// takes a contiguous share of the velocities, the n_w flux balance adds the
-// CTAs' partial sums in rank order through distributed shared memory
+// diffuse wall: one cluster of WALL_CL CTAs per wall face cell, all wall
+// faces in one launch; each CTA takes a contiguous share of the velocities,
+// the n_w flux balance adds the CTAs' partial sums in rank order through
+// distributed shared memory
 // ---------------------------------------------------------------------------
 constexpr int WALL_CL = 8;
 
-struct WallFace {
-    // position of the face cells in the (a,b) layout
-    int on_scan;      // 1: wall at a scan-axis end (cells along b), 0: march end
-    int hi;           // 1: high end
-    int nfc;          // face cells
+// the wall faces of one launch: face cells of face q are the global face
+// cells first[q] .. first[q+1]-1; on_scan: wall at a scan-axis end (cells
+// along b), else at a march end; hi: the high end
+template <typename real> struct WallSet {
+    real *fw[4];
+    const double *wd[4];
+    int on_scan[4], hi[4], first[5], nface;
 };
 
 template <typename real>
 __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
-    k_wall(const real *__restrict__ f, real *__restrict__ fw, const double *__restrict__ wd,
-           const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ w, int nvi,
-           int nv, int Na, int Nb, int PA, int on_scan, int hi) {
+    k_wall(const real *__restrict__ f, WallSet<real> W, const double *__restrict__ vx,
+           const double *__restrict__ vy, const double *__restrict__ w, int nvi, int nv, int Na, int Nb, int PA) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
-    const int k = blockIdx.x / WALL_CL;   // face cell (0-based, face order)
+    const int kg = blockIdx.x / WALL_CL;  // global face cell
+    // the face of kg (constant indices: the set stays in parameter space)
+    real *fw = W.fw[0];
+    const double *wd = W.wd[0];
+    int on_scan = W.on_scan[0], hi = W.hi[0], k0 = W.first[0];
+#pragma unroll
+    for (int u = 1; u < 4; u++)
+        if (u < W.nface && kg >= W.first[u]) {
+            fw = W.fw[u];
+            wd = W.wd[u];
+            on_scan = W.on_scan[u];
+            hi = W.hi[u];
+            k0 = W.first[u];
+        }
+    const int k = kg - k0;                // face cell (0-based, face order)
     const int per = (nv + WALL_CL - 1) / WALL_CL, vb = rank * per, ve = min(nv, vb + per);
     // wall data: [k][6] = u, v, t, swnx, swny, step
     const double uw = wd[k * 6 + 0], vw = wd[k * 6 + 1], tw = wd[k * 6 + 2];
@@ -564,37 +580,51 @@ static void face_role(const hyb_ctx *ctx, int face, int *on_scan, int *hi) {
     *hi = (face == 3 || face == 4);
 }
 
+template <typename real>
+static void launch_wall_real(hyb_ctx *ctx, const WallSet<real> &W, size_t smem) {
+    k_wall<real><<<W.first[W.nface] * WALL_CL, 256, smem, ctx->stream>>>((const real *)ctx->d_f, W, ctx->d_vx,
+                                                                          ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv,
+                                                                          ctx->Na, ctx->Nb, ctx->PA);
+}
+
+// every wall face of the context in one launch
 int launch_wall(hyb_ctx *ctx) {
+    WallSet<double> Wd;
+    WallSet<float> Wf;
+    int nf = 0, first = 0;
     for (int face = 1; face <= 4; face++) {
         if (ctx->bc[face - 1] != HYB_BC_WALL) continue;
         int on_scan, hi;
         face_role(ctx, face, &on_scan, &hi);
-        int nfc = (face == 1 || face == 3) ? ctx->ncy : ctx->ncx;
+        const int nfc = (face == 1 || face == 3) ? ctx->ncy : ctx->ncx;
         const double *wd = ctx->d_wall + (size_t)(face - 1) * 6 * 4096;
-        const size_t wall_smem = (size_t)((ctx->nv + WALL_CL - 1) / WALL_CL) * sizeof(double);
-        if (wall_smem > (size_t)200 * 1024) {
-            ctx->last_error = "wall: velocity grid too large for one cluster's shared memory";
-            return HYB_ERR_UNSUPPORTED;
-        }
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_wall<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            cudaFuncSetAttribute(k_wall<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            attr = true;
-        }
-        if (ctx->precision == HYB_PREC_FP64)
-            k_wall<double><<<nfc * WALL_CL, 256, wall_smem, ctx->stream>>>((const double *)ctx->d_f, (double *)ctx->d_fw[face - 1], wd,
-                                                          ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
-                                                          ctx->Nb, ctx->PA, on_scan, hi);
-        else
-            k_wall<float><<<nfc * WALL_CL, 256, wall_smem, ctx->stream>>>((const float *)ctx->d_f, (float *)ctx->d_fw[face - 1], wd,
-                                                         ctx->d_vx, ctx->d_vy, ctx->d_w, ctx->nvi, ctx->nv, ctx->Na,
-                                                         ctx->Nb, ctx->PA, on_scan, hi);
-        ctx->launches++;
-        int rc = check_err(ctx, "k_wall");
-        if (rc) return rc;
+        Wd.fw[nf] = (double *)ctx->d_fw[face - 1];
+        Wf.fw[nf] = (float *)ctx->d_fw[face - 1];
+        Wd.wd[nf] = Wf.wd[nf] = wd;
+        Wd.on_scan[nf] = Wf.on_scan[nf] = on_scan;
+        Wd.hi[nf] = Wf.hi[nf] = hi;
+        Wd.first[nf] = Wf.first[nf] = first;
+        first += nfc;
+        nf++;
     }
-    return HYB_OK;
+    if (nf == 0) return HYB_OK;
+    Wd.first[nf] = Wf.first[nf] = first;
+    Wd.nface = Wf.nface = nf;
+    const size_t wall_smem = (size_t)((ctx->nv + WALL_CL - 1) / WALL_CL) * sizeof(double);
+    if (wall_smem > (size_t)200 * 1024) {
+        ctx->last_error = "wall: velocity grid too large for one cluster's shared memory";
+        return HYB_ERR_UNSUPPORTED;
+    }
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_wall<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_wall<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    if (ctx->precision == HYB_PREC_FP64) launch_wall_real<double>(ctx, Wd, wall_smem);
+    else launch_wall_real<float>(ctx, Wf, wall_smem);
+    ctx->launches++;
+    return check_err(ctx, "k_wall");
 }
 
 int moments_slices(const hyb_ctx *ctx) {

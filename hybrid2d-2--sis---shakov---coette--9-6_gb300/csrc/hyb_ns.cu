@@ -1,6 +1,6 @@
 // hyb_ns.cu -- FP64 macroscopic kernels around the kinetic step.
 //
-//   k_sghost_*     S ghost cells: DETFPwall (GKUA_DETFP_WALL.f90:34-95) on wall
+//   k_sghost       S ghost cells: DETFPwall (GKUA_DETFP_WALL.f90:34-95) on wall
 //                  faces, the inner-block exchange (GKUA_boundary.f90:514-633)
 //                  on periodic faces
 //   k_cns_*        Convert_NS (Hybrid_Sub.f90:191-461): NS state from the
@@ -26,9 +26,8 @@ struct NsGeom {
 __device__ __forceinline__ size_t C2(const NsGeom &G, int i, int j) { return hyb_c2(G.nx, i, j); }
 
 // ---- S ghosts: walls (DETFPwall), components 1..10 ---------------------------
-__global__ void k_sghost_wall(double *S, NsGeom G) {
+__device__ __forceinline__ void sghost_wall(double *S, const NsGeom &G, int idx) {
     const int nx = G.nx, ny = G.ny;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     // faces 2/4: i = 1..nx-1; faces 1/3: j = 1..ny-1
     int nfx = nx - 1, nfy = ny - 1;
     int face, k;
@@ -51,9 +50,8 @@ __global__ void k_sghost_wall(double *S, NsGeom G) {
 }
 
 // ---- S ghosts: periodic faces, components 1..10, LAP layers -----------------
-__global__ void k_sghost_periodic(double *S, NsGeom G) {
+__device__ __forceinline__ void sghost_periodic(double *S, const NsGeom &G, int idx) {
     const int nx = G.nx, ny = G.ny;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     int n1 = G.perx ? (ny - 1) : 0, n2 = G.pery ? (nx - 1) : 0;
     if (idx < n1) {
         int j = idx + 1;
@@ -74,6 +72,15 @@ __global__ void k_sghost_periodic(double *S, NsGeom G) {
             }
         }
     }
+}
+
+// both ghost kinds in one launch: the wall ghosts (rows / columns 0 and n
+// along the wall) and the periodic layers (interior rows / columns copied
+// across) write disjoint cells and read interior cells only
+__global__ void k_sghost(double *S, NsGeom G, int nwall) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < nwall) sghost_wall(S, G, idx);
+    else sghost_periodic(S, G, idx - nwall);
 }
 
 // ---- Convert_NS ------------------------------------------------------------
@@ -305,13 +312,11 @@ static int check(hyb_ctx *ctx, const char *what) {
 
 int launch_sghost(hyb_ctx *ctx) {
     NsGeom G = make_geom(ctx);
-    int n = 2 * (ctx->nx - 1) + 2 * (ctx->ny - 1);
-    k_sghost_wall<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_S, G);
+    const int nwall = 2 * (ctx->nx - 1) + 2 * (ctx->ny - 1);
+    const int nper = (G.perx ? ctx->ny - 1 : 0) + (G.pery ? ctx->nx - 1 : 0);
+    const int n = nwall + nper;
+    k_sghost<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_S, G, nwall);
     ctx->launches++;
-    if (G.perx || G.pery) {
-        k_sghost_periodic<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_S, G);
-        ctx->launches++;
-    }
     return check(ctx, "k_sghost");
 }
 
