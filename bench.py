@@ -14,6 +14,7 @@ sharded across GPUs); value is the sum over ranks.
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -128,6 +129,31 @@ def cpu_sample(case, seconds=10.0, max_seconds=30.0, threads=0):
             break
     val = c.cells * c.nv * n / el
     return val, nthreads, f"{c.ncx}x{c.ncy} cells x 16x16 velocities, {n} FP64 oracle iterations, {el:.1f}s"
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
+def cpu_channel_iteration_s(seconds=3.0):
+    """Oracle seconds per plain FP64 iteration of the Kn 0.1 channel (4x64
+    cells, 32x32 velocities) on all host cores."""
+    from oracle import oracle as O
+    o = O.Oracle(cases.couette_small(dt=0.01), threads=os.cpu_count() or 1)
+    o.init_maxwellian()
+    o.step(1)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        o.step(10)
+        n += 10
+    return (time.perf_counter() - t0) / n
 
 
 # ---------------------------------------------------------------------------
@@ -345,7 +371,18 @@ def run_gb300(args, world, rank, local):
         line["time_to_residual"] = time_to_residual()
     if not args.no_cpu:
         cv, cores, sample = cpu_sample(case, seconds=args.cpu_seconds)
-        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cv1, _, sample1 = cpu_sample(case, seconds=args.cpu_seconds / 2, threads=1)
+        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                                "value_1_thread": cv1, "sample_1_thread": sample1,
+                                "nproc": os.cpu_count(), "cpu_model": cpu_model()}
+        # the channel to 1e-8 on the host: oracle time per iteration times
+        # the plain iteration count measured on the GPU (FP64 parity makes
+        # the two runs take the same iterations)
+        it_s = cpu_channel_iteration_s()
+        ttr = line.get("time_to_residual", {}).get("runs", {}).get("plain_fp64")
+        line["cpu_baseline"]["channel_plain_fp64_s_per_iteration"] = it_s
+        if ttr and ttr.get("reached"):
+            line["cpu_baseline"]["channel_plain_fp64_to_1e-8_s_extrapolated"] = it_s * ttr["iterations"]
     print(json.dumps(line), flush=True)
     return 0
 
