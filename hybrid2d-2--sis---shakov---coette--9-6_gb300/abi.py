@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libhyb_gb300.so")
 EXPORTS = [
     "hyb_create", "hyb_destroy", "hyb_last_error", "hyb_version",
     "hyb_init_maxwellian", "hyb_upload_f", "hyb_download_f", "hyb_download_moments",
-    "hyb_download_hot", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
+    "hyb_download_hot", "hyb_download_hoq", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
     "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
     "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
     "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc", "hyb_autotune",
@@ -61,6 +61,7 @@ def load(path=None):
     L.hyb_download_f.argtypes = [vp, dp]
     L.hyb_download_moments.argtypes = [vp, dp, dp]
     L.hyb_download_hot.argtypes = [vp, dp, dp, dp, dp]
+    L.hyb_download_hoq.argtypes = [vp, dp, dp]
     L.hyb_step.argtypes = [vp, ip, vp]
     for fn in ("hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp", "hyb_convert_ns"):
         getattr(L, fn).argtypes = [vp]
@@ -252,6 +253,13 @@ class Solver:
         ti, qi, tj, qj = np.zeros(4 * nc), np.zeros(2 * nc), np.zeros(4 * nc), np.zeros(2 * nc)
         self._ck(self.L.hyb_download_hot(self.h, _dp(ti), _dp(qi), _dp(tj), _dp(qj)), "download_hot")
         return ti, qi, tj, qj
+
+    def hoq(self):
+        """HOT_GKUA(6, -3:nx+3, -3:ny+3) and HOQ_GKUA(4, ...) of the current f
+        (flat, column-major; interior cells)."""
+        hot, hoq = np.zeros(6 * self.P), np.zeros(4 * self.P)
+        self._ck(self.L.hyb_download_hoq(self.h, _dp(hot), _dp(hoq)), "download_hoq")
+        return hot, hoq
 
     def launches(self):
         n = C.c_longlong()

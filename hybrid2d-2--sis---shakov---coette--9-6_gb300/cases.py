@@ -63,6 +63,47 @@ def grid_gl(dv, n, vdown, kgln, single_literals=True):
     return np.array(v), np.array(w)
 
 
+def half_range_hermite(n, m=600, vcut=12.0):
+    """Nodes and weights of the n-point Gauss rule for integral_0^inf
+    exp(-v^2) g(v) dv (the reference's "modified (half-range)
+    Gauss-Hermite" rule, GKUA_lisansudu.f90:364-440, which tabulates n = 7, 8
+    and 16).  Computed here from the weight function: the recurrence
+    coefficients of its orthogonal polynomials by the discretised Stieltjes
+    procedure on an m-point Gauss-Legendre discretisation of [0, vcut]
+    (exp(-vcut^2) is below double precision), then the Golub-Welsch
+    eigenvalue problem of the Jacobi matrix."""
+    x, h = np.polynomial.legendre.leggauss(m)
+    x = 0.5 * vcut * (x + 1.0)
+    w = 0.5 * vcut * h * np.exp(-x * x)
+    alpha, beta = np.zeros(n), np.zeros(n)
+    p_prev, p = np.zeros(m), np.ones(m)
+    norm_prev = 1.0
+    for k in range(n):
+        norm = np.sum(w * p * p)
+        alpha[k] = np.sum(w * x * p * p) / norm
+        beta[k] = norm if k == 0 else norm / norm_prev
+        p_prev, p = p, (x - alpha[k]) * p - (beta[k] if k > 0 else 0.0) * p_prev
+        norm_prev = norm
+    J = np.diag(alpha) + np.diag(np.sqrt(beta[1:]), 1) + np.diag(np.sqrt(beta[1:]), -1)
+    nodes, vec = np.linalg.eigh(J)
+    weights = beta[0] * vec[0, :] ** 2
+    return nodes, weights
+
+
+def grid_gh(n2):
+    """Gauss-Hermite velocity grid of n2 = 2n nodes (lisanv with
+    Quadrature_Mode = GKUA_GH, GKUA_lisansudu.f90:102-115): the half-range
+    nodes mirrored to negative velocities.  The returned weights are the
+    ones the moments use, H exp(v^2) (IntegralGaussHermite,
+    GKUA_DETFP.f90:174-201)."""
+    if n2 % 2:
+        raise ValueError("a Gauss-Hermite grid has an even node count")
+    a, h = half_range_hermite(n2 // 2)
+    v = np.concatenate([-a[::-1], a])
+    w = np.concatenate([h[::-1], h]) * np.exp(v * v)
+    return v, w
+
+
 @dataclass
 class Case:
     """One planar-Couette problem: everything hyb_create needs."""
@@ -86,6 +127,7 @@ class Case:
     pr: float = 2.0 / 3.0
     gamma: float = 5.0 / 3.0
     nc_rule: int = 1         # the reference NewtonCotes pattern (GKUA_DETFP.f90:419-444)
+    quadrature: str = "nc"   # "nc": Newton-Cotes on [-vmax, vmax]; "gh": Gauss-Hermite (vmax unused)
     stretch: float = 0.0     # >0: tanh clustering of the y nodes towards both plates
     extra: dict = field(default_factory=dict)
 
@@ -132,6 +174,10 @@ class Case:
         return u, v, t
 
     def vgrid(self):
+        if self.quadrature == "gh":
+            vi, wi = grid_gh(self.nvx)
+            vj, wj = grid_gh(self.nvy)
+            return vi, wi, vj, wj
         vi, wi = grid_nc(self.nvx, -self.vmax, self.vmax, self.nc_rule)
         vj, wj = grid_nc(self.nvy, -self.vmax, self.vmax, self.nc_rule)
         return vi, wi, vj, wj

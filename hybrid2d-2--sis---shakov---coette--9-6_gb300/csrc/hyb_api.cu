@@ -696,6 +696,39 @@ int hyb_download_moments(hyb_ctx *ctx, double *s_gkua, double *cf) {
     return HYB_OK;
 }
 
+int hyb_download_hoq(hyb_ctx *ctx, double *hot, double *hoq) {
+    if (!ctx || (!hot && !hoq)) return HYB_ERR_INVALID;
+    cudaSetDevice(ctx->dev);
+    const int nx = ctx->nx, ny = ctx->ny, pw = nx + 7;
+    const size_t nc2 = (size_t)(nx + 3) * (ny + 3), P = (size_t)(nx + 7) * (ny + 7);
+    double *d = nullptr;
+    if (cudaMalloc((void **)&d, 9 * nc2 * sizeof(double)) != cudaSuccess) {
+        ctx->last_error = "download_hoq: device allocation failed";
+        return HYB_ERR_NOMEM;
+    }
+    std::vector<double> H(9 * nc2);
+    int rc = HYB_OK;
+    if (cudaMemsetAsync(d, 0, 9 * nc2 * sizeof(double), ctx->stream) != cudaSuccess) rc = HYB_ERR_CUDA;
+    if (!rc) rc = hyb::launch_hoq(ctx, d);
+    if (!rc && cudaMemcpyAsync(H.data(), d, H.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) !=
+                   cudaSuccess)
+        rc = HYB_ERR_CUDA;
+    if (!rc && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = HYB_ERR_CUDA;
+    cudaFree(d);
+    if (rc) return rc;
+    if (hot) std::fill(hot, hot + 6 * P, 0.0);
+    if (hoq) std::fill(hoq, hoq + 4 * P, 0.0);
+    for (int j = -1; j <= ny + 1; j++)
+        for (int i = -1; i <= nx + 1; i++) {
+            const size_t c2 = hyb_c2(nx, i, j), ix = (size_t)(i + 3) + (size_t)pw * (j + 3);
+            if (hot)
+                for (int k = 0; k < 6; k++) hot[ix * 6 + k] = H[(size_t)k * nc2 + c2];
+            if (hoq)
+                for (int k = 0; k < 3; k++) hoq[ix * 4 + k] = H[(size_t)(6 + k) * nc2 + c2];
+        }
+    return HYB_OK;
+}
+
 int hyb_download_hot(hyb_ctx *ctx, double *tao_i, double *q_i, double *tao_j, double *q_j) {
     if (!ctx) return HYB_ERR_INVALID;
     cudaSetDevice(ctx->dev);

@@ -147,6 +147,7 @@ int launch_sghost(hyb_ctx *ctx);
 int launch_residual(hyb_ctx *ctx, hyb_residual *out);
 int launch_rhs_moments(hyb_ctx *ctx, double *cellm);
 int residual_blocks(const hyb_ctx *ctx);   // blocks of the residual partials
+int launch_hoq(hyb_ctx *ctx, double *out);   // HOT_GKUA(1:6), HOQ_GKUA(1:3), [9][(nx+3)(ny+3)]
 int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);
 int launch_convert_ns(hyb_ctx *ctx);
 int ns_create(hyb_ctx *ctx);

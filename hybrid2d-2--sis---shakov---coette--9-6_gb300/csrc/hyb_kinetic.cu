@@ -236,7 +236,8 @@ __host__ __device__ inline size_t mom_smem_bytes(int PA, int nloc_max) {
 }
 
 // NM = 10: the DETFP moments; NM = 4: moments 1-4 only (the residual of a
-// stored RHS, DETFP_res)
+// stored RHS, DETFP_res); NM = 9: the higher-order moments HOT_GKUA(1:6),
+// HOQ_GKUA(1:3) of IntegralGaussHermite (GKUA_DETFP.f90:217-229)
 template <typename real, int MC, int NM>
 __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -318,21 +319,39 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
 #pragma unroll
                     for (int c = 0; c < MC; c++) { gg[c] = g[c]; hh[c] = g[PA + c]; }
                     const real wx = wv * vx, wy = wv * vy, wxy = wx * vy, c2 = vx * vx + vy * vy;
+                    if constexpr (NM == 9) {
+                        const real t1 = wx * vx, t2 = wy * vy;   // w vx^2, w vy^2
+                        const real t1x = t1 * vx, t1y = t1 * vy, t2x = t2 * vx, t2y = t2 * vy;
 #pragma unroll
-                    for (int c = 0; c < MC; c++) {
-                        const real wg = wv * gg[c];
-                        const real b4 = hh[c] + c2 * gg[c];
-                        blk[0][c] += wg;
-                        blk[1][c] += wx * gg[c];
-                        blk[2][c] += wy * gg[c];
-                        blk[3][c] += wv * b4;
-                        if constexpr (NM > 4) {
-                            blk[4][c] += wx * (vx * gg[c]);
-                            blk[5][c] += wy * (vy * gg[c]);
-                            blk[6][c] += wxy * gg[c];
-                            blk[7][c] += wx * b4;
-                            blk[8][c] += wy * b4;
-                            blk[9][c] += wv * hh[c];
+                        for (int c = 0; c < MC; c++) {
+                            const real e = gg[c] * c2 + hh[c];     // G c^2 + H
+                            blk[0][c] += t1x * gg[c];
+                            blk[1][c] += t1y * gg[c];
+                            blk[2][c] += t2x * gg[c];
+                            blk[3][c] += t2y * gg[c];
+                            blk[4][c] += wx * hh[c];
+                            blk[5][c] += wy * hh[c];
+                            blk[6][c] += t1 * e;
+                            blk[7][c] += wxy * e;
+                            blk[8][c] += t2 * e;
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < MC; c++) {
+                            const real wg = wv * gg[c];
+                            const real b4 = hh[c] + c2 * gg[c];
+                            blk[0][c] += wg;
+                            blk[1][c] += wx * gg[c];
+                            blk[2][c] += wy * gg[c];
+                            blk[3][c] += wv * b4;
+                            if constexpr (NM > 4) {
+                                blk[4][c] += wx * (vx * gg[c]);
+                                blk[5][c] += wy * (vy * gg[c]);
+                                blk[6][c] += wxy * gg[c];
+                                blk[7][c] += wx * b4;
+                                blk[8][c] += wy * b4;
+                                blk[9][c] += wv * hh[c];
+                            }
                         }
                     }
                 }
@@ -427,6 +446,34 @@ __global__ void k_moments_finish(MomArgs M, int lpc) {
     ep[5 * ncell + cell] = (real)(cpt * qx);
     ep[6 * ncell + cell] = (real)(cpt * qy);
     ep[7 * ncell + cell] = (real)cf;
+}
+
+// higher-order moments per cell: slice sums as in k_moments_finish, written
+// to out[q][(nx+3)(ny+3)] (q = HOT 1..6, HOQ 1..3) at the interior cells
+template <typename real>
+__global__ void k_hoq_finish(MomArgs M, int lpc, double *__restrict__ out) {
+    const size_t ncell = (size_t)M.Nb * M.PA;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t cell = tid / lpc;
+    const int sub = (int)(tid % lpc);
+    const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
+    const bool ok = cell < ncell && a <= M.Na;
+    SliceSum<real> acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q].zero();
+    if (ok)
+        for (int sl = sub; sl < M.vs; sl += lpc)
+#pragma unroll
+            for (int q = 0; q < 9; q++) acc[q].add_part(M.part, ((size_t)sl * 9 + q) * ncell + cell);
+    for (int off = lpc >> 1; off > 0; off >>= 1)
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q].shfl_xor(off);
+    if (!ok || sub != 0) return;
+    const int i = M.scan_is_j ? b : a, j = M.scan_is_j ? a : b;
+    const size_t c2 = hyb_c2(M.nx, i, j);
+    const size_t plane = (size_t)(M.nx + 3) * (size_t)(M.ny + 3);
+#pragma unroll
+    for (int q = 0; q < 9; q++) out[(size_t)q * plane + c2] = acc[q].value();
 }
 
 // ---------------------------------------------------------------------------
@@ -754,6 +801,23 @@ static int residual_part(hyb_ctx *ctx, const void *rhs, double *cellm, int *nblk
 int launch_rhs_moments(hyb_ctx *ctx, double *cellm) {
     int nblk;
     return residual_part(ctx, ctx->d_rhs_gsis, cellm, &nblk);
+}
+
+// higher-order moments of the current f at the interior cells,
+// out[9][(nx+3)(ny+3)] (zero-filled by the caller)
+int launch_hoq(hyb_ctx *ctx, double *out) {
+    size_t smem;
+    int mc;
+    MomArgs M = mom_args(ctx, ctx->d_f, &smem, &mc);
+    int rc = launch_mom_pass<9>(ctx, M, mc, smem);
+    if (rc) return rc;
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    const int lpc = finish_lpc(ncell, M.vs);
+    const unsigned nb = (unsigned)((ncell * lpc + 255) / 256);
+    if (ctx->precision == HYB_PREC_FP64) k_hoq_finish<double><<<nb, 256, 0, ctx->stream>>>(M, lpc, out);
+    else k_hoq_finish<float><<<nb, 256, 0, ctx->stream>>>(M, lpc, out);
+    ctx->launches++;
+    return check_err(ctx, "k_hoq_finish");
 }
 
 int launch_residual(hyb_ctx *ctx, hyb_residual *out) {

@@ -93,6 +93,11 @@ module hyb_dvm
        type(c_ptr), value :: ctx
        real(c_double), intent(inout) :: tao_i(*), q_i(*), tao_j(*), q_j(*)
      end function
+     integer(c_int) function hyb_download_hoq(ctx, hot, hoq) bind(c, name="hyb_download_hoq")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: hot(*), hoq(*)
+     end function
      integer(c_int) function hyb_step(ctx, n_iter, res) bind(c, name="hyb_step")
        import :: c_int, c_ptr, hyb_residual
        type(c_ptr), value :: ctx

@@ -184,6 +184,14 @@ int hyb_download_moments(hyb_ctx *ctx, double *s_gkua, double *cf);
  * Any pointer may be NULL. */
 int hyb_download_hot(hyb_ctx *ctx, double *tao_i, double *q_i,
                      double *tao_j, double *q_j);
+/* Higher-order velocity moments of the current f (IntegralGaussHermite,
+ * GKUA_DETFP.f90:174-229; written by output, IO.f90:442-445), for any
+ * velocity grid: HOT_GKUA(6,-3:nx+3,-3:ny+3) = sums of w G vx^3, G vx^2 vy,
+ * G vx vy^2, G vy^3, H vx, H vy; HOQ_GKUA(4,-3:nx+3,-3:ny+3) = sums of
+ * w (G c^2 + H) vx^2, vx vy, vy^2 and a zero fourth component.  Interior
+ * cells only (ghost cells are zero).  Either pointer may be NULL; allocates
+ * a temporary device buffer. */
+int hyb_download_hoq(hyb_ctx *ctx, double *hot, double *hoq);
 
 /* ---- the iteration (Hybrid_Time_advance_LU_SGS, Hybrid_Sub.f90:4-160) --- */
 /* n_iter outer iterations; each runs the boundary conditions, the kinetic

@@ -828,6 +828,47 @@ int orc_detfp(orc *o)
     return HYB_OK;
 }
 
+/* ---- higher-order moments of IntegralGaussHermite (GKUA_DETFP.f90:174-229)
+ * HOT_GKUA(1:6), HOQ_GKUA(1:3) of the current FRD, summed with the grid's
+ * full weights (the reference's GH weights are w exp(v^2), which is what a
+ * Gauss-Hermite grid passes in).  Interior cells 1..nx-1 x 1..ny-1; hot is
+ * (6,-3:nx+3,-3:ny+3) and hoq (4,...), column-major, zero elsewhere. */
+int orc_hoq(orc *o, double *hot, double *hoq)
+{
+    const int nx = o->nx, ny = o->ny, pw = nx + 7;
+    const size_t P = (size_t)(nx + 7) * (ny + 7);
+    memset(hot, 0, 6 * P * sizeof(double));
+    memset(hoq, 0, 4 * P * sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+            double t[6] = {0}, q[3] = {0};
+            for (int jv = 0; jv < o->nvj; jv++) {
+                double vy = o->vj[jv];
+                for (int iv = 0; iv < o->nvi; iv++) {
+                    double vx = o->vi[iv];
+                    int v = iv + o->nvi * jv;
+                    double w = o->wi[iv] * o->wj[jv];
+                    double wg = w * FRD(o, 0, i, j, v), wh = w * FRD(o, 1, i, j, v);
+                    double e = wg * (vx * vx + vy * vy) + wh;
+                    t[0] += wg * vx * vx * vx;
+                    t[1] += wg * vx * vx * vy;
+                    t[2] += wg * vx * vy * vy;
+                    t[3] += wg * vy * vy * vy;
+                    t[4] += wh * vx;
+                    t[5] += wh * vy;
+                    q[0] += e * vx * vx;
+                    q[1] += e * vx * vy;
+                    q[2] += e * vy * vy;
+                }
+            }
+            size_t ix = (size_t)(i + 3) + (size_t)pw * (j + 3);
+            for (int k = 0; k < 6; k++) hot[ix * 6 + k] = t[k];
+            for (int k = 0; k < 3; k++) hoq[ix * 4 + k] = q[k];
+        }
+    return HYB_OK;
+}
+
 /* ---- DETFP_res + GaussLegendre_rs (GKUA_DETFP_RES.f90:4-136) ------------ */
 int orc_detfp_res(orc *o, hyb_residual *r)
 {
@@ -1212,12 +1253,6 @@ int orc_grid_gl(double dv, int n, double vdown, int kgln, int single_literals, d
         }
     }
     return m;
-}
-
-int orc_grid_gh(int nh, int single_literals, double *v, double *w)
-{
-    (void)nh; (void)single_literals; (void)v; (void)w;
-    return -1;   /* half-range Gauss-Hermite tables: not built (see DESIGN) */
 }
 
 int orc_grid_nc(int n, double vdown, double vup, int rule, double *v, double *w)

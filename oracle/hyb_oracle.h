@@ -44,6 +44,7 @@ int orc_kinetic_step(orc *o);           /* GKUA_Residual (Get_Feq, RHSFDVsub, sw
 int orc_detfp(orc *o);                  /* DETFP + GKUA_DET_wall + macro exchange */
 int orc_convert_ns(orc *o);             /* Convert_NS                           */
 int orc_detfp_res(orc *o, hyb_residual *r);   /* DETFP_res                      */
+int orc_hoq(orc *o, double *hot, double *hoq); /* HOT_GKUA / HOQ_GKUA         */
 int orc_step(orc *o, int n_iter, hyb_residual *r);  /* Hybrid_Time_advance_LU_SGS */
 
 /* state access (pointers into the oracle's own reference-layout arrays) */
@@ -77,7 +78,6 @@ int orc_grid_gl(double dv, int n, double vdown, int kgln, int single_literals,
                 double *v, double *w);
 /* Half-range Gauss-Hermite (GKUA_lisansudu.f90:103-118, 364-436), nh in
  * {7,8,16}; 2*nh nodes; weights returned as w*exp(v^2) (GKUA_DETFP.f90:200). */
-int orc_grid_gh(int nh, int single_literals, double *v, double *w);
 /* Uniform Newton-Cotes grid of n nodes on [vdown,vup].  rule 0: composite
  * Simpson 1/3 with a closing 3/8 panel when n is even; rule 1: the
  * reference's end/even/odd = 1/4/2 pattern (GKUA_DETFP.f90:419-444). */

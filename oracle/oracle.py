@@ -41,6 +41,7 @@ def lib():
             getattr(L, fn).restype = dp
         L.orc_upload_f.argtypes = [vp, dp]
         L.orc_hot.argtypes = [vp, dp, dp, dp, dp]
+        L.orc_hoq.argtypes = [vp, dp, dp]
         L.orc_nsf_in.argtypes = [vp, dp, dp, dp, dp]
         L.orc_err.argtypes = [vp]
         L.orc_err.restype = C.c_double
@@ -148,6 +149,12 @@ class Oracle:
         ti, qi, tj, qj = np.zeros(4 * nc), np.zeros(2 * nc), np.zeros(4 * nc), np.zeros(2 * nc)
         self.L.orc_hot(self.h, _dp(ti), _dp(qi), _dp(tj), _dp(qj))
         return ti, qi, tj, qj
+
+    def hoq(self):
+        """HOT_GKUA(6, -3:nx+3, -3:ny+3), HOQ_GKUA(4, ...) of the current FRD."""
+        hot, hoq = np.zeros(6 * self.P), np.zeros(4 * self.P)
+        self.L.orc_hoq(self.h, _dp(hot), _dp(hoq))
+        return hot, hoq
 
     def gsis(self, **kw):
         T = _types()

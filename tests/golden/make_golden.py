@@ -11,9 +11,17 @@ flow2d_gkua_step0.json
     :22-53) for the inputs in Hybrid2D/input/control.in and
     Quadrature_Para.dat.  The file is uniform; one row plus the inputs that
     produced it are stored.
+
+gauss_hermite_half_range.json
+    The node / weight table of the reference's "modified (half-range)
+    Gauss-Hermite" velocity grid (GaussHermite in
+    Hybrid2D/src/GKUA_lisansudu.f90:364-440): nodes a_k and weights H_k of
+    the quadrature of integral_0^inf exp(-v^2) g(v) dv for 7, 8 and 16 nodes,
+    as printed in that routine.
 """
 import json
 import os
+import re
 import sys
 
 ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
@@ -46,3 +54,29 @@ out = {
 with open(os.path.join(here, "flow2d_gkua_step0.json"), "w") as fh:
     json.dump(out, fh, indent=1)
 print("wrote", os.path.join(here, "flow2d_gkua_step0.json"))
+
+
+# ---- half-range Gauss-Hermite table -------------------------------------------
+src = os.path.join(ref, "Hybrid2D", "src", "GKUA_lisansudu.f90")
+with open(src, errors="replace") as fh:
+    text = fh.read()
+body = text[text.index("SUBROUTINE GaussHermite(AGH,HGH,NV)"):]
+body = body[:body.index("END IF")]
+tables, cur = {}, None
+for line in body.splitlines():
+    m = re.search(r"NV\.EQ\.(\d+)", line)
+    if m:
+        cur = int(m.group(1))
+        tables[cur] = {"a": {}, "h": {}}
+        continue
+    m = re.match(r"\s*(AGH|HGH)\((\d+)\)\s*=\s*([-+0-9.EeDd]+)", line)
+    if m and cur is not None:
+        key = "a" if m.group(1) == "AGH" else "h"
+        tables[cur][key][int(m.group(2))] = float(m.group(3).replace("D", "E").replace("d", "e"))
+out = {"source": "Hybrid2D/src/GKUA_lisansudu.f90, SUBROUTINE GaussHermite",
+       "weight": "exp(-v^2) on [0, inf)",
+       "tables": {str(n): {"nodes": [t["a"][k] for k in range(1, n + 1)],
+                           "weights": [t["h"][k] for k in range(1, n + 1)]} for n, t in sorted(tables.items())}}
+with open(os.path.join(here, "gauss_hermite_half_range.json"), "w") as fh:
+    json.dump(out, fh, indent=1)
+print("wrote", os.path.join(here, "gauss_hermite_half_range.json"))
