@@ -3,12 +3,23 @@
 // A batch owns one context per instance (each with its own stream and
 // buffers, so instances of different mesh and velocity-grid sizes coexist).
 // One outer iteration of every instance -- wall, sweep, moments, S ghosts
-// (and Convert_NS on the last iteration of a step) -- is captured once into a single
-// CUDA graph whose per-instance chains are independent branches, so one
-// graph launch advances all instances by one iteration and the GPU runs the
-// small per-instance kernels side by side.  Two graphs are kept: one for
-// plain iterations and one whose sweeps also store the RHS (used on the last
-// iteration when residuals are requested).
+// (and Convert_NS on the last iteration of a step) -- is captured once into a
+// CUDA graph, so one graph launch advances all instances by one iteration.
+// Two graphs are kept: one for plain iterations and one whose sweeps also
+// store the RHS (the last iteration of a step).
+//
+// Plain iterations run as batched launches: the instances are grouped by
+// launch shape (scan-axis padding, layout chunk, sweep cells per thread and
+// velocity groups per CTA, uniform spacing), and each group issues five
+// kernels -- walls, sweeps, moment partials, moment finish, S ghosts -- whose
+// CTAs each read their instance's argument record from a device table and
+// take one (instance, block) pair from a work table.  The groups are the
+// graph's branches; a last kernel gathers the error words.  The kernels are
+// the per-context kernels' bodies, so every instance computes bit for bit
+// what a standalone context computes.  The last iteration of a step (RHS
+// store, residual, Convert_NS) keeps one branch per instance, and so do
+// batches the batched kernels do not cover (schemes other than NND, slices
+// beyond the batched kernels' shared memory).
 //
 // The autotuner (hyb_autotune) times every admissible sweep launch shape
 // (cells per thread dividing the layout chunk, velocity groups per CTA up to
@@ -19,6 +30,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <string.h>
+
+#include <algorithm>
 #include <new>
 #include <string>
 #include <vector>
@@ -40,6 +54,9 @@ struct hyb_batch {
     // and error word, read back with one copy each per step
     double *d_res = nullptr, *h_res = nullptr;
     int *d_errs = nullptr, *h_errs = nullptr;
+    // argument records and work tables of the batched launches
+    void *d_tab = nullptr;
+    int ngroups = 0;
 };
 
 namespace {
@@ -71,6 +88,223 @@ void drop_graphs(hyb_batch *b) {
     if (b->g_iter) cudaGraphExecDestroy(b->g_iter);
     if (b->g_last) cudaGraphExecDestroy(b->g_last);
     b->g_iter = b->g_last = nullptr;
+    if (b->d_tab) cudaFree(b->d_tab);
+    b->d_tab = nullptr;
+    b->ngroups = 0;
+}
+
+// ---- batched plain iteration ------------------------------------------------
+struct Group {
+    std::vector<int> members;            // instance indices
+    int PA = 0, cpt = 0, vpb = 0, uni = 0, mc = 0, tpv = 0;
+    size_t wall_smem = 0, mom_smem = 0;
+    // offsets into the table (bytes) and launch sizes
+    size_t o_wall, o_wwork, o_kin, o_kwork, o_mom, o_mwork, o_fwork, o_sg, o_swork, o_scount;
+    int n_wall = 0, n_kin = 0, n_mom = 0, n_fin = 0, n_sg = 0;
+};
+
+// host image of the table: sections appended at 256-byte boundaries
+struct Table {
+    std::vector<unsigned char> bytes;
+    size_t put(const void *src, size_t n) {
+        size_t off = (bytes.size() + 255) & ~(size_t)255;
+        bytes.resize(off + n);
+        if (n) memcpy(bytes.data() + off, src, n);
+        return off;
+    }
+};
+
+// groups of one launch shape; false when an instance is outside what the
+// batched kernels cover
+bool make_groups(hyb_batch *b, std::vector<Group> &gs) {
+    for (size_t k = 0; k < b->inst.size(); k++) {
+        hyb_ctx *c = b->inst[k];
+        if (c->prm.scheme != HYB_SCHEME_NND) return false;
+        if (hyb::sweep_smem_bytes(c) > (size_t)227 * 1024 - 1024) return false;
+        int cpt, vpb;
+        hyb::sweep_shape(c, &cpt, &vpb);
+        Group *g = nullptr;
+        for (Group &q : gs)
+            if (q.PA == c->PA && q.cpt == cpt && q.vpb == vpb && q.uni == (c->uniform != 0) &&
+                b->inst[q.members[0]]->cpt == c->cpt)
+                g = &q;
+        if (!g) {
+            gs.emplace_back();
+            g = &gs.back();
+            g->PA = c->PA;
+            g->cpt = cpt;
+            g->vpb = vpb;
+            g->uni = c->uniform != 0;
+        }
+        g->members.push_back((int)k);
+    }
+    return true;
+}
+
+// device tables of every group; returns HYB_ERR_UNSUPPORTED when the
+// batched kernels do not cover the batch
+int build_tables(hyb_batch *b, std::vector<Group> &gs, int **d_errp) {
+    if (!make_groups(b, gs)) return HYB_ERR_UNSUPPORTED;
+    const int prec = b->inst[0]->precision;
+    Table T;
+    std::vector<unsigned char> rec;
+    for (Group &g : gs) {
+        const size_t n = g.members.size();
+        std::vector<int2> wwork, kwork, swork;
+        std::vector<int4> mwork, fwork;
+        std::vector<int> scount(n);
+        // walls
+        rec.assign(hyb::wall_arg_bytes(prec) * n, 0);
+        for (size_t li = 0; li < n; li++) {
+            size_t sm = 0;
+            const int nw = hyb::wall_arg_fill(b->inst[g.members[li]], rec.data() + li * hyb::wall_arg_bytes(prec), &sm);
+            g.wall_smem = std::max(g.wall_smem, sm);
+            for (int kg = 0; kg < nw; kg++) wwork.push_back(make_int2((int)li, kg));
+        }
+        g.o_wall = T.put(rec.data(), rec.size());
+        g.o_wwork = T.put(wwork.data(), wwork.size() * sizeof(int2));
+        g.n_wall = (int)wwork.size();
+        // sweeps
+        const size_t kb = prec == HYB_PREC_FP64 ? sizeof(hyb::KinArgs<double>) : sizeof(hyb::KinArgs<float>);
+        rec.assign(kb * n, 0);
+        for (size_t li = 0; li < n; li++) {
+            hyb_ctx *c = b->inst[g.members[li]];
+            if (prec == HYB_PREC_FP64) hyb::sweep_args_f64(c, 0, (hyb::KinArgs<double> *)(rec.data() + li * kb));
+            else hyb::sweep_args_f32(c, 0, (hyb::KinArgs<float> *)(rec.data() + li * kb));
+            const int nvb = (c->nv + g.vpb - 1) / g.vpb;
+            for (int vb = 0; vb < nvb; vb++) kwork.push_back(make_int2((int)li, vb));
+        }
+        g.o_kin = T.put(rec.data(), rec.size());
+        g.o_kwork = T.put(kwork.data(), kwork.size() * sizeof(int2));
+        g.n_kin = (int)kwork.size();
+        // moments
+        const size_t mb = hyb::mom_arg_bytes();
+        rec.assign(mb * n, 0);
+        for (size_t li = 0; li < n; li++) {
+            hyb_ctx *c = b->inst[g.members[li]];
+            int mc, tpv, vs, lpc, nfin;
+            size_t sm;
+            if (hyb::mom_arg_fill(c, rec.data() + li * mb, &mc, &tpv, &sm, &vs, &lpc, &nfin)) return HYB_ERR_UNSUPPORTED;
+            if (li == 0) {
+                g.mc = mc;
+                g.tpv = tpv;
+            } else if (mc != g.mc || tpv != g.tpv) {
+                return HYB_ERR_UNSUPPORTED;
+            }
+            g.mom_smem = std::max(g.mom_smem, sm);
+            for (int row = 0; row < c->Nb; row++)
+                for (int sl = 0; sl < vs; sl++) mwork.push_back(make_int4((int)li, row, sl, 0));
+            for (int blk = 0; blk < nfin; blk++) fwork.push_back(make_int4((int)li, blk, lpc, 0));
+        }
+        g.o_mom = T.put(rec.data(), rec.size());
+        g.o_mwork = T.put(mwork.data(), mwork.size() * sizeof(int4));
+        g.o_fwork = T.put(fwork.data(), fwork.size() * sizeof(int4));
+        g.n_mom = (int)mwork.size();
+        g.n_fin = (int)fwork.size();
+        // S ghosts
+        const size_t sb = hyb::sghost_arg_bytes();
+        rec.assign(sb * n, 0);
+        for (size_t li = 0; li < n; li++) {
+            scount[li] = hyb::sghost_arg_fill(b->inst[g.members[li]], rec.data() + li * sb);
+            for (int o = 0; o < scount[li]; o += 128) swork.push_back(make_int2((int)li, o));
+        }
+        g.o_sg = T.put(rec.data(), rec.size());
+        g.o_swork = T.put(swork.data(), swork.size() * sizeof(int2));
+        g.o_scount = T.put(scount.data(), scount.size() * sizeof(int));
+        g.n_sg = (int)swork.size();
+    }
+    std::vector<int *> errp(b->inst.size());
+    for (size_t k = 0; k < b->inst.size(); k++) errp[k] = b->inst[k]->d_err;
+    const size_t o_err = T.put(errp.data(), errp.size() * sizeof(int *));
+    if (b->d_tab) cudaFree(b->d_tab);
+    b->d_tab = nullptr;
+    if (cudaMalloc(&b->d_tab, T.bytes.size()) != cudaSuccess ||
+        cudaMemcpy(b->d_tab, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        b->last_error = "batch: launch tables could not be allocated";
+        return HYB_ERR_CUDA;
+    }
+    *d_errp = (int *)((unsigned char *)b->d_tab + o_err);
+    b->ngroups = (int)gs.size();
+    return HYB_OK;
+}
+
+// one group's plain iteration on stream s
+int group_launches(hyb_batch *b, const Group &g, cudaStream_t s) {
+    const int prec = b->inst[0]->precision;
+    unsigned char *t = (unsigned char *)b->d_tab;
+    int rc = hyb::wall_batch_launch(prec, t + g.o_wall, (const int2 *)(t + g.o_wwork), g.n_wall, g.wall_smem, s);
+    if (!rc) {
+        const int2 *kw = (const int2 *)(t + g.o_kwork);
+        rc = prec == HYB_PREC_FP64
+                 ? hyb::sweep_batch_f64((const hyb::KinArgs<double> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
+                                        g.uni, HYB_SCHEME_NND, s)
+                 : hyb::sweep_batch_f32((const hyb::KinArgs<float> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
+                                        g.uni, HYB_SCHEME_NND, s);
+    }
+    if (!rc)
+        rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, t + g.o_mom, (const int4 *)(t + g.o_mwork), g.n_mom,
+                                            g.mom_smem, s);
+    if (!rc) rc = hyb::moments_finish_batch_launch(prec, t + g.o_mom, (const int4 *)(t + g.o_fwork), g.n_fin, s);
+    if (!rc)
+        rc = hyb::sghost_batch_launch(t + g.o_sg, (const int2 *)(t + g.o_swork), (const int *)(t + g.o_scount), g.n_sg,
+                                      s);
+    return rc;
+}
+
+// shared-memory attributes of a group's kernels (outside any capture)
+int group_prepare(hyb_batch *b, const Group &g) {
+    const int prec = b->inst[0]->precision;
+    int rc = hyb::wall_batch_launch(prec, nullptr, nullptr, 0, g.wall_smem, b->main);
+    if (!rc)
+        rc = prec == HYB_PREC_FP64
+                 ? hyb::sweep_batch_f64(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main)
+                 : hyb::sweep_batch_f32(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main);
+    if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, nullptr, nullptr, 0, g.mom_smem, b->main);
+    return rc;
+}
+
+// capture the batched plain iteration; HYB_ERR_UNSUPPORTED leaves the
+// per-instance graph to the caller
+int build_graph_batched(hyb_batch *b, cudaGraphExec_t *exec, long long *nodes) {
+    std::vector<Group> gs;
+    int *d_errp = nullptr;
+    int rc = build_tables(b, gs, &d_errp);
+    for (size_t q = 0; q < gs.size() && !rc; q++) rc = group_prepare(b, gs[q]);
+    if (rc) return rc;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        b->last_error = "batch: stream capture could not begin";
+        return HYB_ERR_CUDA;
+    }
+    cudaEventRecord(b->fork, b->main);
+    for (size_t q = 0; q < gs.size() && !rc; q++) {
+        // the group's branch runs on its first instance's stream
+        const int k0 = gs[q].members[0];
+        cudaStream_t s = b->inst[k0]->stream;
+        cudaStreamWaitEvent(s, b->fork, 0);
+        rc = group_launches(b, gs[q], s);
+        if (rc) b->last_error = "batch: batched launch failed";
+        cudaEventRecord(b->done[k0], s);
+        cudaStreamWaitEvent(b->main, b->done[k0], 0);
+    }
+    if (!rc) rc = hyb::gather_err_launch((int *const *)d_errp, b->d_errs, (int)b->inst.size(), b->main);
+    cudaError_t e = cudaStreamEndCapture(b->main, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc == HYB_ERR_UNSUPPORTED ? HYB_ERR_CUDA : rc;
+    }
+    if (e != cudaSuccess || !g) {
+        b->last_error = std::string("batch: capture failed: ") + cudaGetErrorString(e);
+        return HYB_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        b->last_error = std::string("batch: graph instantiation failed: ") + cudaGetErrorString(e);
+        return HYB_ERR_CUDA;
+    }
+    *nodes = 5 * (long long)gs.size() + 1;
+    return HYB_OK;
 }
 
 // capture one iteration of every instance into one graph
@@ -277,13 +511,29 @@ int hyb_batch_init_maxwellian(hyb_batch *b, double rho, double u, double v, doub
     return HYB_OK;
 }
 
+// instances of the same mesh and velocity-grid sizes share one tuned shape:
+// the first of them is timed and the rest take its shape, so that they fall
+// into one launch group
+static bool same_sizes(const hyb_ctx *a, const hyb_ctx *c) {
+    return a->PA == c->PA && a->Na == c->Na && a->Nb == c->Nb && a->nvi == c->nvi && a->nvj == c->nvj &&
+           a->cpt == c->cpt && a->uniform == c->uniform && a->prm.scheme == c->prm.scheme;
+}
+
 int hyb_batch_autotune(hyb_batch *b, int reps) {
     if (!b || reps < 1) return HYB_ERR_INVALID;
     drop_graphs(b);   // the captured launches carry the old shapes
     for (size_t k = 0; k < b->inst.size(); k++) {
-        int rc = hyb_autotune(b->inst[k], reps, nullptr, nullptr);
+        hyb_ctx *c = b->inst[k];
+        size_t j = 0;
+        while (j < k && !same_sizes(b->inst[j], c)) j++;
+        if (j < k) {
+            c->sw_cpt = b->inst[j]->sw_cpt;
+            c->sw_vpb = b->inst[j]->sw_vpb;
+            continue;
+        }
+        int rc = hyb_autotune(c, reps, nullptr, nullptr);
         if (rc) {
-            b->last_error = "batch instance " + std::to_string(k) + ": " + b->inst[k]->last_error;
+            b->last_error = "batch instance " + std::to_string(k) + ": " + c->last_error;
             return rc;
         }
     }
@@ -294,7 +544,10 @@ int hyb_batch_step(hyb_batch *b, int n_iter, hyb_residual *res) {
     if (!b || n_iter < 1) return HYB_ERR_INVALID;
     cudaSetDevice(b->dev);
     int rc = HYB_OK;
-    if (!b->g_iter) rc = build_graph(b, 0, &b->g_iter, &b->nodes_iter);
+    if (!b->g_iter) {
+        rc = build_graph_batched(b, &b->g_iter, &b->nodes_iter);
+        if (rc == HYB_ERR_UNSUPPORTED) rc = build_graph(b, 0, &b->g_iter, &b->nodes_iter);
+    }
     if (!rc && !b->g_last) rc = build_graph(b, 1, &b->g_last, &b->nodes_last);
     if (rc) return rc;
     cudaEventRecord(b->ev0, b->main);

@@ -140,7 +140,28 @@ int launch_wall(hyb_ctx *ctx);
 int launch_sweep(hyb_ctx *ctx, int store_rhs);
 int sweep_prepare(hyb_ctx *ctx);
 void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb);
+// batched launches over many contexts (hyb_batch): per-context arguments and
+// work tables in device memory, one launch per launch shape
+void sweep_args_f32(hyb_ctx *ctx, int store_rhs, KinArgs<float> *A);
+void sweep_args_f64(hyb_ctx *ctx, int store_rhs, KinArgs<double> *A);
+int sweep_batch_f32(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int cpt, int vpb, bool uni,
+                    int scheme, cudaStream_t s);
+int sweep_batch_f64(const KinArgs<double> *args, const int2 *work, int nwork, int PA, int cpt, int vpb, bool uni,
+                    int scheme, cudaStream_t s);
 size_t sweep_smem_bytes(const hyb_ctx *ctx);
+size_t wall_arg_bytes(int precision);
+int wall_arg_fill(hyb_ctx *ctx, void *dst, size_t *smem);   // returns the wall face cells
+int wall_batch_launch(int precision, const void *args, const int2 *work, int nclusters, size_t smem,
+                      cudaStream_t s);
+size_t mom_arg_bytes();
+int mom_arg_fill(hyb_ctx *ctx, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc, int *nfin);
+int moments_part_batch_launch(int precision, int mc, int tpv, const void *args, const int4 *work, int nwork,
+                              size_t smem, cudaStream_t s);
+int moments_finish_batch_launch(int precision, const void *args, const int4 *work, int nwork, cudaStream_t s);
+size_t sghost_arg_bytes();
+int sghost_arg_fill(hyb_ctx *ctx, void *dst);   // returns the ghost threads
+int sghost_batch_launch(const void *args, const int2 *work, const int *count, int nblocks, cudaStream_t s);
+int gather_err_launch(int *const *errs, int *out, int n, cudaStream_t s);
 int launch_moments(hyb_ctx *ctx);
 int moments_slices(const hyb_ctx *ctx);
 int launch_sghost(hyb_ctx *ctx);

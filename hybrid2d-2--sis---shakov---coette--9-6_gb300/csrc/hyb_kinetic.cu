@@ -14,6 +14,7 @@
 #include <stdio.h>
 
 #include <cooperative_groups.h>
+#include <string.h>
 
 #include "hyb_common.cuh"
 #include "hyb_device.cuh"
@@ -37,14 +38,22 @@ template <typename real> struct WallSet {
     int on_scan[4], hi[4], first[5], nface;
 };
 
+template <typename real> struct WallArgs {
+    const real *f;
+    WallSet<real> W;
+    const double *vx, *vy, *w;
+    int nvi, nv, Na, Nb, PA;
+};
+
+// face cell kg (over all wall faces) of the cluster's context
 template <typename real>
-__global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
-    k_wall(const real *__restrict__ f, WallSet<real> W, const double *__restrict__ vx,
-           const double *__restrict__ vy, const double *__restrict__ w, int nvi, int nv, int Na, int Nb, int PA) {
+__device__ __forceinline__ void wall_body(const real *__restrict__ f, const WallSet<real> &W,
+                                          const double *__restrict__ vx, const double *__restrict__ vy,
+                                          const double *__restrict__ w, int nvi, int nv, int Na, int Nb, int PA,
+                                          int kg) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
-    const int kg = blockIdx.x / WALL_CL;  // global face cell
     // the face of kg (constant indices: the set stays in parameter space)
     real *fw = W.fw[0];
     const double *wd = W.wd[0];
@@ -138,6 +147,24 @@ __global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
             fw[((size_t)v * 2 + 1) * nslot + k] = (real)(tw * gg / 2.0);
         }
     }
+}
+
+template <typename real>
+__global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
+    k_wall(const real *__restrict__ f, WallSet<real> W, const double *__restrict__ vx,
+           const double *__restrict__ vy, const double *__restrict__ w, int nvi, int nv, int Na, int Nb, int PA) {
+    wall_body<real>(f, W, vx, vy, w, nvi, nv, Na, Nb, PA, blockIdx.x / WALL_CL);
+}
+
+// many contexts: cluster i handles face cell work[i].y of context work[i].x
+template <typename real>
+__global__ void __cluster_dims__(WALL_CL, 1, 1) __launch_bounds__(256)
+    k_wall_batch(const WallArgs<real> *__restrict__ args, const int2 *__restrict__ work) {
+    __shared__ WallArgs<real> Wa;
+    const int2 wk = work[blockIdx.x / WALL_CL];
+    if (threadIdx.x == 0) Wa = args[wk.x];
+    __syncthreads();
+    wall_body<real>(Wa.f, Wa.W, Wa.vx, Wa.vy, Wa.w, Wa.nvi, Wa.nv, Wa.Na, Wa.Nb, Wa.PA, wk.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -239,12 +266,12 @@ __host__ __device__ inline size_t mom_smem_bytes(int PA, int nloc_max) {
 // stored RHS, DETFP_res); NM = 9: the higher-order moments HOT_GKUA(1:6),
 // HOQ_GKUA(1:3) of IntegralGaussHermite (GKUA_DETFP.f90:217-229)
 template <typename real, int MC, int NM>
-__global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
+__device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int slice) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int VPS = MomVps<real>::v;
     constexpr int FLUSH = 8 / VPS;                  // slots per block of 8 velocities
     const int PA = M.PA, t = threadIdx.x, TPV = blockDim.x;
-    const int b = blockIdx.x + 1, slice = blockIdx.y;
+    const int b = bidx + 1;
     const int a0 = t * MC + 1;
     const bool act = a0 <= M.Na;
     const int nvi = M.nvi, nvj = M.nv / M.nvi;
@@ -385,10 +412,27 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
 // lpc lanes per cell (a power of two <= 32): lane l of a cell's group adds
 // the slices l, l+lpc, ... in order, then the group folds by xor shuffles
 // (a fixed order); small meshes spread the slice sums over the lanes
+template <typename real, int MC, int NM>
+__global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
+    moments_body<real, MC, NM>(M, blockIdx.x, blockIdx.y);
+}
+
+// many contexts in one launch: CTA i takes march row work[i].y and velocity
+// slice work[i].z of context work[i].x
+template <typename real, int MC>
+__global__ void __launch_bounds__(512, 1) k_moments_part_batch(const MomArgs *__restrict__ args,
+                                                               const int4 *__restrict__ work) {
+    __shared__ MomArgs Ms;
+    const int4 w = work[blockIdx.x];
+    if (threadIdx.x == 0) Ms = args[w.x];
+    __syncthreads();
+    moments_body<real, MC, 10>(Ms, w.y, w.z);
+}
+
 template <typename real>
-__global__ void k_moments_finish(MomArgs M, int lpc) {
+__device__ __forceinline__ void moments_finish_body(const MomArgs &M, int lpc, int blk) {
     const size_t ncell = (size_t)M.Nb * M.PA;
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t tid = (size_t)blk * blockDim.x + threadIdx.x;
     const size_t cell = tid / lpc;
     const int sub = (int)(tid % lpc);
     const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
@@ -446,6 +490,23 @@ __global__ void k_moments_finish(MomArgs M, int lpc) {
     ep[5 * ncell + cell] = (real)(cpt * qx);
     ep[6 * ncell + cell] = (real)(cpt * qy);
     ep[7 * ncell + cell] = (real)cf;
+}
+
+template <typename real>
+__global__ void k_moments_finish(MomArgs M, int lpc) {
+    moments_finish_body<real>(M, lpc, blockIdx.x);
+}
+
+// many contexts: block i is block work[i].y of context work[i].x, with
+// work[i].z lanes per cell
+template <typename real>
+__global__ void __launch_bounds__(256) k_moments_finish_batch(const MomArgs *__restrict__ args,
+                                                             const int4 *__restrict__ work) {
+    __shared__ MomArgs Ms;
+    const int4 w = work[blockIdx.x];
+    if (threadIdx.x == 0) Ms = args[w.x];
+    __syncthreads();
+    moments_finish_body<real>(Ms, w.z, w.y);
 }
 
 // higher-order moments per cell: slice sums as in k_moments_finish, written
@@ -634,10 +695,8 @@ static void launch_wall_real(hyb_ctx *ctx, const WallSet<real> &W, size_t smem) 
                                                                           ctx->Na, ctx->Nb, ctx->PA);
 }
 
-// every wall face of the context in one launch
-int launch_wall(hyb_ctx *ctx) {
-    WallSet<double> Wd;
-    WallSet<float> Wf;
+// the wall faces of a context (returns the number of wall face cells)
+static int wall_sets(hyb_ctx *ctx, WallSet<double> &Wd, WallSet<float> &Wf) {
     int nf = 0, first = 0;
     for (int face = 1; face <= 4; face++) {
         if (ctx->bc[face - 1] != HYB_BC_WALL) continue;
@@ -654,10 +713,21 @@ int launch_wall(hyb_ctx *ctx) {
         first += nfc;
         nf++;
     }
-    if (nf == 0) return HYB_OK;
     Wd.first[nf] = Wf.first[nf] = first;
     Wd.nface = Wf.nface = nf;
-    const size_t wall_smem = (size_t)((ctx->nv + WALL_CL - 1) / WALL_CL) * sizeof(double);
+    return first;
+}
+
+static size_t wall_smem_bytes(const hyb_ctx *ctx) {
+    return (size_t)((ctx->nv + WALL_CL - 1) / WALL_CL) * sizeof(double);
+}
+
+// every wall face of the context in one launch
+int launch_wall(hyb_ctx *ctx) {
+    WallSet<double> Wd;
+    WallSet<float> Wf;
+    if (wall_sets(ctx, Wd, Wf) == 0) return HYB_OK;
+    const size_t wall_smem = wall_smem_bytes(ctx);
     if (wall_smem > (size_t)200 * 1024) {
         ctx->last_error = "wall: velocity grid too large for one cluster's shared memory";
         return HYB_ERR_UNSUPPORTED;
@@ -851,6 +921,108 @@ int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double 
                                                      ctx->Na, ctx->Nb, ctx->PA, rho, u, v, t);
     ctx->launches++;
     return check_err(ctx, "k_init");
+}
+
+// ---- batched launches over many contexts (hyb_batch) ------------------------
+// Per-context argument records (filled on the host, copied to the device by
+// the caller) and work tables; one launch per launch shape.
+size_t wall_arg_bytes(int precision) {
+    return precision == HYB_PREC_FP64 ? sizeof(WallArgs<double>) : sizeof(WallArgs<float>);
+}
+
+int wall_arg_fill(hyb_ctx *ctx, void *dst, size_t *smem) {
+    WallSet<double> Wd;
+    WallSet<float> Wf;
+    const int n = wall_sets(ctx, Wd, Wf);
+    *smem = wall_smem_bytes(ctx);
+    if (ctx->precision == HYB_PREC_FP64) {
+        WallArgs<double> a{(const double *)ctx->d_f, Wd, ctx->d_vx, ctx->d_vy, ctx->d_w,
+                           ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA};
+        memcpy(dst, &a, sizeof(a));
+    } else {
+        WallArgs<float> a{(const float *)ctx->d_f, Wf, ctx->d_vx, ctx->d_vy, ctx->d_w,
+                          ctx->nvi, ctx->nv, ctx->Na, ctx->Nb, ctx->PA};
+        memcpy(dst, &a, sizeof(a));
+    }
+    return n;
+}
+
+int wall_batch_launch(int precision, const void *args, const int2 *work, int nclusters, size_t smem,
+                      cudaStream_t s) {
+    if (smem > (size_t)200 * 1024) return HYB_ERR_UNSUPPORTED;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_wall_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_wall_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = true;
+    }
+    if (nclusters <= 0) return HYB_OK;   // attributes only (before a capture)
+    if (precision == HYB_PREC_FP64)
+        k_wall_batch<double><<<nclusters * WALL_CL, 256, smem, s>>>((const WallArgs<double> *)args, work);
+    else
+        k_wall_batch<float><<<nclusters * WALL_CL, 256, smem, s>>>((const WallArgs<float> *)args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+size_t mom_arg_bytes() { return sizeof(MomArgs); }
+
+// the moment pass of a context: its arguments, cells per thread, threads
+// per CTA, shared memory, velocity slices, lanes per cell and finish blocks
+int mom_arg_fill(hyb_ctx *ctx, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc, int *nfin) {
+    MomArgs M = mom_args(ctx, ctx->d_f, smem, mc);
+    if (*smem > (size_t)227 * 1024 - 1024) return HYB_ERR_UNSUPPORTED;   // the batched kernel's limit
+    memcpy(dst, &M, sizeof(M));
+    *tpv = ctx->PA / *mc;
+    *vs = M.vs;
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    *lpc = finish_lpc(ncell, M.vs);
+    *nfin = (int)((ncell * *lpc + 255) / 256);
+    return HYB_OK;
+}
+
+template <typename real, int MC>
+static int mom_part_batch_one(const MomArgs *args, const int4 *work, int nwork, int tpv, size_t smem,
+                              cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_moments_part_batch<real, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024 - 1024);
+        attr = true;
+    }
+    if (nwork <= 0) return HYB_OK;   // attributes only (before a capture)
+    k_moments_part_batch<real, MC><<<nwork, tpv, smem, s>>>(args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+int moments_part_batch_launch(int precision, int mc, int tpv, const void *args, const int4 *work, int nwork,
+                              size_t smem, cudaStream_t s) {
+    const MomArgs *a = (const MomArgs *)args;
+    if (precision == HYB_PREC_FP64)
+        return mc == 2 ? mom_part_batch_one<double, 2>(a, work, nwork, tpv, smem, s)
+                       : mom_part_batch_one<double, 1>(a, work, nwork, tpv, smem, s);
+    return mc == 2 ? mom_part_batch_one<float, 2>(a, work, nwork, tpv, smem, s)
+                   : mom_part_batch_one<float, 1>(a, work, nwork, tpv, smem, s);
+}
+
+int moments_finish_batch_launch(int precision, const void *args, const int4 *work, int nwork, cudaStream_t s) {
+    if (nwork <= 0) return HYB_OK;
+    if (precision == HYB_PREC_FP64)
+        k_moments_finish_batch<double><<<nwork, 256, 0, s>>>((const MomArgs *)args, work);
+    else
+        k_moments_finish_batch<float><<<nwork, 256, 0, s>>>((const MomArgs *)args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+// error words of many contexts into one array
+__global__ void k_gather_err(int *const *__restrict__ errs, int *__restrict__ out, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = *errs[k];
+}
+
+int gather_err_launch(int *const *errs, int *out, int n, cudaStream_t s) {
+    if (n <= 0) return HYB_OK;
+    k_gather_err<<<(n + 127) / 128, 128, 0, s>>>(errs, out, n);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
 }
 
 }  // namespace hyb

@@ -320,6 +320,42 @@ int launch_sghost(hyb_ctx *ctx) {
     return check(ctx, "k_sghost");
 }
 
+// ---- S ghosts of many contexts in one launch (hyb_batch) ----------------------
+struct SghostArgs {
+    double *S;
+    NsGeom G;
+    int nwall;
+};
+
+// work[blockIdx.x] = (context, first ghost index of the block)
+__global__ void k_sghost_batch(const SghostArgs *__restrict__ args, const int2 *__restrict__ work,
+                               const int *__restrict__ count) {
+    const int2 w = work[blockIdx.x];
+    const SghostArgs &A = args[w.x];
+    const int idx = w.y + threadIdx.x;
+    if (idx >= count[w.x]) return;
+    if (idx < A.nwall) sghost_wall(A.S, A.G, idx);
+    else sghost_periodic(A.S, A.G, idx - A.nwall);
+}
+
+size_t sghost_arg_bytes() { return sizeof(SghostArgs); }
+
+// fills the context's record; returns its number of ghost threads
+int sghost_arg_fill(hyb_ctx *ctx, void *dst) {
+    SghostArgs a;
+    a.S = ctx->d_S;
+    a.G = make_geom(ctx);
+    a.nwall = 2 * (ctx->nx - 1) + 2 * (ctx->ny - 1);
+    memcpy(dst, &a, sizeof(a));
+    return a.nwall + (a.G.perx ? ctx->ny - 1 : 0) + (a.G.pery ? ctx->nx - 1 : 0);
+}
+
+int sghost_batch_launch(const void *args, const int2 *work, const int *count, int nblocks, cudaStream_t s) {
+    if (nblocks <= 0) return HYB_OK;
+    k_sghost_batch<<<nblocks, 128, 0, s>>>((const SghostArgs *)args, work, count);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
 // layout of ctx->d_hot: U[4], d, uu, vv, T, amu, tao_i_in[4], q_i_in[2],
 // tao_j_in[4], q_j_in[2], tao_i_g[4], q_i_g[2], tao_j_g[4], q_j_g[2]
 static CnsArgs make_cns(hyb_ctx *ctx) {

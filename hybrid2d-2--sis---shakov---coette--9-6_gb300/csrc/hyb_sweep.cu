@@ -88,6 +88,9 @@ static int sweep_dispatch(hyb_ctx *ctx, int store_rhs, bool launch) {
     return sweep_launch_f32(ctx, A, cpt, vpb, launch);
 }
 
+void sweep_args_f32(hyb_ctx *ctx, int store_rhs, KinArgs<float> *A) { fill_args<float>(ctx, store_rhs, *A); }
+void sweep_args_f64(hyb_ctx *ctx, int store_rhs, KinArgs<double> *A) { fill_args<double>(ctx, store_rhs, *A); }
+
 // store_rhs: 0 no RHS store, 1 RHS to d_rhs with the update, 2 RHS only
 // (to d_rhs_gsis, f unchanged)
 int launch_sweep(hyb_ctx *ctx, int store_rhs) { return sweep_dispatch(ctx, store_rhs, true); }

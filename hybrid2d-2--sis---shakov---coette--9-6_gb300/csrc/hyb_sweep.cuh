@@ -120,15 +120,16 @@ __device__ __forceinline__ real flux_whi(real s, real f1, real f2, real f3) {
     else return s > real(0) ? s * (f2 + real(0.5) * fminmd(f1 - f2, f2 - f3)) : s * (f1 - real(0.5) * (f1 - f2));
 }
 
+// the sweep of the CTA's velocity block vblk (velocities vblk * vpb + g)
 template <typename real, int CPT, bool UNI, int SCHEME>
-__global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
+__device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int PA = A.PA, Na = A.Na, Nb = A.Nb;
     const int TPV = PA / CPT;
     const int g = threadIdx.y, t = threadIdx.x;
     const int a0 = t * CPT + 1;                  // first cell of this thread
     const int lane = t & 31, warp = t >> 5;
-    const int v = blockIdx.x * blockDim.y + g;
+    const int v = vblk * blockDim.y + g;
     const bool vok = v < A.nv;
     const bool act = vok && (a0 <= Na);          // chunks are all-in or all-out
     const bool producer = (t == 0) && vok;
@@ -531,6 +532,23 @@ __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
     // for above, so no copy is in flight when the CTA exits
 }
 
+template <typename real, int CPT, bool UNI, int SCHEME>
+__global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
+    sweep_body<real, CPT, UNI, SCHEME>(A, blockIdx.x);
+}
+
+// many contexts of one launch shape in one launch: CTA i sweeps velocity
+// block work[i].y of context work[i].x (arguments staged in shared memory)
+template <typename real, int CPT, bool UNI, int SCHEME>
+__global__ void __launch_bounds__(256, 2) k_sweep_batch(const KinArgs<real> *__restrict__ args,
+                                                        const int2 *__restrict__ work) {
+    __shared__ KinArgs<real> As;
+    const int2 w = work[blockIdx.x];
+    if (threadIdx.x == 0 && threadIdx.y == 0) As = args[w.x];
+    __syncthreads();
+    sweep_body<real, CPT, UNI, SCHEME>(As, w.y);
+}
+
 // ---- host side --------------------------------------------------------------
 // launch = false only sets the kernel's shared-memory attribute (done before
 // any stream capture of the launch)
@@ -575,6 +593,37 @@ int sweep_launch_real(hyb_ctx *ctx, const KinArgs<real> &A, int cpt, int vpb, bo
                          : sweep_launch_scheme<real, 2, false>(ctx, A, vpb, launch);
         default: return u ? sweep_launch_scheme<real, 1, true>(ctx, A, vpb, launch)
                           : sweep_launch_scheme<real, 1, false>(ctx, A, vpb, launch);
+    }
+}
+
+template <typename real, int CPT, bool UNI, int SCHEME>
+int sweep_batch_one(const KinArgs<real> *args, const int2 *work, int nwork, int PA, int vpb, cudaStream_t s) {
+    const int tpv = PA / CPT;
+    const size_t smem = sweep_group_bytes<real>(PA, tpv) * vpb;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sweep_batch<real, CPT, UNI, SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024 - 512);
+        attr = true;
+    }
+    if (nwork <= 0) return HYB_OK;
+    k_sweep_batch<real, CPT, UNI, SCHEME><<<nwork, dim3(tpv, vpb), smem, s>>>(args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+// batched sweeps exist for the NND scheme (the batched workloads' scheme);
+// other schemes keep one launch per context
+template <typename real>
+int sweep_batch_real(const KinArgs<real> *args, const int2 *work, int nwork, int PA, int cpt, int vpb, bool uni,
+                     int scheme, cudaStream_t s) {
+    if (scheme != HYB_SCHEME_NND) return HYB_ERR_UNSUPPORTED;
+    switch (cpt) {
+        case 4: return uni ? sweep_batch_one<real, 4, true, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s)
+                           : sweep_batch_one<real, 4, false, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s);
+        case 2: return uni ? sweep_batch_one<real, 2, true, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s)
+                           : sweep_batch_one<real, 2, false, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s);
+        default: return uni ? sweep_batch_one<real, 1, true, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s)
+                            : sweep_batch_one<real, 1, false, HYB_SCHEME_NND>(args, work, nwork, PA, vpb, s);
     }
 }
 

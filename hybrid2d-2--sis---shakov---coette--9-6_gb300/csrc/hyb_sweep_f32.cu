@@ -6,4 +6,8 @@ int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb, bo
     return sweep_launch_real<float>(ctx, A, cpt, vpb, launch);
 }
 size_t sweep_group_bytes_f32(int PA, int tpv) { return sweep_group_bytes<float>(PA, tpv); }
+int sweep_batch_f32(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int cpt, int vpb, bool uni,
+                   int scheme, cudaStream_t s) {
+    return sweep_batch_real<float>(args, work, nwork, PA, cpt, vpb, uni, scheme, s);
+}
 }  // namespace hyb
