@@ -262,6 +262,12 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     const size_t ncell = (size_t)Nb * PA;
 
     for (int bp = -1; bp <= 2; bp++) wait_row(bp);
+    // the copies of rows 1, 2 for rows Nb+1, Nb+2 read f rows that the
+    // backward step overwrites from step 2 on: they complete before any write
+    if (perB) {
+        wait_row(Nb + 1);
+        wait_row(Nb + 2);
+    }
     if (act) {
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
