@@ -217,7 +217,7 @@ template <> struct SliceSum<double> {
     double a;
     __device__ void zero() { a = 0.0; }
     __device__ void add_part(const double *part, size_t i) { a += part[i]; }
-    __device__ void shfl_xor(int off) { a += __shfl_xor_sync(0xffffffffu, a, off); }
+    __device__ void add_sum(const SliceSum &o) { a += o.a; }
     __device__ double value() const { return a; }
 };
 template <> struct SliceSum<float> {
@@ -235,12 +235,44 @@ template <> struct SliceSum<float> {
         const float2 p = reinterpret_cast<const float2 *>(part)[i];
         add2(p.x, p.y);
     }
-    __device__ void shfl_xor(int off) {
-        const float x = __shfl_xor_sync(0xffffffffu, hi, off), y = __shfl_xor_sync(0xffffffffu, lo, off);
-        add2(x, y);
-    }
+    __device__ void add_sum(const SliceSum &o) { add2(o.hi, o.lo); }
     __device__ double value() const { return (double)hi + (double)lo; }
 };
+
+// Slice sums of a block's cells (blocks of 256 threads).  The block takes
+// 256 / lpc consecutive cells; thread (sub, c) adds slices sub, sub + lpc, ...
+// of cell c, so the threads of a warp read consecutive cells of one slice,
+// and the lpc partial sums of a cell are then folded pairwise in shared
+// memory in a fixed order.  The threads with own set hold the cell's sums.
+template <typename real, int NM>
+__device__ __forceinline__ void slice_fold(const MomArgs &M, int lpc, int blk, SliceSum<real> (&acc)[NM],
+                                           size_t &cell, bool &own) {
+    __shared__ SliceSum<real> red[NM][256];
+    const size_t ncell = (size_t)M.Nb * M.PA;
+    const int cb = 256 / lpc, c = threadIdx.x % cb, sub = threadIdx.x / cb;
+    cell = (size_t)blk * cb + c;
+    const bool ok = cell < ncell && (int)(cell % M.PA) < M.Na;
+#pragma unroll
+    for (int q = 0; q < NM; q++) acc[q].zero();
+    if (ok)
+        for (int sl = sub; sl < M.vs; sl += lpc)
+#pragma unroll
+            for (int q = 0; q < NM; q++) acc[q].add_part(M.part, ((size_t)sl * NM + q) * ncell + cell);
+    if (lpc > 1) {
+#pragma unroll
+        for (int q = 0; q < NM; q++) red[q][threadIdx.x] = acc[q];
+        for (int off = lpc >> 1; off > 0; off >>= 1) {
+            __syncthreads();
+            if (sub < off)
+#pragma unroll
+                for (int q = 0; q < NM; q++) {
+                    acc[q].add_sum(red[q][threadIdx.x + off * cb]);
+                    red[q][threadIdx.x] = acc[q];
+                }
+        }
+    }
+    own = ok && sub == 0;
+}
 template <typename real> __device__ __forceinline__ void store_part(double *part, size_t i, KahanAcc<real> &k);
 template <> __device__ __forceinline__ void store_part<double>(double *part, size_t i, KahanAcc<double> &k) {
     part[i] = k.s;
@@ -409,9 +441,6 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
         for (int c = 0; c < MC; c++) store_part<real>(M.part, ((size_t)slice * NM + q) * ncell + cell0 + c, ks[q][c]);
 }
 
-// lpc lanes per cell (a power of two <= 32): lane l of a cell's group adds
-// the slices l, l+lpc, ... in order, then the group folds by xor shuffles
-// (a fixed order); small meshes spread the slice sums over the lanes
 template <typename real, int MC, int NM>
 __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
     moments_body<real, MC, NM>(M, blockIdx.x, blockIdx.y);
@@ -432,22 +461,12 @@ __global__ void __launch_bounds__(512, 1) k_moments_part_batch(const MomArgs *__
 template <typename real>
 __device__ __forceinline__ void moments_finish_body(const MomArgs &M, int lpc, int blk) {
     const size_t ncell = (size_t)M.Nb * M.PA;
-    const size_t tid = (size_t)blk * blockDim.x + threadIdx.x;
-    const size_t cell = tid / lpc;
-    const int sub = (int)(tid % lpc);
-    const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
-    const bool ok = cell < ncell && a <= M.Na;
     SliceSum<real> acc[10];
-#pragma unroll
-    for (int q = 0; q < 10; q++) acc[q].zero();
-    if (ok)
-        for (int sl = sub; sl < M.vs; sl += lpc)
-#pragma unroll
-            for (int q = 0; q < 10; q++) acc[q].add_part(M.part, ((size_t)sl * 10 + q) * ncell + cell);
-    for (int off = lpc >> 1; off > 0; off >>= 1)
-#pragma unroll
-        for (int q = 0; q < 10; q++) acc[q].shfl_xor(off);
-    if (!ok || sub != 0) return;
+    size_t cell;
+    bool own;
+    slice_fold<real, 10>(M, lpc, blk, acc, cell, own);
+    if (!own) return;
+    const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
     double s[10];
 #pragma unroll
     for (int q = 0; q < 10; q++) s[q] = acc[q].value();
@@ -512,24 +531,13 @@ __global__ void __launch_bounds__(256) k_moments_finish_batch(const MomArgs *__r
 // higher-order moments per cell: slice sums as in k_moments_finish, written
 // to out[q][(nx+3)(ny+3)] (q = HOT 1..6, HOQ 1..3) at the interior cells
 template <typename real>
-__global__ void k_hoq_finish(MomArgs M, int lpc, double *__restrict__ out) {
-    const size_t ncell = (size_t)M.Nb * M.PA;
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t cell = tid / lpc;
-    const int sub = (int)(tid % lpc);
-    const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
-    const bool ok = cell < ncell && a <= M.Na;
+__global__ void __launch_bounds__(256) k_hoq_finish(MomArgs M, int lpc, double *__restrict__ out) {
     SliceSum<real> acc[9];
-#pragma unroll
-    for (int q = 0; q < 9; q++) acc[q].zero();
-    if (ok)
-        for (int sl = sub; sl < M.vs; sl += lpc)
-#pragma unroll
-            for (int q = 0; q < 9; q++) acc[q].add_part(M.part, ((size_t)sl * 9 + q) * ncell + cell);
-    for (int off = lpc >> 1; off > 0; off >>= 1)
-#pragma unroll
-        for (int q = 0; q < 9; q++) acc[q].shfl_xor(off);
-    if (!ok || sub != 0) return;
+    size_t cell;
+    bool own;
+    slice_fold<real, 9>(M, lpc, blockIdx.x, acc, cell, own);
+    if (!own) return;
+    const int a = (int)(cell % M.PA) + 1, b = (int)(cell / M.PA) + 1;
     const int i = M.scan_is_j ? b : a, j = M.scan_is_j ? a : b;
     const size_t c2 = hyb_c2(M.nx, i, j);
     const size_t plane = (size_t)(M.nx + 3) * (size_t)(M.ny + 3);
@@ -553,22 +561,10 @@ template <typename real>
 __global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, double *__restrict__ part,
                                                          double *__restrict__ cellm) {
     const size_t ncell = (size_t)M.Nb * M.PA;
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t cell = tid / lpc;
-    const int sub = (int)(tid % lpc);
-    const int a = (int)(cell % M.PA) + 1;
-    const bool ok = cell < ncell && a <= M.Na;
     SliceSum<real> acc[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) acc[q].zero();
-    if (ok)
-        for (int sl = sub; sl < M.vs; sl += lpc)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[q].add_part(M.part, ((size_t)sl * 4 + q) * ncell + cell);
-    for (int off = lpc >> 1; off > 0; off >>= 1)
-#pragma unroll
-        for (int q = 0; q < 4; q++) acc[q].shfl_xor(off);
-    const bool own = ok && sub == 0;
+    size_t cell;
+    bool own;
+    slice_fold<real, 4>(M, lpc, blockIdx.x, acc, cell, own);
     double s[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) s[q] = acc[q].value();
