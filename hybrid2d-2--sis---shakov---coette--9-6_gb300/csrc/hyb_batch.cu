@@ -8,18 +8,21 @@
 // Two graphs are kept: one for plain iterations and one whose sweeps also
 // store the RHS (the last iteration of a step).
 //
-// Plain iterations run as batched launches: the instances are grouped by
+// Both graphs are made of batched launches: the instances are grouped by
 // launch shape (scan-axis padding, layout chunk, sweep cells per thread and
 // velocity groups per CTA, uniform spacing), and each group issues five
-// kernels -- walls, sweeps, moment partials, moment finish, S ghosts -- whose
-// CTAs each read their instance's argument record from a device table and
-// take one (instance, block) pair from a work table.  The groups are the
-// graph's branches; a last kernel gathers the error words.  The kernels are
-// the per-context kernels' bodies, so every instance computes bit for bit
-// what a standalone context computes.  The last iteration of a step (RHS
-// store, residual, Convert_NS) keeps one branch per instance, and so do
-// batches the batched kernels do not cover (schemes other than NND, slices
-// beyond the batched kernels' shared memory).
+// kernels -- walls, sweeps, moment partials, moment finish, S ghosts; on the
+// last iteration also the residual moments of the stored RHS and their
+// per-block fold -- whose CTAs each read their instance's argument record
+// from a device table and take one (instance, block) pair from a work table.
+// The groups are the graph's branches.  After them the last iteration runs
+// Convert_NS of every instance (six launches, one per phase) and the final
+// residual folds (one warp per instance, which also gathers the residuals
+// for the single host copy); a last kernel gathers the error words.  The
+// kernels are the per-context kernels' bodies, so every instance computes
+// bit for bit what a standalone context computes.  Batches the batched
+// kernels do not cover (schemes other than NND, slices beyond the batched
+// kernels' shared memory) keep one graph branch per instance.
 //
 // The autotuner (hyb_autotune) times every admissible sweep launch shape
 // (cells per thread dividing the layout chunk, velocity groups per CTA up to
@@ -54,9 +57,8 @@ struct hyb_batch {
     // and error word, read back with one copy each per step
     double *d_res = nullptr, *h_res = nullptr;
     int *d_errs = nullptr, *h_errs = nullptr;
-    // argument records and work tables of the batched launches
-    void *d_tab = nullptr;
-    int ngroups = 0;
+    // argument records and work tables of the batched graphs
+    void *d_tab_iter = nullptr, *d_tab_last = nullptr;
 };
 
 namespace {
@@ -88,19 +90,29 @@ void drop_graphs(hyb_batch *b) {
     if (b->g_iter) cudaGraphExecDestroy(b->g_iter);
     if (b->g_last) cudaGraphExecDestroy(b->g_last);
     b->g_iter = b->g_last = nullptr;
-    if (b->d_tab) cudaFree(b->d_tab);
-    b->d_tab = nullptr;
-    b->ngroups = 0;
+    if (b->d_tab_iter) cudaFree(b->d_tab_iter);
+    if (b->d_tab_last) cudaFree(b->d_tab_last);
+    b->d_tab_iter = b->d_tab_last = nullptr;
 }
 
-// ---- batched plain iteration ------------------------------------------------
+// ---- batched iterations -----------------------------------------------------
 struct Group {
     std::vector<int> members;            // instance indices
     int PA = 0, cpt = 0, vpb = 0, uni = 0, mc = 0, tpv = 0;
     size_t wall_smem = 0, mom_smem = 0;
     // offsets into the table (bytes) and launch sizes
     size_t o_wall, o_wwork, o_kin, o_kwork, o_mom, o_mwork, o_fwork, o_sg, o_swork, o_scount;
+    size_t o_rmom = 0, o_parts = 0;      // last iteration: residual moments of the stored RHS
     int n_wall = 0, n_kin = 0, n_mom = 0, n_fin = 0, n_sg = 0;
+};
+
+// the launches of one captured iteration
+struct Plan {
+    bool last = false;                   // RHS store, Convert_NS and residual
+    std::vector<Group> gs;
+    size_t o_err = 0, o_cns = 0, o_rfin = 0;
+    size_t o_cwork[6] = {0, 0, 0, 0, 0, 0};
+    int n_cwork[6] = {0, 0, 0, 0, 0, 0};
 };
 
 // host image of the table: sections appended at 256-byte boundaries
@@ -141,14 +153,15 @@ bool make_groups(hyb_batch *b, std::vector<Group> &gs) {
     return true;
 }
 
-// device tables of every group; returns HYB_ERR_UNSUPPORTED when the
-// batched kernels do not cover the batch
-int build_tables(hyb_batch *b, std::vector<Group> &gs, int **d_errp) {
-    if (!make_groups(b, gs)) return HYB_ERR_UNSUPPORTED;
+// device tables of the plan; HYB_ERR_UNSUPPORTED when the batched kernels do
+// not cover the batch
+int build_tables(hyb_batch *b, Plan &P, void **d_tab) {
+    if (!make_groups(b, P.gs)) return HYB_ERR_UNSUPPORTED;
     const int prec = b->inst[0]->precision;
+    const int store_rhs = P.last ? 1 : 0;
     Table T;
-    std::vector<unsigned char> rec;
-    for (Group &g : gs) {
+    std::vector<unsigned char> rec, rrec;
+    for (Group &g : P.gs) {
         const size_t n = g.members.size();
         std::vector<int2> wwork, kwork, swork;
         std::vector<int4> mwork, fwork;
@@ -169,22 +182,36 @@ int build_tables(hyb_batch *b, std::vector<Group> &gs, int **d_errp) {
         rec.assign(kb * n, 0);
         for (size_t li = 0; li < n; li++) {
             hyb_ctx *c = b->inst[g.members[li]];
-            if (prec == HYB_PREC_FP64) hyb::sweep_args_f64(c, 0, (hyb::KinArgs<double> *)(rec.data() + li * kb));
-            else hyb::sweep_args_f32(c, 0, (hyb::KinArgs<float> *)(rec.data() + li * kb));
+            if (prec == HYB_PREC_FP64)
+                hyb::sweep_args_f64(c, store_rhs, (hyb::KinArgs<double> *)(rec.data() + li * kb));
+            else
+                hyb::sweep_args_f32(c, store_rhs, (hyb::KinArgs<float> *)(rec.data() + li * kb));
             const int nvb = (c->nv + g.vpb - 1) / g.vpb;
             for (int vb = 0; vb < nvb; vb++) kwork.push_back(make_int2((int)li, vb));
         }
         g.o_kin = T.put(rec.data(), rec.size());
         g.o_kwork = T.put(kwork.data(), kwork.size() * sizeof(int2));
         g.n_kin = (int)kwork.size();
-        // moments
+        // moments (and, on the last iteration, the residual moments of the
+        // RHS: the same slicing over the RHS buffer)
         const size_t mb = hyb::mom_arg_bytes();
         rec.assign(mb * n, 0);
+        rrec.assign(P.last ? mb * n : 0, 0);
+        std::vector<double *> parts(n, nullptr);
         for (size_t li = 0; li < n; li++) {
             hyb_ctx *c = b->inst[g.members[li]];
             int mc, tpv, vs, lpc, nfin;
             size_t sm;
-            if (hyb::mom_arg_fill(c, rec.data() + li * mb, &mc, &tpv, &sm, &vs, &lpc, &nfin)) return HYB_ERR_UNSUPPORTED;
+            if (hyb::mom_arg_fill(c, nullptr, rec.data() + li * mb, &mc, &tpv, &sm, &vs, &lpc, &nfin))
+                return HYB_ERR_UNSUPPORTED;
+            if (P.last) {
+                int mc2, tpv2, vs2, lpc2, nfin2;
+                size_t sm2;
+                if (hyb::mom_arg_fill(c, c->d_rhs, rrec.data() + li * mb, &mc2, &tpv2, &sm2, &vs2, &lpc2, &nfin2))
+                    return HYB_ERR_UNSUPPORTED;
+                std::vector<unsigned char> fin(hyb::resfinal_arg_bytes());
+                hyb::resfinal_arg_fill(c, fin.data(), &parts[li]);   // where the block partials go
+            }
             if (li == 0) {
                 g.mc = mc;
                 g.tpv = tpv;
@@ -201,6 +228,10 @@ int build_tables(hyb_batch *b, std::vector<Group> &gs, int **d_errp) {
         g.o_fwork = T.put(fwork.data(), fwork.size() * sizeof(int4));
         g.n_mom = (int)mwork.size();
         g.n_fin = (int)fwork.size();
+        if (P.last) {
+            g.o_rmom = T.put(rrec.data(), rrec.size());
+            g.o_parts = T.put(parts.data(), parts.size() * sizeof(double *));
+        }
         // S ghosts
         const size_t sb = hyb::sghost_arg_bytes();
         rec.assign(sb * n, 0);
@@ -213,25 +244,46 @@ int build_tables(hyb_batch *b, std::vector<Group> &gs, int **d_errp) {
         g.o_scount = T.put(scount.data(), scount.size() * sizeof(int));
         g.n_sg = (int)swork.size();
     }
-    std::vector<int *> errp(b->inst.size());
-    for (size_t k = 0; k < b->inst.size(); k++) errp[k] = b->inst[k]->d_err;
-    const size_t o_err = T.put(errp.data(), errp.size() * sizeof(int *));
-    if (b->d_tab) cudaFree(b->d_tab);
-    b->d_tab = nullptr;
-    if (cudaMalloc(&b->d_tab, T.bytes.size()) != cudaSuccess ||
-        cudaMemcpy(b->d_tab, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    const size_t ni = b->inst.size();
+    if (P.last) {
+        // Convert_NS of every instance: six launches (the face phases share one)
+        const size_t cb = hyb::cns_arg_bytes();
+        rec.assign(cb * ni, 0);
+        std::vector<int4> cw[6];
+        for (size_t k = 0; k < ni; k++) {
+            int cnt[7];
+            hyb::cns_arg_fill(b->inst[k], rec.data() + k * cb, cnt);
+            for (int ph = 0; ph < 7; ph++)
+                for (int o = 0; o * 128 < cnt[ph]; o++) cw[ph < 6 ? ph : 5].push_back(make_int4((int)k, ph, o, 0));
+        }
+        P.o_cns = T.put(rec.data(), rec.size());
+        for (int L = 0; L < 6; L++) {
+            P.o_cwork[L] = T.put(cw[L].data(), cw[L].size() * sizeof(int4));
+            P.n_cwork[L] = (int)cw[L].size();
+        }
+        // final residual folds
+        const size_t fb = hyb::resfinal_arg_bytes();
+        rec.assign(fb * ni, 0);
+        for (size_t k = 0; k < ni; k++) {
+            double *unused;
+            hyb::resfinal_arg_fill(b->inst[k], rec.data() + k * fb, &unused);
+        }
+        P.o_rfin = T.put(rec.data(), rec.size());
+    }
+    std::vector<int *> errp(ni);
+    for (size_t k = 0; k < ni; k++) errp[k] = b->inst[k]->d_err;
+    P.o_err = T.put(errp.data(), errp.size() * sizeof(int *));
+    if (cudaMalloc(d_tab, T.bytes.size()) != cudaSuccess ||
+        cudaMemcpy(*d_tab, T.bytes.data(), T.bytes.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         b->last_error = "batch: launch tables could not be allocated";
         return HYB_ERR_CUDA;
     }
-    *d_errp = (int *)((unsigned char *)b->d_tab + o_err);
-    b->ngroups = (int)gs.size();
     return HYB_OK;
 }
 
-// one group's plain iteration on stream s
-int group_launches(hyb_batch *b, const Group &g, cudaStream_t s) {
+// one group's launches on stream s
+int group_launches(hyb_batch *b, const Plan &P, const Group &g, unsigned char *t, cudaStream_t s) {
     const int prec = b->inst[0]->precision;
-    unsigned char *t = (unsigned char *)b->d_tab;
     int rc = hyb::wall_batch_launch(prec, t + g.o_wall, (const int2 *)(t + g.o_wwork), g.n_wall, g.wall_smem, s);
     if (!rc) {
         const int2 *kw = (const int2 *)(t + g.o_kwork);
@@ -241,13 +293,18 @@ int group_launches(hyb_batch *b, const Group &g, cudaStream_t s) {
                  : hyb::sweep_batch_f32((const hyb::KinArgs<float> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
                                         g.uni, HYB_SCHEME_NND, s);
     }
-    if (!rc)
-        rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, t + g.o_mom, (const int4 *)(t + g.o_mwork), g.n_mom,
-                                            g.mom_smem, s);
-    if (!rc) rc = hyb::moments_finish_batch_launch(prec, t + g.o_mom, (const int4 *)(t + g.o_fwork), g.n_fin, s);
+    const int4 *mw = (const int4 *)(t + g.o_mwork), *fw = (const int4 *)(t + g.o_fwork);
+    if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 10, t + g.o_mom, mw, g.n_mom, g.mom_smem, s);
+    if (!rc) rc = hyb::moments_finish_batch_launch(prec, t + g.o_mom, fw, g.n_fin, s);
     if (!rc)
         rc = hyb::sghost_batch_launch(t + g.o_sg, (const int2 *)(t + g.o_swork), (const int *)(t + g.o_scount), g.n_sg,
                                       s);
+    if (!rc && P.last) {
+        rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 4, t + g.o_rmom, mw, g.n_mom, g.mom_smem, s);
+        if (!rc)
+            rc = hyb::residual_finish_batch_launch(prec, t + g.o_rmom, fw, (double *const *)(t + g.o_parts), g.n_fin,
+                                                   s);
+    }
     return rc;
 }
 
@@ -259,35 +316,46 @@ int group_prepare(hyb_batch *b, const Group &g) {
         rc = prec == HYB_PREC_FP64
                  ? hyb::sweep_batch_f64(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main)
                  : hyb::sweep_batch_f32(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main);
-    if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, nullptr, nullptr, 0, g.mom_smem, b->main);
+    if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 10, nullptr, nullptr, 0, g.mom_smem, b->main);
+    if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 4, nullptr, nullptr, 0, g.mom_smem, b->main);
     return rc;
 }
 
-// capture the batched plain iteration; HYB_ERR_UNSUPPORTED leaves the
-// per-instance graph to the caller
-int build_graph_batched(hyb_batch *b, cudaGraphExec_t *exec, long long *nodes) {
-    std::vector<Group> gs;
-    int *d_errp = nullptr;
-    int rc = build_tables(b, gs, &d_errp);
-    for (size_t q = 0; q < gs.size() && !rc; q++) rc = group_prepare(b, gs[q]);
+// capture a batched iteration; HYB_ERR_UNSUPPORTED leaves the per-instance
+// graph to the caller
+int build_graph_batched(hyb_batch *b, bool last, cudaGraphExec_t *exec, long long *nodes, void **d_tab) {
+    Plan P;
+    P.last = last;
+    int rc = build_tables(b, P, d_tab);
+    for (size_t q = 0; q < P.gs.size() && !rc; q++) rc = group_prepare(b, P.gs[q]);
     if (rc) return rc;
+    unsigned char *t = (unsigned char *)*d_tab;
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         b->last_error = "batch: stream capture could not begin";
         return HYB_ERR_CUDA;
     }
+    long long n = 0;
     cudaEventRecord(b->fork, b->main);
-    for (size_t q = 0; q < gs.size() && !rc; q++) {
+    for (size_t q = 0; q < P.gs.size() && !rc; q++) {
         // the group's branch runs on its first instance's stream
-        const int k0 = gs[q].members[0];
+        const int k0 = P.gs[q].members[0];
         cudaStream_t s = b->inst[k0]->stream;
         cudaStreamWaitEvent(s, b->fork, 0);
-        rc = group_launches(b, gs[q], s);
+        rc = group_launches(b, P, P.gs[q], t, s);
         if (rc) b->last_error = "batch: batched launch failed";
         cudaEventRecord(b->done[k0], s);
         cudaStreamWaitEvent(b->main, b->done[k0], 0);
+        n += last ? 7 : 5;
     }
-    if (!rc) rc = hyb::gather_err_launch((int *const *)d_errp, b->d_errs, (int)b->inst.size(), b->main);
+    if (last) {
+        for (int L = 0; L < 6 && !rc; L++, n++)
+            rc = hyb::cns_batch_launch(t + P.o_cns, (const int4 *)(t + P.o_cwork[L]), P.n_cwork[L], b->main);
+        if (!rc) rc = hyb::residual_final_batch_launch(t + P.o_rfin, (int)b->inst.size(), b->d_res, b->main);
+        n++;
+    }
+    if (!rc) rc = hyb::gather_err_launch((int *const *)(t + P.o_err), b->d_errs, (int)b->inst.size(), b->main);
+    n++;
     cudaError_t e = cudaStreamEndCapture(b->main, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -303,7 +371,7 @@ int build_graph_batched(hyb_batch *b, cudaGraphExec_t *exec, long long *nodes) {
         b->last_error = std::string("batch: graph instantiation failed: ") + cudaGetErrorString(e);
         return HYB_ERR_CUDA;
     }
-    *nodes = 5 * (long long)gs.size() + 1;
+    *nodes = n;
     return HYB_OK;
 }
 
@@ -545,10 +613,13 @@ int hyb_batch_step(hyb_batch *b, int n_iter, hyb_residual *res) {
     cudaSetDevice(b->dev);
     int rc = HYB_OK;
     if (!b->g_iter) {
-        rc = build_graph_batched(b, &b->g_iter, &b->nodes_iter);
+        rc = build_graph_batched(b, false, &b->g_iter, &b->nodes_iter, &b->d_tab_iter);
         if (rc == HYB_ERR_UNSUPPORTED) rc = build_graph(b, 0, &b->g_iter, &b->nodes_iter);
     }
-    if (!rc && !b->g_last) rc = build_graph(b, 1, &b->g_last, &b->nodes_last);
+    if (!rc && !b->g_last) {
+        rc = build_graph_batched(b, true, &b->g_last, &b->nodes_last, &b->d_tab_last);
+        if (rc == HYB_ERR_UNSUPPORTED) rc = build_graph(b, 1, &b->g_last, &b->nodes_last);
+    }
     if (rc) return rc;
     cudaEventRecord(b->ev0, b->main);
     for (int it = 0; it < n_iter; it++) {

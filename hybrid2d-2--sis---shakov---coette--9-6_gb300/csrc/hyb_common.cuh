@@ -154,9 +154,18 @@ int wall_arg_fill(hyb_ctx *ctx, void *dst, size_t *smem);   // returns the wall 
 int wall_batch_launch(int precision, const void *args, const int2 *work, int nclusters, size_t smem,
                       cudaStream_t s);
 size_t mom_arg_bytes();
-int mom_arg_fill(hyb_ctx *ctx, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc, int *nfin);
-int moments_part_batch_launch(int precision, int mc, int tpv, const void *args, const int4 *work, int nwork,
+int mom_arg_fill(hyb_ctx *ctx, const void *f, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc,
+                 int *nfin);   // f: the distribution summed (nullptr: ctx->d_f)
+int moments_part_batch_launch(int precision, int mc, int tpv, int nm, const void *args, const int4 *work, int nwork,
                               size_t smem, cudaStream_t s);
+int residual_finish_batch_launch(int precision, const void *args, const int4 *work, double *const *parts, int nwork,
+                                 cudaStream_t s);
+size_t resfinal_arg_bytes();
+void resfinal_arg_fill(hyb_ctx *ctx, void *dst, double **part);
+int residual_final_batch_launch(const void *args, int n, double *copy, cudaStream_t s);
+size_t cns_arg_bytes();
+int cns_arg_fill(hyb_ctx *ctx, void *dst, int counts[7]);   // threads of the seven Convert_NS phases
+int cns_batch_launch(const void *args, const int4 *work, int nwork, cudaStream_t s);
 int moments_finish_batch_launch(int precision, const void *args, const int4 *work, int nwork, cudaStream_t s);
 size_t sghost_arg_bytes();
 int sghost_arg_fill(hyb_ctx *ctx, void *dst);   // returns the ghost threads

@@ -448,14 +448,14 @@ __global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
 
 // many contexts in one launch: CTA i takes march row work[i].y and velocity
 // slice work[i].z of context work[i].x
-template <typename real, int MC>
+template <typename real, int MC, int NM>
 __global__ void __launch_bounds__(512, 1) k_moments_part_batch(const MomArgs *__restrict__ args,
                                                                const int4 *__restrict__ work) {
     __shared__ MomArgs Ms;
     const int4 w = work[blockIdx.x];
     if (threadIdx.x == 0) Ms = args[w.x];
     __syncthreads();
-    moments_body<real, MC, 10>(Ms, w.y, w.z);
+    moments_body<real, MC, NM>(Ms, w.y, w.z);
 }
 
 template <typename real>
@@ -558,13 +558,13 @@ __device__ __forceinline__ double nanmax(double a, double b) {
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, double *__restrict__ part,
-                                                         double *__restrict__ cellm) {
+__device__ __forceinline__ void residual_finish_body(const MomArgs &M, int lpc, int blk, double *__restrict__ part,
+                                                     double *__restrict__ cellm) {
     const size_t ncell = (size_t)M.Nb * M.PA;
     SliceSum<real> acc[4];
     size_t cell;
     bool own;
-    slice_fold<real, 4>(M, lpc, blockIdx.x, acc, cell, own);
+    slice_fold<real, 4>(M, lpc, blk, acc, cell, own);
     double s[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) s[q] = acc[q].value();
@@ -600,13 +600,33 @@ __global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, dou
             m = nanmax(m, wm[w][q]);
             t += ws[w][q];
         }
-        part[(size_t)blockIdx.x * 8 + q] = m;
-        part[(size_t)blockIdx.x * 8 + 4 + q] = t;
+        part[(size_t)blk * 8 + q] = m;
+        part[(size_t)blk * 8 + 4 + q] = t;
     }
 }
 
-__global__ void k_residual_final(const double *__restrict__ part, int nblk, double ncell, double *__restrict__ out) {
-    // one warp per component pair; deterministic sequential fold per lane
+template <typename real>
+__global__ void __launch_bounds__(256) k_residual_finish(MomArgs M, int lpc, double *__restrict__ part,
+                                                         double *__restrict__ cellm) {
+    residual_finish_body<real>(M, lpc, blockIdx.x, part, cellm);
+}
+
+// many contexts: block i is block work[i].y of context work[i].x (work[i].z
+// lanes per cell), block partials to parts[work[i].x]
+template <typename real>
+__global__ void __launch_bounds__(256) k_residual_finish_batch(const MomArgs *__restrict__ args,
+                                                               const int4 *__restrict__ work,
+                                                               double *const *__restrict__ parts) {
+    __shared__ MomArgs Ms;
+    const int4 w = work[blockIdx.x];
+    if (threadIdx.x == 0) Ms = args[w.x];
+    __syncthreads();
+    residual_finish_body<real>(Ms, w.z, w.y, parts[w.x], nullptr);
+}
+
+__device__ __forceinline__ void residual_final_body(const double *__restrict__ part, int nblk, double ncell,
+                                                    double *__restrict__ out) {
+    // one warp; deterministic sequential fold per lane
     __shared__ double mx[32][4], ss[32][4];
     const int lane = threadIdx.x;
     double m[4] = {0, 0, 0, 0}, s[4] = {0, 0, 0, 0};
@@ -635,6 +655,25 @@ __global__ void k_residual_final(const double *__restrict__ part, int nblk, doub
         }
         out[8] = mrms;
     }
+}
+
+__global__ void k_residual_final(const double *__restrict__ part, int nblk, double ncell, double *__restrict__ out) {
+    residual_final_body(part, nblk, ncell, out);
+}
+
+// many contexts: warp k folds context k's block partials into its residual
+// and copies the 9 values to copy[9 k ..]
+struct ResFinalArgs {
+    const double *part;
+    double *out;
+    int nblk;
+    double ncell;
+};
+__global__ void k_residual_final_batch(const ResFinalArgs *__restrict__ args, double *__restrict__ copy) {
+    const ResFinalArgs A = args[blockIdx.x];
+    residual_final_body(A.part, A.nblk, A.ncell, A.out);
+    __syncwarp();
+    if (threadIdx.x < 9) copy[(size_t)blockIdx.x * 9 + threadIdx.x] = A.out[threadIdx.x];
 }
 
 // ---------------------------------------------------------------------------
@@ -964,8 +1003,9 @@ size_t mom_arg_bytes() { return sizeof(MomArgs); }
 
 // the moment pass of a context: its arguments, cells per thread, threads
 // per CTA, shared memory, velocity slices, lanes per cell and finish blocks
-int mom_arg_fill(hyb_ctx *ctx, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc, int *nfin) {
-    MomArgs M = mom_args(ctx, ctx->d_f, smem, mc);
+int mom_arg_fill(hyb_ctx *ctx, const void *f, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc,
+                 int *nfin) {
+    MomArgs M = mom_args(ctx, f ? f : ctx->d_f, smem, mc);
     if (*smem > (size_t)227 * 1024 - 1024) return HYB_ERR_UNSUPPORTED;   // the batched kernel's limit
     memcpy(dst, &M, sizeof(M));
     *tpv = ctx->PA / *mc;
@@ -976,28 +1016,66 @@ int mom_arg_fill(hyb_ctx *ctx, void *dst, int *mc, int *tpv, size_t *smem, int *
     return HYB_OK;
 }
 
-template <typename real, int MC>
+template <typename real, int MC, int NM>
 static int mom_part_batch_one(const MomArgs *args, const int4 *work, int nwork, int tpv, size_t smem,
                               cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_moments_part_batch<real, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_moments_part_batch<real, MC, NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              227 * 1024 - 1024);
         attr = true;
     }
     if (nwork <= 0) return HYB_OK;   // attributes only (before a capture)
-    k_moments_part_batch<real, MC><<<nwork, tpv, smem, s>>>(args, work);
+    k_moments_part_batch<real, MC, NM><<<nwork, tpv, smem, s>>>(args, work);
     return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
 }
 
-int moments_part_batch_launch(int precision, int mc, int tpv, const void *args, const int4 *work, int nwork,
+template <int NM>
+static int mom_part_batch_nm(int precision, int mc, int tpv, const MomArgs *a, const int4 *work, int nwork,
+                             size_t smem, cudaStream_t s) {
+    if (precision == HYB_PREC_FP64)
+        return mc == 2 ? mom_part_batch_one<double, 2, NM>(a, work, nwork, tpv, smem, s)
+                       : mom_part_batch_one<double, 1, NM>(a, work, nwork, tpv, smem, s);
+    return mc == 2 ? mom_part_batch_one<float, 2, NM>(a, work, nwork, tpv, smem, s)
+                   : mom_part_batch_one<float, 1, NM>(a, work, nwork, tpv, smem, s);
+}
+
+// nm = 10: the DETFP moments; nm = 4: the residual moments of a stored RHS
+int moments_part_batch_launch(int precision, int mc, int tpv, int nm, const void *args, const int4 *work, int nwork,
                               size_t smem, cudaStream_t s) {
     const MomArgs *a = (const MomArgs *)args;
+    if (nm == 4) return mom_part_batch_nm<4>(precision, mc, tpv, a, work, nwork, smem, s);
+    return mom_part_batch_nm<10>(precision, mc, tpv, a, work, nwork, smem, s);
+}
+
+int residual_finish_batch_launch(int precision, const void *args, const int4 *work, double *const *parts, int nwork,
+                                 cudaStream_t s) {
+    if (nwork <= 0) return HYB_OK;
     if (precision == HYB_PREC_FP64)
-        return mc == 2 ? mom_part_batch_one<double, 2>(a, work, nwork, tpv, smem, s)
-                       : mom_part_batch_one<double, 1>(a, work, nwork, tpv, smem, s);
-    return mc == 2 ? mom_part_batch_one<float, 2>(a, work, nwork, tpv, smem, s)
-                   : mom_part_batch_one<float, 1>(a, work, nwork, tpv, smem, s);
+        k_residual_finish_batch<double><<<nwork, 256, 0, s>>>((const MomArgs *)args, work, parts);
+    else
+        k_residual_finish_batch<float><<<nwork, 256, 0, s>>>((const MomArgs *)args, work, parts);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+size_t resfinal_arg_bytes() { return sizeof(ResFinalArgs); }
+
+// the context's final residual fold; *part receives its block partials
+void resfinal_arg_fill(hyb_ctx *ctx, void *dst, double **part) {
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA;
+    ResFinalArgs a;
+    a.part = ctx->d_resid + 16;
+    a.out = ctx->d_resid;
+    a.nblk = (int)((ncell * finish_lpc(ncell, moments_slices(ctx)) + 255) / 256);
+    a.ncell = (double)ctx->ncx * ctx->ncy;
+    memcpy(dst, &a, sizeof(a));
+    *part = ctx->d_resid + 16;
+}
+
+int residual_final_batch_launch(const void *args, int n, double *copy, cudaStream_t s) {
+    if (n <= 0) return HYB_OK;
+    k_residual_final_batch<<<n, 32, 0, s>>>((const ResFinalArgs *)args, copy);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
 }
 
 int moments_finish_batch_launch(int precision, const void *args, const int4 *work, int nwork, cudaStream_t s) {

@@ -96,10 +96,9 @@ struct CnsArgs {
 };
 
 // corners of S (Hybrid_Sub.f90:221-224; periodic faces copy the partner)
-__global__ void k_cns_corners(CnsArgs A) {
+__device__ __forceinline__ void cns_corners(const CnsArgs &A, int k) {
     const NsGeom &G = A.G;
     const int nx = G.nx, ny = G.ny;
-    int k = threadIdx.x;
     if (k >= HYB_NSUM) return;
     double *Sk = A.S + (size_t)k * G.nc;
     if (G.perx) {
@@ -122,10 +121,9 @@ __global__ void k_cns_corners(CnsArgs A) {
 
 // U from S on 0..nx x 0..ny (Hybrid_Sub.f90:225-235); cells outside keep
 // the reference's initial state
-__global__ void k_cns_u(CnsArgs A) {
+__device__ __forceinline__ void cns_u(const CnsArgs &A, size_t idx) {
     const NsGeom &G = A.G;
     const int nx = G.nx, ny = G.ny;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G.nc) return;
     int i = (int)(idx % (nx + 3)) - 1, j = (int)(idx / (nx + 3)) - 1;
     double *U0 = A.U, *U1 = A.U + G.nc, *U2 = A.U + 2 * G.nc, *U3 = A.U + 3 * G.nc;
@@ -144,10 +142,10 @@ __global__ void k_cns_u(CnsArgs A) {
 }
 
 // ghost U: columns then rows (Hybrid_Sub.f90:236-239), periodic faces copy
-__global__ void k_cns_ughost_cols(CnsArgs A) {
+__device__ __forceinline__ void cns_ughost_col(const CnsArgs &A, int t) {
     const NsGeom &G = A.G;
     const int nx = G.nx;
-    int j = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+    const int j = t - 1;
     if (j > G.ny + 1) return;
     for (int m = 0; m < 4; m++) {
         double *Um = A.U + (size_t)m * G.nc;
@@ -162,10 +160,10 @@ __global__ void k_cns_ughost_cols(CnsArgs A) {
         }
     }
 }
-__global__ void k_cns_ughost_rows(CnsArgs A) {
+__device__ __forceinline__ void cns_ughost_row(const CnsArgs &A, int t) {
     const NsGeom &G = A.G;
     const int ny = G.ny;
-    int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+    const int i = t - 1;
     if (i > G.nx + 1) return;
     for (int m = 0; m < 4; m++) {
         double *Um = A.U + (size_t)m * G.nc;
@@ -182,9 +180,8 @@ __global__ void k_cns_ughost_rows(CnsArgs A) {
 }
 
 // primitive NS variables and viscosity (comput_duvtpckw, get_viscous)
-__global__ void k_cns_prim(CnsArgs A) {
+__device__ __forceinline__ void cns_prim(const CnsArgs &A, size_t idx) {
     const NsGeom &G = A.G;
-    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= G.nc) return;
     int i = (int)(idx % (G.nx + 3)) - 1, j = (int)(idx / (G.nx + 3)) - 1;
     double d = A.U[idx];
@@ -198,11 +195,10 @@ __global__ void k_cns_prim(CnsArgs A) {
 }
 
 // face quantities: dir 0 = i-faces (i=1..nx, j=1..ny-1), 1 = j-faces
-__global__ void k_cns_faces(CnsArgs A, int dir) {
+__device__ __forceinline__ void cns_face(const CnsArgs &A, int dir, int idx) {
     const NsGeom &G = A.G;
     const int nx = G.nx, ny = G.ny;
     int ni = dir == 0 ? nx : nx - 1, nj = dir == 0 ? ny - 1 : ny;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ni * nj) return;
     int i = idx % ni + 1, j = idx / ni + 1;
     const double *x1 = A.x1, *y1 = A.y1, *uu = A.uu, *vv = A.vv, *T = A.T, *amu = A.amu;
@@ -287,6 +283,34 @@ __global__ void k_cns_faces(CnsArgs A, int dir) {
         tg[3 * G.nc + c] = -(S10[cc] - tmp) / g2 - t33;
         qg[0 * G.nc + c] = -S8[cc] * q2 - qx;
         qg[1 * G.nc + c] = -S9[cc] * q2 - qy;
+    }
+}
+
+__global__ void k_cns_corners(CnsArgs A) { cns_corners(A, threadIdx.x); }
+__global__ void k_cns_u(CnsArgs A) { cns_u(A, (size_t)blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_cns_ughost_cols(CnsArgs A) { cns_ughost_col(A, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_cns_ughost_rows(CnsArgs A) { cns_ughost_row(A, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_cns_prim(CnsArgs A) { cns_prim(A, (size_t)blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_cns_faces(CnsArgs A, int dir) { cns_face(A, dir, blockIdx.x * blockDim.x + threadIdx.x); }
+
+// Convert_NS of many contexts: block i runs phase work[i].y (0 corners, 1 U,
+// 2 ghost columns, 3 ghost rows, 4 primitives, 5 i-faces, 6 j-faces) for
+// threads 128 work[i].z .. of context work[i].x; a launch holds one phase, or
+// the two face phases, which are independent
+__global__ void __launch_bounds__(128) k_cns_batch(const CnsArgs *__restrict__ args, const int4 *__restrict__ work) {
+    __shared__ CnsArgs As;
+    const int4 w = work[blockIdx.x];
+    if (threadIdx.x == 0) As = args[w.x];
+    __syncthreads();
+    const int t = w.z * 128 + threadIdx.x;
+    switch (w.y) {
+        case 0: cns_corners(As, t); break;
+        case 1: cns_u(As, (size_t)t); break;
+        case 2: cns_ughost_col(As, t); break;
+        case 3: cns_ughost_row(As, t); break;
+        case 4: cns_prim(As, (size_t)t); break;
+        case 5: cns_face(As, 0, t); break;
+        default: cns_face(As, 1, t); break;
     }
 }
 
@@ -391,6 +415,28 @@ static CnsArgs make_cns(hyb_ctx *ctx) {
 }
 
 size_t hot_doubles(int nx, int ny) { return (size_t)(nx + 3) * (ny + 3) * 33; }
+
+size_t cns_arg_bytes() { return sizeof(CnsArgs); }
+
+// the context's record and the threads of its seven phases
+int cns_arg_fill(hyb_ctx *ctx, void *dst, int counts[7]) {
+    CnsArgs A = make_cns(ctx);
+    memcpy(dst, &A, sizeof(A));
+    counts[0] = HYB_NSUM;
+    counts[1] = (int)A.G.nc;
+    counts[2] = ctx->ny + 3;
+    counts[3] = ctx->nx + 3;
+    counts[4] = (int)A.G.nc;
+    counts[5] = ctx->nx * (ctx->ny - 1);
+    counts[6] = (ctx->nx - 1) * ctx->ny;
+    return HYB_OK;
+}
+
+int cns_batch_launch(const void *args, const int4 *work, int nwork, cudaStream_t s) {
+    if (nwork <= 0) return HYB_OK;
+    k_cns_batch<<<nwork, 128, 0, s>>>((const CnsArgs *)args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
 
 int launch_convert_ns(hyb_ctx *ctx) {
     CnsArgs A = make_cns(ctx);
