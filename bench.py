@@ -443,7 +443,8 @@ def run_batch(args, world, rank, local):
         "config": {"workload": "batched Couette, 256 instances", "instances": len(cl),
                    "cell_velocities_per_step": units // args.steps,
                    "precision": "fp32 f/fluxes/sweeps, fp64 moments", "scheme": "NND",
-                   "launch": "one CUDA graph launch per outer iteration, one branch per instance",
+                   "launch": "one CUDA graph launch per outer iteration; one batched launch per kernel and "
+                             "launch-shape group (instances grouped by sweep shape)",
                    "autotune_s": round(t_tune, 2), "parallelism": f"replicas x{world}",
                    "l2": "per-step working set above L2 (sum of f over instances)"},
         "e2e": {"value": world * units / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,

@@ -312,6 +312,7 @@ class Batch:
             raise HybError(rc, "hyb_batch_create failed")
         self.h = h
         self.n = n
+        self._res = (T.HybResidual * n)()     # reused by every step
 
     def _ck(self, rc, what):
         if rc != 0:
@@ -342,9 +343,12 @@ class Batch:
         self._ck(self.L.hyb_batch_autotune(self.h, reps), "batch_autotune")
 
     def step(self, n=1, residual=True):
-        res = (T.HybResidual * self.n)() if residual else None
-        self._ck(self.L.hyb_batch_step(self.h, n, res), "batch_step")
-        return [r.as_dict() for r in res] if residual else None
+        self._ck(self.L.hyb_batch_step(self.h, n, self._res if residual else None), "batch_step")
+        if not residual:
+            return None
+        # hyb_residual is 9 packed doubles: res_max[4], res_rms[4], max_rms
+        rows = np.frombuffer(self._res, dtype=np.float64).reshape(self.n, 9).tolist()
+        return [{"res_max": r[:4], "res_rms": r[4:8], "max_rms": r[8]} for r in rows]
 
     def last_ms(self):
         x = C.c_double()

@@ -545,7 +545,10 @@ int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
         if (!rc) rc = staged(ctx, ST_SWEEP, &evi, [&] { return hyb::launch_sweep(ctx, last ? 1 : 0); });
         if (!rc) rc = staged(ctx, ST_MOM, &evi, [&] { return hyb::launch_moments(ctx); });
         if (!rc) rc = staged(ctx, ST_SGHOST, &evi, [&] { return hyb::launch_sghost(ctx); });
-        if (!rc) rc = staged(ctx, ST_CNS, &evi, [&] { return hyb::launch_convert_ns(ctx); });
+        // Convert_NS feeds the synthetic solve and the NS / HoT fields a caller
+        // downloads: without GSIS only the call's last iteration needs it
+        if (!rc && (ctx->gsis.enable || last))
+            rc = staged(ctx, ST_CNS, &evi, [&] { return hyb::launch_convert_ns(ctx); });
         if (!rc && ctx->gsis.enable) rc = staged(ctx, ST_GSIS, &evi, [&] { return hyb::gsis_solve(ctx); });
         if (!rc && ctx->gsis.enable) {
             ctx->gsis_outer++;

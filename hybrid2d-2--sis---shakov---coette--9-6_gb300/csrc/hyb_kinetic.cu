@@ -71,6 +71,7 @@ __device__ __forceinline__ void wall_body(const real *__restrict__ f, const Wall
     const int per = (nv + WALL_CL - 1) / WALL_CL, vb = rank * per, ve = min(nv, vb + per);
     // wall data: [k][6] = u, v, t, swnx, swny, step
     const double uw = wd[k * 6 + 0], vw = wd[k * 6 + 1], tw = wd[k * 6 + 2];
+    const float itw_f = (float)(1.0 / tw), ipt_f = (float)(1.0 / (HYB_PI * tw));
     const double swnx = wd[k * 6 + 3], swny = wd[k * 6 + 4], step = wd[k * 6 + 5];
     // cell offsets of the two cells next to the wall
     size_t cp, cp1, nslot;
@@ -104,8 +105,16 @@ __device__ __forceinline__ void wall_body(const real *__restrict__ f, const Wall
         double vnw = ((vxx - uw) * swnx + (vyy - vw) * swny) * step;
         double vnn = (vnw - fabs(vnw)) / 2.0;
         s0 += wt * (vnn * tG);
-        const double cv = (vxx - uw) * (vxx - uw) + (vyy - vw) * (vyy - vw);
-        const double em = exp(-cv / tw) / (HYB_PI * tw);
+        double em;
+        if constexpr (sizeof(real) == 4) {
+            // FP32 distribution: the wall Maxwellian in FP32 (it is stored in
+            // FP32); its weighted sum below stays FP64
+            const float dx = (float)(vxx - uw), dy = (float)(vyy - vw);
+            em = (double)(expf(-(dx * dx + dy * dy) * itw_f) * ipt_f);
+        } else {
+            const double cv = (vxx - uw) * (vxx - uw) + (vyy - vw) * (vyy - vw);
+            em = exp(-cv / tw) / (HYB_PI * tw);
+        }
         emax[v - vb] = em;
         double fb = (vnw + fabs(vnw)) / 2.0 * em;
         s1 += wt * fb;
