@@ -153,7 +153,7 @@ void free_all(hyb_ctx *c) {
     for (int k = 0; k < 4; k++) F(c->d_fw[k]);
     F(c->d_eqp); F(c->d_vol); F(c->d_gA1); F(c->d_gA2); F(c->d_gB1); F(c->d_gB2);
     F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_CF); F(c->d_wall);
-    F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err); F(c->d_mpart);
+    F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err); F(c->d_mpart); F(c->d_stage);
     if (c->h_resid) cudaFreeHost(c->h_resid);
     if (c->h_wall) cudaFreeHost(c->h_wall);
     for (auto ev : c->prof_ev) cudaEventDestroy(ev);
@@ -679,23 +679,28 @@ int hyb_download_f(hyb_ctx *ctx, double *frd) {
     return HYB_OK;
 }
 
+// S_GKUA is transposed to the host's component-fastest order on the device
+// and copied row by row into the block -1..nx+1 x -1..ny+1 of the host array
+// (the outer ghost layers of the host array are left as they are)
 int hyb_download_moments(hyb_ctx *ctx, double *s_gkua, double *cf) {
     if (!ctx || (!s_gkua && !cf)) return HYB_ERR_INVALID;
     cudaSetDevice(ctx->dev);
     const int nx = ctx->nx, ny = ctx->ny, pw = nx + 7;
     const size_t nc2 = (size_t)(nx + 3) * (ny + 3);
-    std::vector<double> S(HYB_NSUM * nc2), C(nc2);
-    HYB_CK(cudaStreamSynchronize(ctx->stream));
-    HYB_CK(cudaMemcpy(S.data(), ctx->d_S, S.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    HYB_CK(cudaMemcpy(C.data(), ctx->d_CF, C.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int j = -1; j <= ny + 1; j++)
-        for (int i = -1; i <= nx + 1; i++) {
-            size_t c2 = hyb_c2(nx, i, j);
-            size_t ix = (size_t)(i + 3) + (size_t)pw * (j + 3);
-            if (s_gkua)
-                for (int k = 0; k < HYB_NSUM; k++) s_gkua[ix * HYB_NSUM + k] = S[(size_t)k * nc2 + c2];
-            if (cf) cf[c2] = C[c2];
+    if (s_gkua) {
+        if (!ctx->d_stage && cudaMalloc((void **)&ctx->d_stage, HYB_NSUM * nc2 * sizeof(double)) != cudaSuccess) {
+            ctx->d_stage = nullptr;
+            ctx->last_error = "download_moments: device staging allocation failed";
+            return HYB_ERR_NOMEM;
         }
+        int rc = hyb::launch_s_host_layout(ctx, ctx->d_stage);
+        if (rc) return rc;
+        const size_t row = (size_t)(nx + 3) * HYB_NSUM * sizeof(double);
+        HYB_CK(cudaMemcpy2DAsync(s_gkua + ((size_t)2 + (size_t)pw * 2) * HYB_NSUM, (size_t)pw * HYB_NSUM * sizeof(double),
+                                 ctx->d_stage, row, row, (size_t)ny + 3, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (cf) HYB_CK(cudaMemcpyAsync(cf, ctx->d_CF, nc2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
     return HYB_OK;
 }
 

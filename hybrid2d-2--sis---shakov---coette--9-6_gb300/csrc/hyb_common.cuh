@@ -100,6 +100,7 @@ struct hyb_ctx {
     double *d_hot;                         // HoT + NSF arrays (see hyb_ns.cu)
     double *d_resid;                       // residual partials / result
     double *d_mpart;                       // moment partial sums [VS][10][Nb*PA]
+    double *d_stage;                       // host-layout staging of downloads (first use)
     int *d_err;
     double *h_resid;                       // pinned
     int rhs_valid;
@@ -174,6 +175,7 @@ int gather_err_launch(int *const *errs, int *out, int n, cudaStream_t s);
 int launch_moments(hyb_ctx *ctx);
 int moments_slices(const hyb_ctx *ctx);
 int launch_sghost(hyb_ctx *ctx);
+int launch_s_host_layout(hyb_ctx *ctx, double *out);   // S as [(ny+3)(nx+3)][NSUM]
 int launch_residual(hyb_ctx *ctx, hyb_residual *out);
 int launch_rhs_moments(hyb_ctx *ctx, double *cellm);
 int residual_blocks(const hyb_ctx *ctx);   // blocks of the residual partials

@@ -10,6 +10,8 @@
 // All arrays are on the reference extents (1-LAP:n+LAP-1) with i fastest,
 // SoA over components: X[c][(nx+3)(ny+3)].
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "hyb_common.cuh"
@@ -342,6 +344,26 @@ int launch_sghost(hyb_ctx *ctx) {
     k_sghost<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_S, G, nwall);
     ctx->launches++;
     return check(ctx, "k_sghost");
+}
+
+// ---- S in the host's component-fastest order ---------------------------------
+// out[c * NSUM + k] = S[k][c] over the (nx+3)(ny+3) block, so that its rows
+// are the host array's rows of S_GKUA(1:NSUM, -1:nx+1, j)
+__global__ void k_s_host_layout(const double *__restrict__ S, size_t nc, double *__restrict__ out) {
+    const size_t n = nc * HYB_NSUM;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = t / HYB_NSUM;
+        out[t] = S[(t - c * HYB_NSUM) * nc + c];
+    }
+}
+
+int launch_s_host_layout(hyb_ctx *ctx, double *out) {
+    const size_t nc = (size_t)(ctx->nx + 3) * (ctx->ny + 3);
+    const size_t n = nc * HYB_NSUM;
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+    k_s_host_layout<<<grid, 256, 0, ctx->stream>>>(ctx->d_S, nc, out);
+    ctx->launches++;
+    return check(ctx, "k_s_host_layout");
 }
 
 // ---- S ghosts of many contexts in one launch (hyb_batch) ----------------------
