@@ -197,7 +197,7 @@ struct MomArgs {
     double cfc, cpr, x1s, r00, t00;
 };
 
-constexpr int MOM_NST = 4;
+constexpr int MOM_NST = 3;
 
 template <typename real> struct KahanAcc;
 template <> struct KahanAcc<double> {
@@ -789,9 +789,10 @@ int launch_wall(hyb_ctx *ctx) {
 }
 
 int moments_slices(const hyb_ctx *ctx) {
-    // enough CTAs to fill the GPU: about 8 per SM, whole velocity rows each
+    // enough CTAs to fill the GPU: about 16 per SM (four waves of the four
+    // CTAs an SM holds with a 3-slot ring at PA = 512), whole velocity rows each
     int nvj = ctx->nvj;
-    int vs = (152 * 8 + ctx->Nb - 1) / ctx->Nb;
+    int vs = (152 * 16 + ctx->Nb - 1) / ctx->Nb;
     if (vs > nvj) vs = nvj;
     if (vs < 1) vs = 1;
     return vs;

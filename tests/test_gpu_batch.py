@@ -97,3 +97,21 @@ def test_batch_autotune_and_mixed_precision(cases_mod):
         fo = _interior_f(c, o.frd())
         assert np.abs(fb - fo).max() < 5e-5 * np.abs(fo).max(), k
         assert np.isfinite(r[k]["max_rms"])
+
+
+def test_batch_outside_the_batched_kernels_keeps_per_instance_launches(cases_mod):
+    """WENO3 instances are not covered by the batched kernels: the batch
+    captures one graph branch per instance and still matches standalone
+    contexts bit for bit."""
+    from hyb_gb300 import abi
+    cl = [cases_mod.couette_small(ncy=32, nvx=12, nvy=12, kn=0.5, uw=0.3, dt=0.02, scheme=3),
+          cases_mod.couette_small(ncy=64, nvx=10, nvy=10, kn=0.05, uw=0.1, dt=0.01, scheme=3)]
+    b = abi.Batch(cl, precision=0)
+    b.init_maxwellian()
+    rb = b.step(4)
+    for k, c in enumerate(cl):
+        s = abi.Solver(c, precision=0)
+        s.init_maxwellian()
+        rs = s.step(4)
+        assert np.array_equal(b.instance(k).download_f(), s.download_f()), k
+        assert rb[k]["max_rms"] == rs["max_rms"], k
