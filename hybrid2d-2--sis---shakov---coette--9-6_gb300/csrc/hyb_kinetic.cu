@@ -450,16 +450,18 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
         for (int c = 0; c < MC; c++) store_part<real>(M.part, ((size_t)slice * NM + q) * ncell + cell0 + c, ks[q][c]);
 }
 
-template <typename real, int MC, int NM>
-__global__ void __launch_bounds__(512, 1) k_moments_part(MomArgs M) {
+// NARROW: CTAs of at most 256 threads, three per SM (80 registers); FP32
+// rows of up to 512 cells take it, wider rows and FP64 keep 512 threads
+template <typename real, int MC, int NM, bool NARROW>
+__global__ void __launch_bounds__(NARROW ? 256 : 512, NARROW ? 3 : 1) k_moments_part(MomArgs M) {
     moments_body<real, MC, NM>(M, blockIdx.x, blockIdx.y);
 }
 
 // many contexts in one launch: CTA i takes march row work[i].y and velocity
 // slice work[i].z of context work[i].x
-template <typename real, int MC, int NM>
-__global__ void __launch_bounds__(512, 1) k_moments_part_batch(const MomArgs *__restrict__ args,
-                                                               const int4 *__restrict__ work) {
+template <typename real, int MC, int NM, bool NARROW>
+__global__ void __launch_bounds__(NARROW ? 256 : 512, NARROW ? 3 : 1)
+    k_moments_part_batch(const MomArgs *__restrict__ args, const int4 *__restrict__ work) {
     __shared__ MomArgs Ms;
     const int4 w = work[blockIdx.x];
     if (threadIdx.x == 0) Ms = args[w.x];
@@ -798,15 +800,24 @@ int moments_slices(const hyb_ctx *ctx) {
     return vs;
 }
 
-template <typename real, int MC, int NM>
-static void launch_mom(hyb_ctx *ctx, const MomArgs &M, dim3 grd, int tpv, size_t smem) {
+template <typename real, int MC, int NM, bool NARROW>
+static void launch_mom_bounds(hyb_ctx *ctx, const MomArgs &M, dim3 grd, int tpv, size_t smem) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_moments_part<real, MC, NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_moments_part<real, MC, NM, NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              227 * 1024);
         attr = true;
     }
-    k_moments_part<real, MC, NM><<<grd, tpv, smem, ctx->stream>>>(M);
+    k_moments_part<real, MC, NM, NARROW><<<grd, tpv, smem, ctx->stream>>>(M);
+}
+
+template <typename real>
+static constexpr bool mom_narrow_ok() { return sizeof(real) == 4; }
+
+template <typename real, int MC, int NM>
+static void launch_mom(hyb_ctx *ctx, const MomArgs &M, dim3 grd, int tpv, size_t smem) {
+    if (mom_narrow_ok<real>() && tpv <= 256) launch_mom_bounds<real, MC, NM, mom_narrow_ok<real>()>(ctx, M, grd, tpv, smem);
+    else launch_mom_bounds<real, MC, NM, false>(ctx, M, grd, tpv, smem);
 }
 
 // lanes per cell of the slice sums: enough for the slices, while the grid
@@ -1026,18 +1037,26 @@ int mom_arg_fill(hyb_ctx *ctx, const void *f, void *dst, int *mc, int *tpv, size
     return HYB_OK;
 }
 
-template <typename real, int MC, int NM>
-static int mom_part_batch_one(const MomArgs *args, const int4 *work, int nwork, int tpv, size_t smem,
-                              cudaStream_t s) {
+template <typename real, int MC, int NM, bool NARROW>
+static int mom_part_batch_bounds(const MomArgs *args, const int4 *work, int nwork, int tpv, size_t smem,
+                                 cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_moments_part_batch<real, MC, NM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             227 * 1024 - 1024);
+        cudaFuncSetAttribute(k_moments_part_batch<real, MC, NM, NARROW>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 1024);
         attr = true;
     }
     if (nwork <= 0) return HYB_OK;   // attributes only (before a capture)
-    k_moments_part_batch<real, MC, NM><<<nwork, tpv, smem, s>>>(args, work);
+    k_moments_part_batch<real, MC, NM, NARROW><<<nwork, tpv, smem, s>>>(args, work);
     return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+template <typename real, int MC, int NM>
+static int mom_part_batch_one(const MomArgs *args, const int4 *work, int nwork, int tpv, size_t smem,
+                              cudaStream_t s) {
+    if (mom_narrow_ok<real>() && tpv <= 256)
+        return mom_part_batch_bounds<real, MC, NM, mom_narrow_ok<real>()>(args, work, nwork, tpv, smem, s);
+    return mom_part_batch_bounds<real, MC, NM, false>(args, work, nwork, tpv, smem, s);
 }
 
 template <int NM>
