@@ -272,9 +272,12 @@ int hyb_autotune(hyb_ctx *ctx, int reps, int *cpt, int *vpb);
  * runs one case per process) ---------------------------------------------- */
 /* n independent cases of any mesh / velocity-grid size on one device and one
  * precision.  One outer iteration of all instances is captured into one CUDA
- * graph with an independent branch per instance; hyb_batch_step launches it
- * once per iteration.  res (n entries, may be NULL) receives each instance's
- * DETFP_res after the last iteration. */
+ * graph; hyb_batch_step launches it once per iteration.  Instances of one
+ * sweep launch shape share one launch per kernel (one graph branch per
+ * shape group); batches the batched kernels do not cover (schemes other than
+ * NND) get one branch per instance.  Either way each instance computes
+ * exactly what a standalone context computes.  res (n entries, may be NULL)
+ * receives each instance's DETFP_res after the last iteration. */
 typedef struct hyb_batch hyb_batch;
 int hyb_batch_create(int n, const hyb_mesh *meshes, const hyb_vgrid *vgrids,
                      const hyb_params *params, hyb_batch **out);
@@ -284,7 +287,10 @@ int hyb_batch_size(const hyb_batch *b, int *n);
 /* The context of instance k (for state transfer and moments). */
 int hyb_batch_instance(hyb_batch *b, int k, hyb_ctx **ctx);
 int hyb_batch_init_maxwellian(hyb_batch *b, double rho, double u, double v, double t);
-/* hyb_autotune on every instance; the captured graphs are rebuilt. */
+/* hyb_autotune on the first instance of each mesh and velocity-grid size,
+ * whose shape the others of that size take; the captured graphs are rebuilt.
+ * A shape set on one instance's context directly takes effect when the
+ * graphs are next rebuilt (by this call). */
 int hyb_batch_autotune(hyb_batch *b, int reps);
 int hyb_batch_step(hyb_batch *b, int n_iter, hyb_residual *res);
 /* Milliseconds of the last hyb_batch_step (CUDA events around the graph
