@@ -120,6 +120,15 @@ __device__ __forceinline__ real flux_whi(real s, real f1, real f2, real f3) {
     else return s > real(0) ? s * (f2 + real(0.5) * fminmd(f1 - f2, f2 - f3)) : s * (f1 - real(0.5) * (f1 - f2));
 }
 
+// After a wait ran out at row `stop`: rows stop+3 .. stop+RING-4 (all
+// within 1..Nb, so each is a real copy) were issued and never waited for;
+// wait (bounded) for each before the CTA leaves.  Out of line, so that the
+// row loop's register allocation does not carry this path.
+static __device__ __noinline__ void sweep_drain(uint64_t *bars, int stop, int Nb) {
+    for (int bp = stop + 3; bp <= Nb && bp <= stop + RING - 4; bp++)
+        mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1));
+}
+
 // the sweep of the CTA's velocity block vblk (velocities vblk * vpb + g)
 template <typename real, int CPT, bool UNI, int SCHEME>
 __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
@@ -454,6 +463,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         }
         if (__syncthreads_or(timeout)) {
             if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
+            if (producer) sweep_drain(bars, b, Nb);
             return;
         }
         // every thread is past this row's reads, so the slot of row b-3 is free
