@@ -351,8 +351,9 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
             bulk_g2s(dst + PA, src + rs, row_bytes, &full[k]);
         }
     };
+    int issued = 0;   // slots issued (thread 0)
     if (t == 0)
-        for (int n = 0; n < MOM_NST - 1 && n < nslot; n++) issue(n);
+        for (; issued < MOM_NST - 1 && issued < nslot; issued++) issue(issued);
     // plain sums over blocks of 8 velocities, compensated sums of the blocks
     KahanAcc<real> ks[NM][MC];
     real blk[NM][MC];
@@ -363,17 +364,20 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
             ks[q][c].zero();
             blk[q][c] = real(0);
         }
+    // A wait that runs out clears the thread's ok: it stops waiting (and
+    // thread 0 stops issuing), and every thread still runs each slot's warp
+    // sync and empty arrival, so no lane leaves a warp barrier early.
     bool ok = true;
-    for (int n = 0; n < nslot && ok; n++) {
+    for (int n = 0; n < nslot; n++) {
         const int k = n % MOM_NST;
         // refill the slot freed by slot n-1 with slot n+NST-1
-        if (t == 0 && n + MOM_NST - 1 < nslot) {
+        if (t == 0 && ok && n + MOM_NST - 1 < nslot) {
             if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
                 ok = false;
             else
-                issue(n + MOM_NST - 1);
+                issue(issued++);
         }
-        if (!mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
+        if (ok && !mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
         if (act && ok) {
             const int cnt = min(VPS, nloc - n * VPS);
             const real *gs = stage + (size_t)k * VPS * 2 * PA + (a0 - 1);
@@ -438,7 +442,12 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
         if (lane == 0) mbar_arrive(&empty[k]);
     }
     if (__syncthreads_or(!ok)) {
-        if (t == 0) atomicExch(M.err, HYB_ERR_TIMEOUT);
+        if (t == 0) {
+            atomicExch(M.err, HYB_ERR_TIMEOUT);
+            // the last NST issued slots may still be in flight: wait (bounded)
+            for (int n = issued > MOM_NST ? issued - MOM_NST : 0; n < issued; n++)
+                mbar_wait_bounded(&full[n % MOM_NST], (uint32_t)((n / MOM_NST) & 1));
+        }
         return;
     }
     if (!act) return;
