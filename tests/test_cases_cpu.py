@@ -1,0 +1,76 @@
+"""The benchmark workloads' set-up (host side, no GPU).
+
+The named configurations carry the sizes and physical parameters of the
+workloads they stand for. The batch manifest is seeded, stays within its
+stated ranges and has every mesh and velocity-grid size. The bench's dt
+rule keeps dt / dy, and with it the kinetic CFL, equal over the instances.
+The wall tables of the sine case follow T_w(x) = 1 + 0.1 sin(2 pi x) at the
+face centres.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def cm(pkg):
+    from hyb_gb300 import cases
+    return cases
+
+
+def test_named_configurations(cm):
+    from hyb_gb300 import hyb_types as T
+    s = cm.couette_small()
+    assert (s.ncx, s.ncy, s.nvx, s.nvy, s.vmax, s.kn, s.uw) == (4, 64, 32, 32, 5.0, 0.1, 0.2)
+    assert s.t_bottom == s.t_top == 1.0 and s.precision == T.HYB_PREC_FP64
+    g = cm.couette_large()
+    assert (g.ncx, g.ncy, g.nvx, g.nvy, g.vmax, g.kn, g.uw) == (128, 512, 64, 64, 6.0, 0.01, 0.5)
+    assert (g.t_bottom, g.t_top) == (1.0, 1.2) and g.precision == T.HYB_PREC_MIXED
+    assert g.cells * g.nv == 268_435_456
+    w = cm.couette_sine()
+    assert (w.ncx, w.ncy, w.nvx, w.nvy, w.vmax, w.kn, w.uw, w.t_pert) == (512, 512, 48, 48, 5.0, 0.005, 0.3, 0.1)
+    assert w.cells * w.nv == 603_979_776      # "about 600 M" cell-velocities, 1.2 G values with G and H
+
+
+def test_gas_and_collision_parameters(cm):
+    p = cm.couette_small().params()
+    assert p.cpr == pytest.approx((1.0 - 2.0 / 3.0) / 2.5)     # Shakhov 1 - Pr over 5/2
+    assert p.x1s == pytest.approx(0.5)                          # hard sphere, omega 0.5
+    assert p.cfc == pytest.approx(math.sqrt(math.pi) / (2.0 * 0.1))
+
+
+def test_sine_wall_temperature(cm):
+    c = cm.couette_sine(ncx=16, ncy=8, nvx=8, nvy=8)
+    _, _, t = c.walls()
+    xc = (np.arange(16) + 0.5) / 16
+    ref = 1.0 + 0.1 * np.sin(2.0 * np.pi * xc)
+    assert np.allclose(t[1], ref) and np.allclose(t[3], ref)
+
+
+def test_batch_manifest_is_seeded_and_in_range(cm):
+    a, b = cm.batch_manifest(), cm.batch_manifest()
+    assert a == b and len(a) == 256
+    assert a != cm.batch_manifest(seed=1)
+    sizes = set()
+    for d in a:
+        assert d["ncx"] == 4 and d["ncy"] in (32, 64, 128, 256)
+        assert d["nvx"] == d["nvy"] and d["nvx"] in (24, 32, 48, 64)
+        assert d["vmax"] == (5.0 if d["nvx"] < 48 else 6.0)
+        assert 1e-3 <= d["kn"] <= 10.0
+        assert 0.05 <= d["uw"] <= 0.8
+        assert d["t_bottom"] == 1.0 and 0.8 <= d["t_top"] <= 1.5
+        sizes.add((d["ncy"], d["nvx"]))
+    assert len(sizes) == 16                    # every mesh x velocity-grid size occurs
+    kn = np.log10([d["kn"] for d in a])
+    assert kn.min() < -2.5 and kn.max() > 0.5  # log-uniform over four decades
+
+
+def test_bench_batch_cases_keep_the_kinetic_cfl(cm):
+    # bench.py scales dt with the cell size, so that dt / dy (and with it the
+    # kinetic CFL of a velocity range) is the same for every instance
+    import bench
+    cl = bench.batch_cases()
+    assert len(cl) == 256 and all(c.precision == 1 for c in cl)
+    ratios = {round(c.dt * c.ncy / c.ly, 12) for c in cl}
+    assert ratios == {0.64}
