@@ -195,9 +195,11 @@ int hyb_download_hoq(hyb_ctx *ctx, double *hot, double *hoq);
 
 /* ---- the iteration (Hybrid_Time_advance_LU_SGS, Hybrid_Sub.f90:4-160) --- */
 /* n_iter outer iterations; each runs the boundary conditions, the kinetic
- * LU-SGS step, the moments, the wall moments, Convert_NS and (when enabled)
- * the GSIS synthetic solve.  If out != NULL the residual of the last
- * iteration (DETFP_res) is written to it. */
+ * LU-SGS step, the moments, the wall moments and (when enabled) Convert_NS
+ * and the GSIS synthetic solve.  Without GSIS, Convert_NS feeds only the NS /
+ * HoT fields a caller downloads, so it runs on the call's last iteration
+ * only; the state after the call is the same.  If out != NULL the residual
+ * of the last iteration (DETFP_res) is written to it. */
 int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out);
 /* The same stages one at a time, named after the reference subroutines. */
 int hyb_phy_boundary(hyb_ctx *ctx);          /* GKUA_Phy_boundary          */
