@@ -359,7 +359,7 @@ def run_gb300(args, world, rank, local):
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "alg_bytes_per_cell_velocity": b_alg,
                      "ms_per_launch": per_launch_s * 1000.0},
-        "survey_basis": {"bytes_per_unit": 40, "note": "whole kinetic step on the 5*NRD*s definition",
+        "whole_step_basis": {"bytes_per_unit": 40, "note": "whole kinetic step on the 5*NRD*s definition",
                          "achieved_gbs": 40.0 * units / (ms / 1000.0) / 1e9 / world,
                          "frac": 40.0 * units / (ms / 1000.0) / 1e9 / world / peak},
         "stage_ms_per_step": stage_ms,
