@@ -598,14 +598,18 @@ __device__ __forceinline__ void residual_finish_body(const MomArgs &M, int lpc, 
         mx[q] = fabs(x);
         sq[q] = x * x;
     }
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            mx[q] = nanmax(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], off));
-            sq[q] += __shfl_xor_sync(0xffffffffu, sq[q], off);
-        }
-    __shared__ double wm[8][4], ws[8][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the cells' sums sit in threads 0 .. blockDim.x / lpc - 1 (slice_fold):
+    // a warp above them holds zeros only, which its reduction would return
+    // unchanged, so it skips the FP64 shuffles
+    if (warp * 32 < (int)blockDim.x / lpc)
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                mx[q] = nanmax(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], off));
+                sq[q] += __shfl_xor_sync(0xffffffffu, sq[q], off);
+            }
+    __shared__ double wm[8][4], ws[8][4];
     if (lane == 0)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
