@@ -129,6 +129,8 @@ class Case:
     nc_rule: int = 1         # the reference NewtonCotes pattern (GKUA_DETFP.f90:419-444)
     quadrature: str = "nc"   # "nc": Newton-Cotes on [-vmax, vmax]; "gh": Gauss-Hermite (vmax unused)
     stretch: float = 0.0     # >0: tanh clustering of the y nodes towards both plates
+    sweep_order: int = T.HYB_SWEEP_REFERENCE   # order of the kinetic implicit step
+    mass_pin: int = 0        # 1: hold the total mass of f at its initial value
     extra: dict = field(default_factory=dict)
 
     # ---- derived arrays -------------------------------------------------
@@ -200,6 +202,8 @@ class Case:
         p.re = cfc * ma * math.sqrt(2.0 * self.gamma)
         p.omega_ns = self.omega
         p.device = 0
+        p.sweep_order = self.sweep_order
+        p.mass_pin = self.mass_pin
         return p
 
     def c_structs(self):

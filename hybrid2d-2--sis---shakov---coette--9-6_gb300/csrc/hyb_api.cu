@@ -154,6 +154,7 @@ void free_all(hyb_ctx *c) {
     F(c->d_eqp); F(c->d_vol); F(c->d_gA1); F(c->d_gA2); F(c->d_gB1); F(c->d_gB2);
     F(c->d_vx); F(c->d_vy); F(c->d_w); F(c->d_S); F(c->d_CF); F(c->d_wall);
     F(c->d_x1); F(c->d_y1); F(c->d_hot); F(c->d_resid); F(c->d_err); F(c->d_mpart); F(c->d_stage);
+    F(c->d_volc); F(c->d_mass);
     if (c->h_resid) cudaFreeHost(c->h_resid);
     if (c->h_wall) cudaFreeHost(c->h_wall);
     for (auto ev : c->prof_ev) cudaEventDestroy(ev);
@@ -213,6 +214,8 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     }
     if ((m->bc[0] == HYB_BC_PERIODIC) != (m->bc[2] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
     if ((m->bc[1] == HYB_BC_PERIODIC) != (m->bc[3] == HYB_BC_PERIODIC)) return HYB_ERR_INVALID;
+    if (p->sweep_order != HYB_SWEEP_REFERENCE && p->sweep_order != HYB_SWEEP_UPWIND) return HYB_ERR_INVALID;
+    if (p->mass_pin != 0 && p->mass_pin != 1) return HYB_ERR_INVALID;
     SweepLayout lay;
     if (!sweep_layout(m->nx - 1, m->ny - 1, &lay)) return HYB_ERR_UNSUPPORTED;
     int ndev = 0;
@@ -301,6 +304,8 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     if (rc == HYB_OK) ALLOC(c->d_resid, (16 + 8 * nblk) * sizeof(double));
     if (rc == HYB_OK) ALLOC(c->d_err, sizeof(int));
     if (rc == HYB_OK) ALLOC(c->d_mpart, (size_t)hyb::moments_slices(c) * 10 * ncell * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_volc, (size_t)ncx * ncy * sizeof(double));
+    if (rc == HYB_OK) ALLOC(c->d_mass, 2 * sizeof(double));
 #undef ALLOC
     if (rc == HYB_OK && cudaMallocHost((void **)&c->h_resid, 16 * sizeof(double)) != cudaSuccess) rc = HYB_ERR_NOMEM;
     if (rc == HYB_OK && maxfc > 4096) { rc = HYB_ERR_UNSUPPORTED; c->last_error = "wall longer than 4096 cells"; }
@@ -394,6 +399,12 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         if (e == cudaSuccess) e = cudaMemcpy(c->d_wall, wall.data(), wall.size() * sizeof(double), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(c->d_x1, c->x1.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(c->d_y1, c->y1.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            std::vector<double> vc((size_t)ncx * ncy);
+            for (int j = 1; j <= ncy; j++)
+                for (int i = 1; i <= ncx; i++) vc[(size_t)(i - 1) + (size_t)ncx * (j - 1)] = c->vol[MI(nx, i, j)];
+            e = cudaMemcpy(c->d_volc, vc.data(), vc.size() * sizeof(double), cudaMemcpyHostToDevice);
+        }
         if (e != cudaSuccess) { c->last_error = cudaGetErrorString(e); r2 = HYB_ERR_CUDA; }
     }
     if (!r2 && cudaStreamSynchronize(c->stream) != cudaSuccess) r2 = HYB_ERR_CUDA;
@@ -401,6 +412,12 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         free_all(c);
         delete c;
         return r2;
+    }
+    // the upwind order mirrors whole rows with a uniform face speed per axis
+    if (p->sweep_order == HYB_SWEEP_UPWIND && !c->uniform) {
+        free_all(c);
+        delete c;
+        return HYB_ERR_UNSUPPORTED;
     }
     c->gsis.enable = 0;
     // launch-shape override, "cpt,vpb,minb"
@@ -485,6 +502,7 @@ int hyb_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t) 
     if (!rc) rc = hyb_phy_boundary(ctx);
     if (!rc) rc = hyb_detfp(ctx);
     if (!rc) rc = hyb_convert_ns(ctx);
+    if (!rc) rc = hyb::launch_total_mass(ctx, 0);
     if (!rc) {
         HYB_CK(cudaStreamSynchronize(ctx->stream));
         ctx->rhs_valid = 0;
@@ -648,6 +666,7 @@ int hyb_upload_f(hyb_ctx *ctx, const double *frd) {
     rc = hyb_phy_boundary(ctx);
     if (!rc) rc = hyb_detfp(ctx);
     if (!rc) rc = hyb_convert_ns(ctx);
+    if (!rc) rc = hyb::launch_total_mass(ctx, 0);
     if (!rc) HYB_CK(cudaStreamSynchronize(ctx->stream));
     ctx->rhs_valid = 0;
     return rc;

@@ -506,6 +506,11 @@ int hyb_batch_create(int n, const hyb_mesh *meshes, const hyb_vgrid *vgrids, con
             hyb_batch_destroy(b);
             return HYB_ERR_INVALID;
         }
+        // the batched graphs carry the reference order without a mass scale
+        if (params[k].sweep_order != HYB_SWEEP_REFERENCE || params[k].mass_pin) {
+            hyb_batch_destroy(b);
+            return HYB_ERR_UNSUPPORTED;
+        }
         hyb_ctx *c = nullptr;
         int rc = hyb_create(&meshes[k], &vgrids[k], &params[k], &c);
         if (rc) {

@@ -62,6 +62,9 @@ struct KinArgs {
     int scan_is_j;         // 1: scan axis = reference j
     real dt;
     int *err;              // device error word
+    // mass_pin: the updated f is multiplied by *mscale (m0 / M of the state
+    // the step starts from); nullptr: no scale
+    const double *mscale;
 };
 
 }  // namespace hyb
@@ -101,6 +104,8 @@ struct hyb_ctx {
     double *d_resid;                       // residual partials / result
     double *d_mpart;                       // moment partial sums [VS][10][Nb*PA]
     double *d_stage;                       // host-layout staging of downloads (first use)
+    double *d_volc;                        // cell volumes, interior cells, i fastest (FP64)
+    double *d_mass;                        // [0] total mass m0 at set-up, [1] scale m0 / M
     int *d_err;
     double *h_resid;                       // pinned
     int rhs_valid;
@@ -181,6 +186,9 @@ int launch_rhs_moments(hyb_ctx *ctx, double *cellm);
 int residual_blocks(const hyb_ctx *ctx);   // blocks of the residual partials
 int launch_hoq(hyb_ctx *ctx, double *out);   // HOT_GKUA(1:6), HOQ_GKUA(1:3), [9][(nx+3)(ny+3)]
 int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t);
+// total mass sum(vol rho) over the interior cells from S: mode 0 stores it as
+// m0, mode 1 stores the mass_pin scale m0 / M
+int launch_total_mass(hyb_ctx *ctx, int mode);
 int launch_convert_ns(hyb_ctx *ctx);
 int ns_create(hyb_ctx *ctx);
 void ns_destroy(hyb_ctx *ctx);

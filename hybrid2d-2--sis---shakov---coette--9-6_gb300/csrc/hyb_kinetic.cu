@@ -980,6 +980,43 @@ int launch_residual(hyb_ctx *ctx, hyb_residual *out) {
     return HYB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// total mass sum(vol rho) over the interior cells (mass_pin).  One CTA: each
+// thread adds its cells k = tid, tid + 1024, ... in order, then a fixed-order
+// tree fold.  mode 0 stores the sum as m0 in mass[0], mode 1 stores the
+// scale m0 / M in mass[1].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_total_mass(const double *__restrict__ S, const double *__restrict__ volc,
+                                                     int nx, int ny, int mode, double *__restrict__ mass) {
+    __shared__ double red[1024];
+    const int ncx = nx - 1, n = (nx - 1) * (ny - 1);
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int i = k % ncx + 1, j = k / ncx + 1;
+        acc += volc[k] * S[hyb_c2(nx, i, j)];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (mode == 0) {
+            mass[0] = red[0];
+            mass[1] = 1.0;
+        } else {
+            mass[1] = mass[0] / red[0];
+        }
+    }
+}
+
+int launch_total_mass(hyb_ctx *ctx, int mode) {
+    k_total_mass<<<1, 1024, 0, ctx->stream>>>(ctx->d_S, ctx->d_volc, ctx->nx, ctx->ny, mode, ctx->d_mass);
+    ctx->launches++;
+    return check_err(ctx, "k_total_mass");
+}
+
 int launch_init_maxwellian(hyb_ctx *ctx, double rho, double u, double v, double t) {
     int grid = 152 * 8;
     if (ctx->precision == HYB_PREC_FP64)

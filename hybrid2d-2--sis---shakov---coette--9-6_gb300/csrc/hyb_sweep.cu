@@ -73,6 +73,7 @@ static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.scan_is_j = ctx->scan_is_j;
     A.dt = (real)ctx->prm.dt;
     A.err = ctx->d_err;
+    A.mscale = (ctx->prm.mass_pin && store_rhs != 2) ? ctx->d_mass + 1 : nullptr;
 }
 
 static int sweep_dispatch(hyb_ctx *ctx, int store_rhs, bool launch) {
@@ -92,8 +93,15 @@ void sweep_args_f32(hyb_ctx *ctx, int store_rhs, KinArgs<float> *A) { fill_args<
 void sweep_args_f64(hyb_ctx *ctx, int store_rhs, KinArgs<double> *A) { fill_args<double>(ctx, store_rhs, *A); }
 
 // store_rhs: 0 no RHS store, 1 RHS to d_rhs with the update, 2 RHS only
-// (to d_rhs_gsis, f unchanged)
-int launch_sweep(hyb_ctx *ctx, int store_rhs) { return sweep_dispatch(ctx, store_rhs, true); }
+// (to d_rhs_gsis, f unchanged).  With mass_pin the scale m0 / M of the
+// current moments is formed first (the update multiplies by it).
+int launch_sweep(hyb_ctx *ctx, int store_rhs) {
+    if (ctx->prm.mass_pin && store_rhs != 2) {
+        int rc = launch_total_mass(ctx, 1);
+        if (rc) return rc;
+    }
+    return sweep_dispatch(ctx, store_rhs, true);
+}
 
 // sets the shared-memory attribute of the kernel the current shape selects
 int sweep_prepare(hyb_ctx *ctx) { return sweep_dispatch(ctx, 0, false); }

@@ -21,6 +21,16 @@
 // sweep and neither dF nor the RHS is written to memory (the RHS only when a
 // residual is requested).  The seam of a periodic face is explicit in both
 // sweeps, as the reference's zero FRD00 ghosts make every block face.
+//
+// Upwind order (UPW, HYB_SWEEP_UPWIND, uniform meshes).  A velocity whose
+// scan-face speed is negative is swept with the scan axis mirrored (logical
+// cell a is physical cell Na+1-a), one whose march-face speed is negative
+// with the march axis mirrored (logical row b is physical row Nb+1-b).  In
+// the mirrored frame both speeds are >= 0, so the forward recurrence is the
+// exact first-order upwind solve and the backward step adds nothing.  The
+// face fluxes are the physical ones: each formula satisfies
+// flux(-s, mirrored stencil) = -flux(s, stencil), and the negated face normal
+// turns that back into the physical divergence.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -130,8 +140,9 @@ static __device__ __noinline__ void sweep_drain(uint64_t *bars, int stop, int Nb
 }
 
 // the sweep of the CTA's velocity block vblk (velocities vblk * vpb + g)
-template <typename real, int CPT, bool UNI, int SCHEME>
+template <typename real, int CPT, bool UNI, int SCHEME, bool UPW = false>
 __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
+    static_assert(!UPW || UNI, "the upwind order is built for uniform meshes");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int PA = A.PA, Na = A.Na, Nb = A.Nb;
     const int TPV = PA / CPT;
@@ -157,9 +168,57 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     const size_t rstride = (size_t)Nb * PA;
     const uint32_t row_bytes = (uint32_t)(PA * sizeof(real));
 
+    // ---- velocity, face speeds and the frame of the sweep ---------------------
+    const int iv = vok ? v % A.nvi : 0, jv = vok ? v / A.nvi : 0;
+    const real vx = vok ? (real)A.vx[iv] : real(0), vy = vok ? (real)A.vy[jv] : real(0);
+    const real dt = A.dt;
+    const int PA1 = PA + 1;
+    real sA_u = 0, sB_u = 0, vol_u = 1, ivol_u = 1, abase_u = 0;
+    if (UNI) {
+        sA_u = vx * A.gA1[0] + vy * A.gA2[0];
+        sB_u = vx * A.gB1[0] + vy * A.gB2[0];
+        vol_u = A.vol[0];
+        ivol_u = real(1) / vol_u;
+        abase_u = vol_u / dt + (posp(sA_u) - negp(sA_u) + posp(sB_u) - negp(sB_u));
+    }
+    // mirrored scan / march axis of this group (upwind order only)
+    const bool ra = UPW && sA_u < real(0), rb = UPW && sB_u < real(0);
+    if (ra) sA_u = -sA_u;
+    if (rb) sB_u = -sB_u;
+    // physical 0-based scan index of logical cell a; physical row of logical
+    // row b (1..Nb)
+    auto pa = [&](int a) -> int { return ra ? Na - a : a - 1; };
+    auto prow = [&](int b) -> int { return rb ? Nb + 1 - b : b; };
+    // the CPT logical cells of this thread from / to a row of physical cells
+    const int pa0 = ra ? Na - a0 - CPT + 1 : a0 - 1;   // first physical index of the chunk
+    auto ldc = [&](const real *row, real *o) {
+        if (!ra) {
+            Vec<real, CPT>::ld(row + pa0, o);
+        } else {
+            real t[CPT];
+            Vec<real, CPT>::ld(row + pa0, t);
+#pragma unroll
+            for (int k = 0; k < CPT; k++) o[k] = t[CPT - 1 - k];
+        }
+    };
+    auto stc = [&](real *row, const real *o) {
+        if (!ra) {
+            Vec<real, CPT>::st(row + pa0, o);
+        } else {
+            real t[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) t[k] = o[CPT - 1 - k];
+            Vec<real, CPT>::st(row + pa0, t);
+        }
+    };
+    // wall slots of the logical low / high ends
+    const real *fw_alo = ra ? A.fw_ahi : A.fw_alo, *fw_ahi = ra ? A.fw_alo : A.fw_ahi;
+    const real *fw_blo = rb ? A.fw_bhi : A.fw_blo, *fw_bhi = rb ? A.fw_blo : A.fw_bhi;
+
+    // physical row held by logical ring row bp (0: none)
     auto phys_row = [&](int bp) -> int {
-        if (bp >= 1 && bp <= Nb) return bp;
-        if (perB && bp <= 0) return bp + Nb;
+        if (bp >= 1 && bp <= Nb) return prow(bp);
+        if (perB && bp <= 0) return prow(bp + Nb);
         return 0;
     };
     auto issue_row = [&](int bp) {
@@ -186,7 +245,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         if (perB) {
             for (int w = 0; w < 2; w++) {
                 mbar_arrive_expect_tx(&bars[RING + w], 2 * row_bytes);
-                const real *src = A.f + vrow0 + (size_t)w * PA;
+                const real *src = A.f + vrow0 + (size_t)(prow(w + 1) - 1) * PA;
                 bulk_g2s(wrap + (size_t)w * 2 * PA, src, row_bytes, &bars[RING + w]);
                 bulk_g2s(wrap + (size_t)w * 2 * PA + PA, src + rstride, row_bytes, &bars[RING + w]);
             }
@@ -211,26 +270,13 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     // wall axis they are only read by the standard faces, which never reach
     // outside 1..Na)
     auto wrapA = [&](int c) -> int {
-        if (perA) return ((c - 1 + 2 * Na) % Na);
-        return c < 1 ? 0 : (c > Na ? Na - 1 : c - 1);
+        const int l = perA ? ((c - 1 + 2 * Na) % Na) : (c < 1 ? 0 : (c > Na ? Na - 1 : c - 1));
+        return ra ? Na - 1 - l : l;
     };
     const int hm2 = wrapA(a0 - 2), hm1 = wrapA(a0 - 1), hp0 = wrapA(a0 + CPT), hp1 = wrapA(a0 + CPT + 1);
     // a thread away from both wall ends of the scan axis has standard faces only
     const bool edgeA = !perA && (a0 <= 2 || a0 + CPT >= Na);
 
-    // ---- velocity and geometry ----------------------------------------------
-    const int iv = vok ? v % A.nvi : 0, jv = vok ? v / A.nvi : 0;
-    const real vx = vok ? (real)A.vx[iv] : real(0), vy = vok ? (real)A.vy[jv] : real(0);
-    const real dt = A.dt;
-    const int PA1 = PA + 1;
-    real sA_u = 0, sB_u = 0, vol_u = 1, ivol_u = 1, abase_u = 0;
-    if (UNI) {
-        sA_u = vx * A.gA1[0] + vy * A.gA2[0];
-        sB_u = vx * A.gB1[0] + vy * A.gB2[0];
-        vol_u = A.vol[0];
-        ivol_u = real(1) / vol_u;
-        abase_u = vol_u / dt + (posp(sA_u) - negp(sA_u) + posp(sB_u) - negp(sB_u));
-    }
     // the scan is needed only when some group of the CTA has a positive
     // scan-face speed somewhere (always assumed on non-uniform meshes)
     const bool need_scan = UNI ? (__syncthreads_or(vok && sA_u > real(0)) != 0) : true;
@@ -246,9 +292,9 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     };
     // march-axis face flux at face q for cell a, component r, wall faces only
     auto fluxB_wall = [&](int q, int a, int r, real sp) -> real {
-        const size_t o = (size_t)r * PA + (a - 1);
-        if (q == 1) return sp * A.fw_blo[((size_t)v * 2 + r) * PA + (a - 1)];
-        if (q == Nb + 1) return sp * A.fw_bhi[((size_t)v * 2 + r) * PA + (a - 1)];
+        const size_t o = (size_t)r * PA + pa(a);
+        if (q == 1) return sp * fw_blo[((size_t)v * 2 + r) * PA + pa(a)];
+        if (q == Nb + 1) return sp * fw_bhi[((size_t)v * 2 + r) * PA + pa(a)];
         if (q == 2) return flux_wlo<SCHEME>(sp, rowp(1)[o], rowp(2)[o], rowp(3)[o]);
         if (q == Nb) return flux_whi<SCHEME>(sp, rowp(Nb)[o], rowp(Nb - 1)[o], rowp(Nb - 2)[o]);
         return flux_std<SCHEME>(sp, rowp(q - 2)[o], rowp(q - 1)[o], rowp(q)[o], rowp(q + 1)[o]);
@@ -267,6 +313,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         sAhp[k] = sBl[k] = FBl_G[k] = FBl_H[k] = real(0);
     }
     const real fl = Consts<real>::floor_();
+    const real msc = A.mscale ? (real)*A.mscale : real(1);
     const real *ep = A.eqp;
     const size_t ncell = (size_t)Nb * PA;
 
@@ -282,7 +329,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         for (int k = 0; k < CPT; k++) {
             sBl[k] = speedB(1, a0 + k);
             if (perB) {
-                const size_t o = a0 - 1 + k;
+                const size_t o = pa(a0 + k);
                 FBl_G[k] = flux_std<SCHEME>(sBl[k], rowp(-1)[o], rowp(0)[o], rowp(1)[o], rowp(2)[o]);
                 FBl_H[k] = flux_std<SCHEME>(sBl[k], rowp(-1)[PA + o], rowp(0)[PA + o], rowp(1)[PA + o],
                                             rowp(2)[PA + o]);
@@ -304,8 +351,8 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         if (act) {
             const real *rm = rowp(b - 1), *r0 = rowp(b), *rp = rowp(b + 1), *rq = rowp(b + 2);
             real f0[CPT], f1[CPT];
-            Vec<real, CPT>::ld(r0 + (a0 - 1), f0);
-            Vec<real, CPT>::ld(r0 + PA + (a0 - 1), f1);
+            ldc(r0, f0);
+            ldc(r0 + PA, f1);
             // scan-axis window f(a0-2 .. a0+CPT+1)
             real w0[CPT + 4], w1[CPT + 4];
             w0[0] = r0[hm2]; w0[1] = r0[hm1]; w0[CPT + 2] = r0[hp0]; w0[CPT + 3] = r0[hp1];
@@ -323,17 +370,17 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
                     FA_G[m] = flux_std<SCHEME>(s, w0[m], w0[m + 1], w0[m + 2], w0[m + 3]);
                     FA_H[m] = flux_std<SCHEME>(s, w1[m], w1[m + 1], w1[m + 2], w1[m + 3]);
                 } else if (q == 1) {
-                    FA_G[m] = s * A.fw_alo[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[m] = s * A.fw_alo[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[m] = s * fw_alo[((size_t)v * 2 + 0) * Nb + (prow(b) - 1)];
+                    FA_H[m] = s * fw_alo[((size_t)v * 2 + 1) * Nb + (prow(b) - 1)];
                 } else if (q == Na + 1) {
-                    FA_G[m] = s * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[m] = s * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[m] = s * fw_ahi[((size_t)v * 2 + 0) * Nb + (prow(b) - 1)];
+                    FA_H[m] = s * fw_ahi[((size_t)v * 2 + 1) * Nb + (prow(b) - 1)];
                 } else if (q == 2) {
-                    FA_G[m] = flux_wlo<SCHEME>(s, r0[0], r0[1], r0[2]);
-                    FA_H[m] = flux_wlo<SCHEME>(s, r0[PA + 0], r0[PA + 1], r0[PA + 2]);
+                    FA_G[m] = flux_wlo<SCHEME>(s, r0[pa(1)], r0[pa(2)], r0[pa(3)]);
+                    FA_H[m] = flux_wlo<SCHEME>(s, r0[PA + pa(1)], r0[PA + pa(2)], r0[PA + pa(3)]);
                 } else if (q == Na) {
-                    FA_G[m] = flux_whi<SCHEME>(s, r0[Na - 1], r0[Na - 2], r0[Na - 3]);
-                    FA_H[m] = flux_whi<SCHEME>(s, r0[PA + Na - 1], r0[PA + Na - 2], r0[PA + Na - 3]);
+                    FA_G[m] = flux_whi<SCHEME>(s, r0[pa(Na)], r0[pa(Na - 1)], r0[pa(Na - 2)]);
+                    FA_H[m] = flux_whi<SCHEME>(s, r0[PA + pa(Na)], r0[PA + pa(Na - 1)], r0[PA + pa(Na - 2)]);
                 } else {
                     FA_G[m] = flux_std<SCHEME>(s, w0[m], w0[m + 1], w0[m + 2], w0[m + 3]);
                     FA_H[m] = flux_std<SCHEME>(s, w1[m], w1[m + 1], w1[m + 2], w1[m + 3]);
@@ -341,34 +388,36 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
             }
             // rows b-1, b+1, b+2 at the thread's cells for the march faces
             real m0[CPT], m1[CPT];
-            Vec<real, CPT>::ld(rm + (a0 - 1), m0);
-            Vec<real, CPT>::ld(rm + PA + (a0 - 1), m1);
+            ldc(rm, m0);
+            ldc(rm + PA, m1);
             const bool stdB = perB || (b + 1 >= 3 && b + 1 <= Nb - 1);
             // Shakhov parameters of the thread's cells
-            const size_t cell0 = (size_t)(b - 1) * PA + (a0 - 1);
+            const size_t prow0 = (size_t)(prow(b) - 1) * PA;    // physical row start
+            const size_t cell0 = prow0 + pa0;
             real e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT], vl[CPT];
-            Vec<real, CPT>::ld(ep + 0 * ncell + cell0, e_crt);
-            Vec<real, CPT>::ld(ep + 1 * ncell + cell0, e_u);
-            Vec<real, CPT>::ld(ep + 2 * ncell + cell0, e_v);
-            Vec<real, CPT>::ld(ep + 3 * ncell + cell0, e_it);
-            Vec<real, CPT>::ld(ep + 4 * ncell + cell0, e_ht);
-            Vec<real, CPT>::ld(ep + 5 * ncell + cell0, e_qx);
-            Vec<real, CPT>::ld(ep + 6 * ncell + cell0, e_qy);
-            Vec<real, CPT>::ld(ep + 7 * ncell + cell0, e_cf);
+            ldc(ep + 0 * ncell + prow0, e_crt);
+            ldc(ep + 1 * ncell + prow0, e_u);
+            ldc(ep + 2 * ncell + prow0, e_v);
+            ldc(ep + 3 * ncell + prow0, e_it);
+            ldc(ep + 4 * ncell + prow0, e_ht);
+            ldc(ep + 5 * ncell + prow0, e_qx);
+            ldc(ep + 6 * ncell + prow0, e_qy);
+            ldc(ep + 7 * ncell + prow0, e_cf);
             if (!UNI) Vec<real, CPT>::ld(A.vol + cell0, vl);
             // the next row's Shakhov parameters towards L1 while this row
             // computes (one prefetch per 128-byte line)
-            if (b < Nb && ((a0 - 1) * (int)sizeof(real)) % 128 == 0) {
+            if (b < Nb && (pa0 * (int)sizeof(real)) % 128 == 0) {
+                const size_t nxt = (size_t)(prow(b + 1) - 1) * PA + pa0;
 #pragma unroll
                 for (int q = 0; q < 8; q++)
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(ep + q * ncell + cell0 + PA));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(ep + q * ncell + nxt));
             }
             if (stdB) {
                 real p0[CPT], p1[CPT], q0[CPT], q1[CPT];
-                Vec<real, CPT>::ld(rp + (a0 - 1), p0);
-                Vec<real, CPT>::ld(rp + PA + (a0 - 1), p1);
-                Vec<real, CPT>::ld(rq + (a0 - 1), q0);
-                Vec<real, CPT>::ld(rq + PA + (a0 - 1), q1);
+                ldc(rp, p0);
+                ldc(rp + PA, p1);
+                ldc(rq, q0);
+                ldc(rq + PA, q1);
 #pragma unroll
                 for (int k = 0; k < CPT; k++) {
                     sBh[k] = speedB(b + 1, a0 + k);
@@ -425,8 +474,8 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
                 P = pc[k] * P;
             }
             if (A.rhs) {
-                Vec<real, CPT>::st(A.rhs + vrow0 + cell0, rG);
-                Vec<real, CPT>::st(A.rhs + vrow0 + rstride + cell0, rH);
+                stc(A.rhs + vrow0 + prow0, rG);
+                stc(A.rhs + vrow0 + rstride + prow0, rH);
             }
         } else {
 #pragma unroll
@@ -502,14 +551,14 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
                 const real nxH = (k + 1 < CPT) ? dH[k + 1] : lastH;
                 const real ca = -negp(sAhp[k]);
                 const real cb = -negp(sBl[k]);
-                real fg = fo0[k] + (dG[k] + (ca * nxG + cb * nG[k]) * iap[k]);
-                real fh = fo1[k] + (dH[k] + (ca * nxH + cb * nH[k]) * iap[k]);
+                real fg = msc * (fo0[k] + (dG[k] + (ca * nxG + cb * nG[k]) * iap[k]));
+                real fh = msc * (fo1[k] + (dH[k] + (ca * nxH + cb * nH[k]) * iap[k]));
                 uG[k] = fg < fl ? fl : fg;
                 uH[k] = fh < fl ? fl : fh;
             }
-            const size_t c1 = (size_t)(b - 2) * PA + (a0 - 1);
-            Vec<real, CPT>::st(A.f + vrow0 + c1, uG);
-            Vec<real, CPT>::st(A.f + vrow0 + rstride + c1, uH);
+            const size_t c1 = (size_t)(prow(b - 1) - 1) * PA;
+            stc(A.f + vrow0 + c1, uG);
+            stc(A.f + vrow0 + rstride + c1, uH);
         }
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
@@ -526,31 +575,31 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     if (act && !A.no_update) {   // backward + update of the last row (downstream values are 0)
         const real *dlp = dlf + (size_t)(Nb & 1) * 2 * TPV;
         const bool has_next = (a0 + CPT <= Na);
-        const real *o0 = rowp(Nb) + (a0 - 1);
+        const real *o0 = rowp(Nb);
         real f0[CPT], f1[CPT], uG[CPT], uH[CPT];
-        Vec<real, CPT>::ld(o0, f0);
-        Vec<real, CPT>::ld(o0 + PA, f1);
+        ldc(o0, f0);
+        ldc(o0 + PA, f1);
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
             const real nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : real(0));
             const real nxH = (k + 1 < CPT) ? dH[k + 1] : (has_next ? dlp[TPV + t + 1] : real(0));
             const real ca = -negp(sAhp[k]);
-            real fg = f0[k] + (dG[k] + (ca * nxG) * iap[k]);
-            real fh = f1[k] + (dH[k] + (ca * nxH) * iap[k]);
+            real fg = msc * (f0[k] + (dG[k] + (ca * nxG) * iap[k]));
+            real fh = msc * (f1[k] + (dH[k] + (ca * nxH) * iap[k]));
             uG[k] = fg < fl ? fl : fg;
             uH[k] = fh < fl ? fl : fh;
         }
-        const size_t c1 = (size_t)(Nb - 1) * PA + (a0 - 1);
-        Vec<real, CPT>::st(A.f + vrow0 + c1, uG);
-        Vec<real, CPT>::st(A.f + vrow0 + rstride + c1, uH);
+        const size_t c1 = (size_t)(prow(Nb) - 1) * PA;
+        stc(A.f + vrow0 + c1, uG);
+        stc(A.f + vrow0 + rstride + c1, uH);
     }
     // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
     // for above, so no copy is in flight when the CTA exits
 }
 
-template <typename real, int CPT, bool UNI, int SCHEME>
+template <typename real, int CPT, bool UNI, int SCHEME, bool UPW>
 __global__ void __launch_bounds__(256, 2) k_sweep(KinArgs<real> A) {
-    sweep_body<real, CPT, UNI, SCHEME>(A, blockIdx.x);
+    sweep_body<real, CPT, UNI, SCHEME, UPW>(A, blockIdx.x);
 }
 
 // many contexts of one launch shape in one launch: CTA i sweeps velocity
@@ -568,19 +617,19 @@ __global__ void __launch_bounds__(256, 2) k_sweep_batch(const KinArgs<real> *__r
 // ---- host side --------------------------------------------------------------
 // launch = false only sets the kernel's shared-memory attribute (done before
 // any stream capture of the launch)
-template <typename real, int CPT, bool UNI, int SCHEME>
+template <typename real, int CPT, bool UNI, int SCHEME, bool UPW>
 int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, bool launch) {
     const int tpv = ctx->PA / CPT;
     const size_t smem = sweep_group_bytes<real>(ctx->PA, tpv) * vpb;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_sweep<real, CPT, UNI, SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_sweep<real, CPT, UNI, SCHEME, UPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              227 * 1024);
         attr = true;
     }
     if (!launch) return HYB_OK;
     dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
-    k_sweep<real, CPT, UNI, SCHEME><<<grd, blk, smem, ctx->stream>>>(A);
+    k_sweep<real, CPT, UNI, SCHEME, UPW><<<grd, blk, smem, ctx->stream>>>(A);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -590,25 +639,35 @@ int sweep_launch_one(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, bool launch)
     return HYB_OK;
 }
 
-template <typename real, int CPT, bool UNI>
+template <typename real, int CPT, bool UNI, bool UPW>
 int sweep_launch_scheme(hyb_ctx *ctx, const KinArgs<real> &A, int vpb, bool launch) {
     switch (A.scheme) {
-        case HYB_SCHEME_UP1: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_UP1>(ctx, A, vpb, launch);
-        case HYB_SCHEME_WENO3: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_WENO3>(ctx, A, vpb, launch);
-        default: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_NND>(ctx, A, vpb, launch);
+        case HYB_SCHEME_UP1: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_UP1, UPW>(ctx, A, vpb, launch);
+        case HYB_SCHEME_WENO3: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_WENO3, UPW>(ctx, A, vpb, launch);
+        default: return sweep_launch_one<real, CPT, UNI, HYB_SCHEME_NND, UPW>(ctx, A, vpb, launch);
     }
 }
 
+// the upwind order is instantiated for uniform meshes only (the context
+// refuses it on other meshes)
 template <typename real>
 int sweep_launch_real(hyb_ctx *ctx, const KinArgs<real> &A, int cpt, int vpb, bool launch) {
     const bool u = ctx->uniform != 0;
+    if (ctx->prm.sweep_order == HYB_SWEEP_UPWIND) {
+        if (!u) return HYB_ERR_UNSUPPORTED;
+        switch (cpt) {
+            case 4: return sweep_launch_scheme<real, 4, true, true>(ctx, A, vpb, launch);
+            case 2: return sweep_launch_scheme<real, 2, true, true>(ctx, A, vpb, launch);
+            default: return sweep_launch_scheme<real, 1, true, true>(ctx, A, vpb, launch);
+        }
+    }
     switch (cpt) {
-        case 4: return u ? sweep_launch_scheme<real, 4, true>(ctx, A, vpb, launch)
-                         : sweep_launch_scheme<real, 4, false>(ctx, A, vpb, launch);
-        case 2: return u ? sweep_launch_scheme<real, 2, true>(ctx, A, vpb, launch)
-                         : sweep_launch_scheme<real, 2, false>(ctx, A, vpb, launch);
-        default: return u ? sweep_launch_scheme<real, 1, true>(ctx, A, vpb, launch)
-                          : sweep_launch_scheme<real, 1, false>(ctx, A, vpb, launch);
+        case 4: return u ? sweep_launch_scheme<real, 4, true, false>(ctx, A, vpb, launch)
+                         : sweep_launch_scheme<real, 4, false, false>(ctx, A, vpb, launch);
+        case 2: return u ? sweep_launch_scheme<real, 2, true, false>(ctx, A, vpb, launch)
+                         : sweep_launch_scheme<real, 2, false, false>(ctx, A, vpb, launch);
+        default: return u ? sweep_launch_scheme<real, 1, true, false>(ctx, A, vpb, launch)
+                          : sweep_launch_scheme<real, 1, false, false>(ctx, A, vpb, launch);
     }
 }
 

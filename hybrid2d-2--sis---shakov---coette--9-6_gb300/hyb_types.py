@@ -25,6 +25,9 @@ HYB_SCHEME_WENO3 = 3
 HYB_PREC_FP64 = 0
 HYB_PREC_MIXED = 1
 
+HYB_SWEEP_REFERENCE = 0
+HYB_SWEEP_UPWIND = 1
+
 HYB_NSUM = 11
 HYB_NRD = 2
 
@@ -54,7 +57,8 @@ class HybParams(C.Structure):
         ("scheme", C.c_int), ("precision", C.c_int),
         ("gamma", C.c_double), ("ma", C.c_double), ("pr", C.c_double), ("re", C.c_double),
         ("omega_ns", C.c_double),
-        ("device", C.c_int), ("reserved", C.c_int * 7),
+        ("device", C.c_int), ("sweep_order", C.c_int), ("mass_pin", C.c_int),
+        ("reserved", C.c_int * 5),
     ]
 
 

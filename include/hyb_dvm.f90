@@ -13,6 +13,7 @@ module hyb_dvm
   integer(c_int), parameter :: HYB_BC_WALL = -2, HYB_BC_PERIODIC = 1
   integer(c_int), parameter :: HYB_SCHEME_UP1 = 0, HYB_SCHEME_NND = 1, HYB_SCHEME_WENO3 = 3
   integer(c_int), parameter :: HYB_PREC_FP64 = 0, HYB_PREC_MIXED = 1
+  integer(c_int), parameter :: HYB_SWEEP_REFERENCE = 0, HYB_SWEEP_UPWIND = 1
   integer(c_int), parameter :: HYB_NSUM = 11, HYB_NRD = 2
   integer(c_int), parameter :: HYB_NOALLOC_MAX_CELLS = 209715
 
@@ -33,7 +34,8 @@ module hyb_dvm
      integer(c_int) :: scheme, precision
      real(c_double) :: gamma, ma, pr, re, omega_ns
      integer(c_int) :: device
-     integer(c_int) :: reserved(7)
+     integer(c_int) :: sweep_order, mass_pin
+     integer(c_int) :: reserved(5)
   end type hyb_params
 
   type, bind(c) :: hyb_residual

@@ -61,6 +61,21 @@ extern "C" {
 #define HYB_PREC_MIXED     1       /* f, fluxes, sweeps in FP32; moments,
                                       residual, synthetic solve in FP64      */
 
+/* ---- order of the kinetic implicit step (hyb_params.sweep_order) -------- */
+#define HYB_SWEEP_REFERENCE 0      /* GKUA_Residual.f90:28-112 as written: a
+                                      forward sweep in increasing (i, j) and a
+                                      backward step that reads the forward
+                                      values of the downstream neighbours     */
+#define HYB_SWEEP_UPWIND    1      /* one Gauss-Seidel sweep per velocity in
+                                      its own upwind order (i and j each
+                                      reversed where that velocity component
+                                      is negative): the same operator alpha
+                                      and the same RHS, solved exactly for the
+                                      first-order upwind transport.  Per step
+                                      it differs from the reference; a
+                                      converged state (RHS = 0) is the same.
+                                      No counterpart in the reference.        */
+
 /* ---- moment vector length (Nsum, COMMONDATA.f90:4) ---------------------- */
 #define HYB_NSUM          11
 #define HYB_NRD            2       /* reduced distributions G and H          */
@@ -106,7 +121,20 @@ typedef struct hyb_params {
                                    get_viscous hard-codes 0.81
                                    (sub_Residual.f90:563)                    */
     int    device;              /* CUDA device ordinal                       */
-    int    reserved[7];
+    int    sweep_order;         /* HYB_SWEEP_*: order of the kinetic LU-SGS step */
+    int    mass_pin;            /* 1: hold the total mass sum(vol rho) of f at
+                                   its value when the state was set
+                                   (hyb_init_maxwellian / hyb_upload_f): every
+                                   kinetic step multiplies its updated f by
+                                   m0 / M, M the total mass of the state the
+                                   step starts from.  The closed channel's
+                                   steady states form a family indexed by the
+                                   total mass, and an iteration that does not
+                                   conserve mass ends on a member that depends
+                                   on its path; pinned, every variant ends on
+                                   the member of mass m0.  0: the reference's
+                                   update.  No counterpart in the reference.  */
+    int    reserved[5];
 } hyb_params;
 
 /* Residual of the kinetic iteration: moments 1..4 of the last RHS,
@@ -278,7 +306,8 @@ int hyb_autotune(hyb_ctx *ctx, int reps, int *cpt, int *vpb);
  * sweep launch shape share one launch per kernel (one graph branch per
  * shape group); batches the batched kernels do not cover (schemes other than
  * NND) get one branch per instance.  Either way each instance computes
- * exactly what a standalone context computes.  res (n entries, may be NULL)
+ * exactly what a standalone context computes.  Every instance uses
+ * HYB_SWEEP_REFERENCE without mass_pin (HYB_ERR_UNSUPPORTED otherwise).  res (n entries, may be NULL)
  * receives each instance's DETFP_res after the last iteration. */
 typedef struct hyb_batch hyb_batch;
 int hyb_batch_create(int n, const hyb_mesh *meshes, const hyb_vgrid *vgrids,

@@ -663,6 +663,9 @@ int orc_kinetic_step(orc *o)
 {
     const int nx = o->nx, ny = o->ny, fp = nx + 2;
     const double dt = o->prm.dt;
+    /* mass_pin: the updated f is multiplied by m0 / M(f) of the state this
+     * step starts from (its moments are the current S) */
+    const double msc = o->prm.mass_pin ? o->m0 / orc_total_mass(o) : 1.0;
 #pragma omp parallel
     {
         double *rhs = (double *)calloc(o->P * NRD, sizeof(double));
@@ -678,6 +681,50 @@ int orc_kinetic_step(orc *o)
             rhs_velocity(o, iv, jv, rhs, ax, ay, flux, dfrd);
 #define AX(i, j) ax[(size_t)(i) + (size_t)fp * (j)]
 #define AY(i, j) ay[(size_t)(i) + (size_t)fp * (j)]
+            if (o->prm.sweep_order == HYB_SWEEP_UPWIND) {
+                /* one Gauss-Seidel sweep in this velocity's upwind order with
+                 * the reference's alpha (:39-57): i runs downwards where the
+                 * i-face speeds are negative, j where the j-face speeds are;
+                 * cells not yet visited (and every ghost) carry 0, so on a
+                 * Cartesian mesh every incoming neighbour is already solved.
+                 * The update is applied directly (no backward step). */
+                double sx = 0.0, sy = 0.0;
+                for (int j = 1; j <= ny - 1; j++) sx += AX(1, j) + AX(nx, j);
+                for (int i = 1; i <= nx - 1; i++) sy += AY(i, 1) + AY(i, ny);
+                const int di = sx < 0.0 ? -1 : 1, dj = sy < 0.0 ? -1 : 1;
+                for (int j = -3; j <= ny + 3; j++)
+                    for (int i = -3; i <= nx + 3; i++)
+                        for (int r = 0; r < NRD; r++) FRD00(o, r, i, j, v) = 0.0;
+                for (int jj = 1; jj <= ny - 1; jj++) {
+                    const int j = dj > 0 ? jj : ny - jj;
+                    for (int ii = 1; ii <= nx - 1; ii++) {
+                        const int i = di > 0 ? ii : nx - ii;
+                        double axp = pos_part(AX(i + 1, j)), ayp = pos_part(AY(i, j + 1));
+                        double axn = neg_part(AX(i, j)), ayn = neg_part(AY(i, j));
+                        double vol = o->vol[MI(o, i, j)];
+                        double alfa = vol / dt + (axp - axn + ayp - ayn) + vol * CFA(o, i, j);
+                        double axp1 = pos_part(AX(i, j)), ayp1 = pos_part(AY(i, j));
+                        double axn1 = neg_part(AX(i + 1, j)), ayn1 = neg_part(AY(i, j + 1));
+                        for (int r = 0; r < NRD; r++) {
+                            double in = axp1 * FRD00(o, r, i - 1, j, v) + ayp1 * FRD00(o, r, i, j - 1, v) -
+                                        axn1 * FRD00(o, r, i + 1, j, v) - ayn1 * FRD00(o, r, i, j + 1, v);
+                            FRD00(o, r, i, j, v) = (vol * rhs[IX(o, i, j) * NRD + r] + in) / alfa;
+                        }
+                    }
+                }
+                for (int j = 1; j <= ny - 1; j++)
+                    for (int i = 1; i <= nx - 1; i++)
+                        for (int r = 0; r < NRD; r++) {
+                            double fn = FRD(o, r, i, j, v) + FRD00(o, r, i, j, v);
+                            FRD(o, r, i, j, v) = o->prm.mass_pin ? msc * fn : fn;
+                            FRD00(o, r, i, j, v) = rhs[IX(o, i, j) * NRD + r];
+                        }
+                for (int j = -1; j <= ny + 1; j++)
+                    for (int i = -1; i <= nx + 1; i++)
+                        for (int r = 0; r < NRD; r++)
+                            if (FRD(o, r, i, j, v) < F_FLOOR) FRD(o, r, i, j, v) = F_FLOOR;
+                continue;
+            }
             /* forward sweep over anti-diagonals, :34-62.  FRD00 of ghost
              * cells is never written and stays 0, so the sweep is explicit
              * across every block face. */
@@ -725,7 +772,8 @@ int orc_kinetic_step(orc *o)
             for (int j = 1; j <= ny - 1; j++)
                 for (int i = 1; i <= nx - 1; i++)
                     for (int r = 0; r < NRD; r++) {
-                        FRD(o, r, i, j, v) = FRD(o, r, i, j, v) + dufrd[IX(o, i, j) * NRD + r];
+                        double fn = FRD(o, r, i, j, v) + dufrd[IX(o, i, j) * NRD + r];
+                        FRD(o, r, i, j, v) = o->prm.mass_pin ? msc * fn : fn;
                         FRD00(o, r, i, j, v) = rhs[IX(o, i, j) * NRD + r];
                     }
             /* floor, :101-109 (ghost layers -1..n+1 included) */
@@ -936,6 +984,7 @@ int orc_init_maxwellian(orc *o, double rho, double u, double v, double t)
     orc_exchange_f(o);
     orc_phy_boundary(o);
     orc_detfp(o);
+    o->m0 = orc_total_mass(o);
     return HYB_OK;
 }
 
@@ -944,7 +993,19 @@ int orc_upload_f(orc *o, const double *frd)
     memcpy(o->frd, frd, o->P * NRD * o->nv * sizeof(double));
     orc_exchange_f(o);
     orc_detfp(o);
+    o->m0 = orc_total_mass(o);
     return HYB_OK;
+}
+
+/* total mass sum(vol rho) over the interior cells, j outer / i inner (the
+ * order of the GPU's single-CTA fold is not this one; the sums agree to
+ * rounding) */
+double orc_total_mass(const orc *o)
+{
+    double m = 0.0;
+    for (int j = 1; j <= o->ny - 1; j++)
+        for (int i = 1; i <= o->nx - 1; i++) m += o->vol[MI(o, i, j)] * SG(o, 1, i, j);
+    return m;
 }
 
 /* ---- Convert_NS (Hybrid_Sub.f90:191-461) --------------------------------

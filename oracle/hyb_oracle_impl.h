@@ -41,6 +41,7 @@ struct orc {
     double *tao_i_g, *q_i_g, *tao_j_g, *q_j_g;        /* HoT, C2 extents      */
     double *tao_i_in, *q_i_in, *tao_j_in, *q_j_in;    /* NSF from kinetic     */
     double err;
+    double m0;            /* total mass when the state was set (mass_pin)     */
     struct orc_ns *ns;           /* GSIS synthetic solver state (hyb_oracle_ns.c) */
     hyb_gsis_params gsis;
     int gsis_last_inner;
@@ -62,5 +63,6 @@ void orc_build_u(orc *o, double *U);
 int orc_kinetic_residual_moments(orc *o, double *rk);
 void orc_feq(const orc *o, const double *s6, int iv, int jv, double *g, double *h);
 int orc_gsis_solve(orc *o);
+double orc_total_mass(const orc *o);
 
 #endif
