@@ -225,6 +225,8 @@ class Solver:
         gp.ns_solver = kw.get("ns_solver", 0)
         gp.no_mass_projection = kw.get("no_mass_projection", 0)
         gp.correct_f = kw.get("correct_f", 0)
+        gp.wall_band = kw.get("wall_band", 0)
+        gp.relax_pct = kw.get("relax_pct", 0)
         self._ck(self.L.hyb_gsis_configure(self.h, C.byref(gp)), "gsis_configure")
 
     def gsis_last_inner(self):

@@ -64,6 +64,9 @@ struct NsDev {
     double *src;                                             // synthetic source Q [4][nc]
     const double *rk;                                        // kinetic RHS moments [4][Nb*PA]
     int src_on, PA, scan_is_j, mass_proj, ns_scheme, correct_f;
+    int wall_band;                                           // band to the walls, reflected ghosts
+    double relax;                                            // correction factor r (relax_pct / 100)
+    double *wface;                                           // wall-face kinetic rho, u, v, T [4][4][mx]
     double *sk;                                              // band moments before the correction [6][nc]
     double *lin;                                             // line-solver scratch [16][nc]
     double *d, *uu, *vv, *T, *p, *cc, *amu;
@@ -656,6 +659,255 @@ __global__ void k_ns_ilines(NsDev D) {
     tri_line(L, ni, D.perx != 0, w + base, w + D.nc + base, w + 2 * D.nc + base, 1);
 }
 
+// ---- wall_band: reflected wall ghosts (boundary_wall, sub_boundary.f90:51-118)
+// Cell k = 1, 2 into the domain and ghost k outside, face f (1..4), face
+// cell m (faces 1 / 3: m = j, faces 2 / 4: m = i).
+__device__ __forceinline__ void wall_pair(const NsDev &D, int f, int m, int k, size_t *ci, size_t *cg) {
+    if (f == 1) { *ci = c2(D, k, m); *cg = c2(D, 1 - k, m); }
+    else if (f == 3) { *ci = c2(D, D.nx - k, m); *cg = c2(D, D.nx - 1 + k, m); }
+    else if (f == 2) { *ci = c2(D, m, k); *cg = c2(D, m, 1 - k); }
+    else { *ci = c2(D, m, D.ny - k); *cg = c2(D, m, D.ny - 1 + k); }
+}
+__device__ __forceinline__ int wall_mx(const NsDev &D) { return D.nx > D.ny ? D.nx : D.ny; }
+// thread t -> (face, face cell) over the wall faces; false past the end
+__device__ __forceinline__ bool wall_item(const NsDev &D, int t, int *f, int *m) {
+    for (int q = 1; q <= 4; q++) {
+        const bool wall = (q == 1 || q == 3) ? !D.perx : !D.pery;
+        if (!wall) continue;
+        const int n = (q == 1 || q == 3) ? D.ny - 1 : D.nx - 1;
+        if (t < n) { *f = q; *m = t + 1; return true; }
+        t -= n;
+    }
+    return false;
+}
+
+// the kinetic state at each wall face: the mean of the first cell and its
+// ghost (the linear wall extrapolation of DETFPwall), frozen for the solve
+__global__ void k_ns_wallstore(NsDev D) {
+    int f, m;
+    if (!wall_item(D, blockIdx.x * blockDim.x + threadIdx.x, &f, &m)) return;
+    size_t ci, cg;
+    wall_pair(D, f, m, 1, &ci, &cg);
+    const int mx = wall_mx(D);
+    double w[2][4];
+    for (int s2 = 0; s2 < 2; s2++) {
+        const size_t c = s2 ? cg : ci;
+        const double d = D.U[c], u = D.U[D.nc + c] / d, v = D.U[2 * D.nc + c] / d;
+        const double t = (D.U[3 * D.nc + c] - 0.5 * d * (u * u + v * v)) / (D.cv * d);
+        w[s2][0] = d; w[s2][1] = u; w[s2][2] = v; w[s2][3] = t;
+    }
+    for (int q = 0; q < 4; q++) D.wface[((size_t)(f - 1) * 4 + q) * mx + m] = 0.5 * (w[0][q] + w[1][q]);
+}
+
+// ghost layers 1, 2: primitive ghost = 2 W - interior
+__global__ void k_ns_wallghost(NsDev D) {
+    if (D.ctrl->done) return;
+    int f, m;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!wall_item(D, t >> 1, &f, &m)) return;
+    const int k = (t & 1) + 1;
+    size_t ci, cg;
+    wall_pair(D, f, m, k, &ci, &cg);
+    const int mx = wall_mx(D);
+    const double *W = D.wface + (size_t)(f - 1) * 4 * mx + m;
+    const double d = D.U[ci], u = D.U[D.nc + ci] / d, v = D.U[2 * D.nc + ci] / d;
+    const double tt = (D.U[3 * D.nc + ci] - 0.5 * d * (u * u + v * v)) / (D.cv * d);
+    const double d2 = 2.0 * W[0] - d, u2 = 2.0 * W[mx] - u, v2 = 2.0 * W[2 * mx] - v, t2 = 2.0 * W[3 * mx] - tt;
+    D.U[cg] = d2;
+    D.U[D.nc + cg] = d2 * u2;
+    D.U[2 * D.nc + cg] = d2 * v2;
+    D.U[3 * D.nc + cg] = d2 * (D.cv * t2 + 0.5 * (u2 * u2 + v2 * v2));
+}
+
+// ---- block line-implicit inner solve (ns_solver 2) -----------------------------
+// On every mesh line between the walls the matrix du_LU_SGS_2D factorises
+// (sub_LU_SGS.f90:26-111: diagonal alpha, neighbour blocks 0.5 (A s +- Lc) +
+// Lv, A the Jacobian of the flux difference comput_DFn) is solved by
+// block-tridiagonal elimination with partial pivoting inside the 4x4 blocks;
+// the neighbours along the other axis carry dU = 0.  With wall_band the
+// reflected ghost moves with -dU of the wall cell, so its coupling block
+// joins that cell's diagonal.  One thread per line.  The elimination is in
+// FP32: it is the preconditioner of the inner iteration, whose residual and
+// update stay FP64, so it sets the rate but not the solution.  Scratch
+// D.lin holds G[16] and g[4] per cell as floats.
+__device__ __forceinline__ void flux_jac(const double *U, double n1, double n2, double g, float *A) {
+    const double r = U[0], u = U[1] / r, v = U[2] / r, E = U[3];
+    const double a1 = g - 1.0, q2 = u * u + v * v, phi = 0.5 * a1 * q2;
+    const double p = a1 * (E - 0.5 * r * q2), H = (E + p) / r, un = u * n1 + v * n2;
+    A[0] = 0.f; A[1] = (float)n1; A[2] = (float)n2; A[3] = 0.f;
+    A[4] = (float)(phi * n1 - u * un); A[5] = (float)(un + u * n1 - a1 * u * n1);
+    A[6] = (float)(u * n2 - a1 * v * n1); A[7] = (float)(a1 * n1);
+    A[8] = (float)(phi * n2 - v * un); A[9] = (float)(v * n1 - a1 * u * n2);
+    A[10] = (float)(un + v * n2 - a1 * v * n2); A[11] = (float)(a1 * n2);
+    A[12] = (float)((phi - H) * un); A[13] = (float)(H * n1 - a1 * u * un);
+    A[14] = (float)(H * n2 - a1 * v * un); A[15] = (float)(g * un);
+}
+
+// X = M^-1 B, M 4x4, B 4 x K (row-major), partial pivoting; M destroyed
+template <int K>
+__device__ __forceinline__ void solve4f(float *M, float *B) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int pr = c;
+#pragma unroll
+        for (int r = c + 1; r < 4; r++)
+            if (fabsf(M[r * 4 + c]) > fabsf(M[pr * 4 + c])) pr = r;
+        if (pr != c) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) { float t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t; }
+#pragma unroll
+            for (int q = 0; q < K; q++) { float t = B[c * K + q]; B[c * K + q] = B[pr * K + q]; B[pr * K + q] = t; }
+        }
+        const float ip = 1.f / M[c * 4 + c];
+#pragma unroll
+        for (int r = c + 1; r < 4; r++) {
+            const float fr = M[r * 4 + c] * ip;
+#pragma unroll
+            for (int q = c; q < 4; q++) M[r * 4 + q] -= fr * M[c * 4 + q];
+#pragma unroll
+            for (int q = 0; q < K; q++) B[r * K + q] -= fr * B[c * K + q];
+        }
+    }
+#pragma unroll
+    for (int c = 3; c >= 0; c--) {
+        const float ip = 1.f / M[c * 4 + c];
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            float t = B[c * K + q];
+#pragma unroll
+            for (int r = c + 1; r < 4; r++) t -= M[c * 4 + r] * B[r * K + q];
+            B[c * K + q] = t * ip;
+        }
+    }
+}
+
+__global__ void k_ns_blines(NsDev D) {
+    if (D.ctrl->done) return;
+    const bool along_j = !D.pery;
+    const int n0 = along_j ? D.ilo : D.jlo, n1 = along_j ? D.ihi : D.jhi;
+    const int k0 = along_j ? D.jlo : D.ilo, k1 = along_j ? D.jhi : D.ihi;
+    const int ln = n0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (ln > n1) return;
+    const double g = D.gamma;
+    float *Gs = reinterpret_cast<float *>(D.lin);            // [16][nc]
+    float *gs = Gs + 16 * D.nc;                              // [4][nc]
+    for (int k = k0; k <= k1; k++) {
+        const int i = along_j ? ln : k, j = along_j ? k : ln;
+        const size_t c = c2(D, i, j);
+        const double alfa = D.vol[mi(D, i, j)] / D.dt[c] + D.Lci[c] + D.Lcj[c] + 2.0 * (D.Lvi[c] + D.Lvj[c]);
+        float M[16], Bm[20];
+#pragma unroll
+        for (int q = 0; q < 16; q++) M[q] = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; q++) M[q * 4 + q] = (float)alfa;
+#pragma unroll
+        for (int q = 0; q < 20; q++) Bm[q] = 0.f;
+#pragma unroll
+        for (int m = 0; m < 4; m++) Bm[m * 5 + 4] = (float)D.Res[(size_t)m * D.nc + c];
+        const bool walls = along_j ? !D.pery : !D.perx;
+        const bool wlo = D.wall_band && walls && k == k0;
+        const bool whi = D.wall_band && walls && k == k1;
+        const double n1f = along_j ? D.nj1[mi(D, i, j)] : D.ni1[mi(D, i, j)];
+        const double n2f = along_j ? D.nj2[mi(D, i, j)] : D.ni2[mi(D, i, j)];
+        if (k > k0 || wlo) {   // lower neighbour: L = 0.5 (A s + Lc) + Lv
+            const size_t cn = along_j ? c2(D, i, j - 1) : c2(D, i - 1, j);
+            const size_t cr = wlo ? c : cn;
+            double Un[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * D.nc + cn];
+            const double sf = along_j ? D.sj[mi(D, i, j)] : D.si[mi(D, i, j)];
+            const double lc = along_j ? D.Lcj[cr] : D.Lci[cr], lv = along_j ? D.Lvj[cr] : D.Lvi[cr];
+            float A[16], L[16];
+            flux_jac(Un, n1f, n2f, g, A);
+#pragma unroll
+            for (int q = 0; q < 16; q++) L[q] = 0.5f * A[q] * (float)sf;
+#pragma unroll
+            for (int q = 0; q < 4; q++) L[q * 4 + q] += (float)(0.5 * lc + lv);
+            if (wlo) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) M[q] += L[q];
+            } else {
+                const size_t cp = along_j ? c2(D, i, j - 1) : c2(D, i - 1, j);
+                float Gp[16], gp[4];
+#pragma unroll
+                for (int q = 0; q < 16; q++) Gp[q] = Gs[(size_t)q * D.nc + cp];
+#pragma unroll
+                for (int q = 0; q < 4; q++) gp[q] = gs[(size_t)q * D.nc + cp];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        float t = 0.f;
+#pragma unroll
+                        for (int m = 0; m < 4; m++) t += L[r * 4 + m] * Gp[m * 4 + q];
+                        M[r * 4 + q] -= t;
+                    }
+                    float t = 0.f;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) t += L[r * 4 + m] * gp[m];
+                    Bm[r * 5 + 4] += t;
+                }
+            }
+        }
+        if (k < k1 || whi) {   // upper neighbour: C = -0.5 (A s - Lc) + Lv
+            const size_t cn = along_j ? c2(D, i, j + 1) : c2(D, i + 1, j);
+            const size_t cr = whi ? c : cn;
+            double Un[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * D.nc + cn];
+            const double sf = along_j ? D.sj[mi(D, i, j + 1)] : D.si[mi(D, i + 1, j)];
+            const double lc = along_j ? D.Lcj[cr] : D.Lci[cr], lv = along_j ? D.Lvj[cr] : D.Lvi[cr];
+            float A[16];
+            flux_jac(Un, n1f, n2f, g, A);
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float cq = -0.5f * A[r * 4 + q] * (float)sf + (r == q ? (float)(0.5 * lc + lv) : 0.f);
+                    if (whi) M[r * 4 + q] += cq;
+                    else Bm[r * 5 + q] = cq;
+                }
+        }
+        solve4f<5>(M, Bm);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) Gs[(size_t)(r * 4 + q) * D.nc + c] = Bm[r * 5 + q];
+            gs[(size_t)r * D.nc + c] = Bm[r * 5 + 4];
+        }
+    }
+    float nxt[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k = k1; k >= k0; k--) {
+        const int i = along_j ? ln : k, j = along_j ? k : ln;
+        const size_t c = c2(D, i, j);
+        float d[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float t = gs[(size_t)r * D.nc + c];
+#pragma unroll
+            for (int q = 0; q < 4; q++) t += Gs[(size_t)(r * 4 + q) * D.nc + c] * nxt[q];
+            d[r] = t;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            D.dU[(size_t)r * D.nc + c] = (double)d[r];
+            nxt[r] = d[r];
+        }
+    }
+}
+
+// relax_pct: U = U_k + r (U - U_k) on the band
+__global__ void k_gsis_relax(NsDev D) {
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= bw * bh) return;
+    const size_t c = c2(D, idx % bw + D.ilo, idx / bw + D.jlo);
+    for (int m = 0; m < 4; m++) {
+        const size_t o = (size_t)m * D.nc + c;
+        D.U[o] = D.U2[o] + D.relax * (D.U[o] - D.U2[o]);
+    }
+}
+
 // U += dU on the band
 __device__ __forceinline__ void ns_update_body(const NsDev &D, int idx) {
     const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
@@ -949,12 +1201,12 @@ __global__ void k_gsis_finish(NsDev D) {
     for (int k = 0; k < 4; k++) {
         double out = 0.25 * (D.ti_out[k * nc + c] + D.tj_out[k * nc + c] + D.ti_out[k * nc + ci1] + D.tj_out[k * nc + cj1]);
         double in = 0.25 * (D.tin_i[k * nc + c] + D.tin_j[k * nc + c] + D.tin_i[k * nc + ci1] + D.tin_j[k * nc + cj1]);
-        tao[k] = -1.0 * (out - in) * g2;
+        tao[k] = -D.relax * (out - in) * g2;
     }
     for (int k = 0; k < 2; k++) {
         double out = 0.25 * (D.qi_out[k * nc + c] + D.qj_out[k * nc + c] + D.qi_out[k * nc + ci1] + D.qj_out[k * nc + cj1]);
         double in = 0.25 * (D.qin_i[k * nc + c] + D.qin_j[k * nc + c] + D.qin_i[k * nc + ci1] + D.qin_j[k * nc + cj1]);
-        q[k] = -1.0 * (out - in) * q2;
+        q[k] = -D.relax * (out - in) * q2;
     }
     D.S[4 * nc + c] += tao[0];
     D.S[5 * nc + c] += tao[1];
@@ -1071,7 +1323,19 @@ void ns_destroy(hyb_ctx *ctx) {
     ctx->ns = nullptr;
 }
 
+// band of cells the synthetic solve updates, with the options that shape it
+static void ns_band(const hyb_ctx *ctx, NsDev &D) {
+    const int e = ctx->gsis.wall_band ? 1 : 3;
+    if (D.perx) { D.ilo = 1; D.ihi = D.nx - 1; } else { D.ilo = e; D.ihi = D.nx - e; }
+    if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = e; D.jhi = D.ny - e; }
+    D.wall_band = ctx->gsis.wall_band != 0;
+    D.relax = ctx->gsis.relax_pct > 0 ? ctx->gsis.relax_pct / 100.0 : 1.0;
+}
+
 int ns_create(hyb_ctx *ctx) {
+    if (ctx->gsis.ns_solver < 0 || ctx->gsis.ns_solver > 2 || ctx->gsis.relax_pct < 0 ||
+        ctx->gsis.relax_pct > 100)
+        return HYB_ERR_INVALID;
     if (ctx->ns) {   // reconfigured: re-capture with the new parameters
         NsState *st = (NsState *)ctx->ns;
         if (st->have_graph) cudaGraphExecDestroy(st->graph);
@@ -1079,6 +1343,7 @@ int ns_create(hyb_ctx *ctx) {
         st->D.mass_proj = ctx->gsis.no_mass_projection == 0;
         st->D.ns_scheme = ctx->gsis.ns_scheme;
         st->D.correct_f = ctx->gsis.correct_f != 0;
+        ns_band(ctx, st->D);
         return HYB_OK;
     }
     if ((ctx->nx < 7 && ctx->bc[0] != HYB_BC_PERIODIC) || (ctx->ny < 7 && ctx->bc[1] != HYB_BC_PERIODIC)) {
@@ -1097,11 +1362,11 @@ int ns_create(hyb_ctx *ctx) {
     D.ny = ctx->ny;
     D.perx = ctx->bc[0] == HYB_BC_PERIODIC;
     D.pery = ctx->bc[1] == HYB_BC_PERIODIC;
-    if (D.perx) { D.ilo = 1; D.ihi = D.nx - 1; } else { D.ilo = 3; D.ihi = D.nx - 3; }
-    if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = 3; D.jhi = D.ny - 3; }
+    ns_band(ctx, D);
     D.nc = (size_t)(D.nx + 3) * (D.ny + 3);
     const size_t nc = D.nc;
-    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6;   // see the pointer carve below
+    // see the pointer carve below; the last term holds the wall-face states
+    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6 + 1;
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
     if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
@@ -1133,6 +1398,7 @@ int ns_create(hyb_ctx *ctx) {
     D.ti_out = h; h += 4 * nc; D.qi_out = h; h += 2 * nc; D.tj_out = h; h += 4 * nc; D.qj_out = h; h += 2 * nc;
     D.lin = h; h += 16 * nc;
     D.sk = h; h += 6 * nc;
+    D.wface = h; h += nc;   // 16 * max(nx, ny) <= (nx + 3)(ny + 3) for nx, ny >= 3
     const size_t nm = (size_t)ctx->nx * ctx->ny;
     if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
         cudaFree(st->buf);
@@ -1210,6 +1476,9 @@ int ns_create(hyb_ctx *ctx) {
     return ck(ctx, "ns_create");
 }
 
+// wall face cells of the block (host)
+static int wall_cells(const NsDev &D) { return (D.perx ? 0 : 2 * (D.ny - 1)) + (D.pery ? 0 : 2 * (D.nx - 1)); }
+
 // launches of one inner iteration (captured NS_BATCH times into a graph)
 static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     const int bs = 256;
@@ -1218,6 +1487,7 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     const int ncell = (D.nx - 1) * (D.ny - 1);
     const int nband = (D.ihi - D.ilo + 1) * (D.jhi - D.jlo + 1);
     cudaStream_t s = ctx->stream;
+    if (D.wall_band) k_ns_wallghost<<<(unsigned)((2 * wall_cells(D) + 127) / 128), 128, 0, s>>>(D);
     k_ns_prims<<<gc, bs, 0, s>>>(D);
     if (D.mlp_on) {
         k_ns_features<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D);
@@ -1226,7 +1496,10 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     k_ns_faces<<<(nfi + bs - 1) / bs, bs, 0, s>>>(D, 0);
     k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D, 1);
     k_ns_res<<<(ncell + bs - 1) / bs, bs, 0, s>>>(D);
-    if (ctx->gsis.ns_solver == 1) {
+    if (ctx->gsis.ns_solver == 2) {
+        const int nl = D.pery ? D.jhi - D.jlo + 1 : D.ihi - D.ilo + 1;
+        k_ns_blines<<<(nl + 31) / 32, 32, 0, s>>>(D);
+    } else if (ctx->gsis.ns_solver == 1) {
         const int ncol = D.ihi - D.ilo + 1, nrow = D.jhi - D.jlo + 1;
         k_ns_jlines<<<(4 * ncol + 63) / 64, 64, 0, s>>>(D);
         k_ns_ilines<<<(4 * nrow + 63) / 64, 64, 0, s>>>(D);
@@ -1241,7 +1514,8 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
 }
 
 static int inner_launches(const hyb_ctx *ctx, const NsDev &D) {
-    return (ctx->gsis.ns_solver == 1 ? 8 : 10) + (D.mlp_on ? 2 : 0);
+    const int solver = ctx->gsis.ns_solver == 2 ? 1 : (ctx->gsis.ns_solver == 1 ? 2 : 4);
+    return 6 + solver + (D.mlp_on ? 2 : 0) + (D.wall_band ? 1 : 0);
 }
 
 // after the inner iterations: mass projection, moment correction with getNSF,
@@ -1300,7 +1574,6 @@ int gsis_solve(hyb_ctx *ctx) {
     // U = U_k, the state Convert_NS left in d_hot
     k_gsis_start<<<(unsigned)((4 * D.nc + bs - 1) / bs), bs, 0, s>>>(D, ctx->d_hot);
     k_ns_ghosts<<<1, 256, 0, s>>>(D);
-    k_gsis_copy<<<(unsigned)((4 * D.nc + bs - 1) / bs), bs, 0, s>>>(D.U2, D.U, 4 * D.nc);
     NsCtrl c0;
     memset(&c0, 0, sizeof(c0));
     c0.max_it = ctx->gsis.max_inner > 0 ? ctx->gsis.max_inner : 2000;
@@ -1308,6 +1581,13 @@ int gsis_solve(hyb_ctx *ctx) {
     c0.rtol = ctx->gsis.inner_rtol;
     *st->h_ctrl = c0;
     HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
+    if (D.wall_band) {
+        const int nw = wall_cells(D);
+        k_ns_wallstore<<<(unsigned)((nw + 127) / 128), 128, 0, s>>>(D);
+        k_ns_wallghost<<<(unsigned)((2 * nw + 127) / 128), 128, 0, s>>>(D);
+        ctx->launches += 2;
+    }
+    k_gsis_copy<<<(unsigned)((4 * D.nc + bs - 1) / bs), bs, 0, s>>>(D.U2, D.U, 4 * D.nc);
     // R_NS(U_k) without the source, then Q = R_K - R_NS(U_k)
     {
         NsDev D0 = D;
@@ -1321,7 +1601,7 @@ int gsis_solve(hyb_ctx *ctx) {
     }
     ctx->launches += 8;
     HYB_CK(cudaGetLastError());
-    if (ctx->gsis.ns_solver == 0 && D.nc <= NS_COOP_MAX_CELLS && st->coop_blocks > 0) {
+    if (ctx->gsis.ns_solver == 0 && !D.wall_band && D.nc <= NS_COOP_MAX_CELLS && st->coop_blocks > 0) {
         // small mesh: the whole inner loop in one cooperative launch
         void *kargs[] = {(void *)&D};
         HYB_CK(cudaLaunchCooperativeKernel((const void *)k_ns_coop, dim3(st->coop_blocks), dim3(NS_COOP_THREADS),
@@ -1353,6 +1633,10 @@ int gsis_solve(hyb_ctx *ctx) {
         ctx->last_error = "synthetic solve: temperature below 0.1 or non-finite residual";
         return st->h_ctrl->err;
     }
+    if (D.relax != 1.0) {
+        k_gsis_relax<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+        ctx->launches++;
+    }
     return finish_correction(ctx, D, D.correct_f != 0);
 }
 
@@ -1375,12 +1659,12 @@ int gsis_warm_start(hyb_ctx *ctx) {
     W.dtmin = ctx->gsis.dtmin > 0 ? ctx->gsis.dtmin : 1e-7;
     W.src_on = 0;
     W.mlp_on = 1;
+    W.relax = 1.0;
     const int bs = 256;
     cudaStream_t s = ctx->stream;
     k_gsis_start<<<(unsigned)((4 * W.nc + bs - 1) / bs), bs, 0, s>>>(W, ctx->d_hot);
     k_ns_ghosts<<<1, 256, 0, s>>>(W);
-    k_gsis_copy<<<(unsigned)((4 * W.nc + bs - 1) / bs), bs, 0, s>>>(W.U2, W.U, 4 * W.nc);
-    ctx->launches += 3;
+    ctx->launches += 2;
     NsCtrl c0;
     memset(&c0, 0, sizeof(c0));
     c0.max_it = ctx->gsis.mlp_warm_inner > 0 ? ctx->gsis.mlp_warm_inner : 2000;
@@ -1388,6 +1672,14 @@ int gsis_warm_start(hyb_ctx *ctx) {
     c0.rtol = ctx->gsis.mlp_warm_rtol > 0 ? ctx->gsis.mlp_warm_rtol : 1e-3;
     *st->h_ctrl = c0;
     HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
+    if (W.wall_band) {
+        const int nw = wall_cells(W);
+        k_ns_wallstore<<<(unsigned)((nw + 127) / 128), 128, 0, s>>>(W);
+        k_ns_wallghost<<<(unsigned)((2 * nw + 127) / 128), 128, 0, s>>>(W);
+        ctx->launches += 2;
+    }
+    k_gsis_copy<<<(unsigned)((4 * W.nc + bs - 1) / bs), bs, 0, s>>>(W.U2, W.U, 4 * W.nc);
+    ctx->launches++;
     const int nbatch = (c0.max_it + NS_BATCH - 1) / NS_BATCH;
     for (int b = 0; b < nbatch; b++) {
         for (int k = 0; k < NS_BATCH; k++) inner_iteration(ctx, W);

@@ -176,7 +176,15 @@ typedef struct hyb_gsis_params {
     int    mlp_warm_inner;  /* inner iterations of the warm start (0: 2000) */
     double mlp_warm_rtol;   /* ... or until max|Res(4)| drops by this factor
                                (0: 1e-3)                                     */
-    int    reserved[2];
+    int    wall_band;       /* 1: the band reaches the walls (cells 1..n-1);
+                               the wall ghost cells take the reference's
+                               no-slip reflection (boundary_wall,
+                               sub_boundary.f90:51-118) about the kinetic
+                               state at the wall face, frozen for the solve.
+                               0: the reference's band 3..n-3 with the
+                               kinetic state held outside it              */
+    int    relax_pct;       /* the correction is applied as U_k + r (U - U_k),
+                               r = relax_pct / 100 (0: r = 1, the reference)  */
 } hyb_gsis_params;
 
 typedef struct hyb_ctx hyb_ctx;

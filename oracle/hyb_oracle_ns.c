@@ -41,6 +41,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
 
 struct orc_ns {
     size_t nc;
@@ -50,6 +51,8 @@ struct orc_ns {
     double *d, *uu, *vv, *T, *p, *cc, *amu;
     double *fluxi, *fluxj;                       /* [4][nc], faces at the C2 index of (i,j) */
     double *ti_out, *qi_out, *tj_out, *qj_out;   /* NS stress at faces, no HoT */
+    double *wface;                               /* wall_band: kinetic rho, u, v, T at the wall
+                                                    faces [4 faces][4][max(nx, ny)] */
     int src_on;
 };
 
@@ -62,7 +65,7 @@ void orc_ns_free(orc *o)
     struct orc_ns *ns = o->ns;
     double **ps[] = {&ns->U, &ns->rk, &ns->src, &ns->sk, &ns->U2, &ns->dU, &ns->Res, &ns->dt, &ns->Lci, &ns->Lcj, &ns->Lvi, &ns->Lvj,
                      &ns->d, &ns->uu, &ns->vv, &ns->T, &ns->p, &ns->cc, &ns->amu, &ns->fluxi, &ns->fluxj,
-                     &ns->ti_out, &ns->qi_out, &ns->tj_out, &ns->qj_out};
+                     &ns->ti_out, &ns->qi_out, &ns->tj_out, &ns->qj_out, &ns->wface};
     for (size_t k = 0; k < sizeof(ps) / sizeof(ps[0]); k++) free(*ps[k]);
     free(ns);
     o->ns = NULL;
@@ -88,6 +91,7 @@ static int ns_alloc(orc *o)
     ns->fluxi = calloc(4 * nc, sizeof(double)); ns->fluxj = calloc(4 * nc, sizeof(double));
     ns->ti_out = calloc(4 * nc, sizeof(double)); ns->qi_out = calloc(2 * nc, sizeof(double));
     ns->tj_out = calloc(4 * nc, sizeof(double)); ns->qj_out = calloc(2 * nc, sizeof(double));
+    ns->wface = calloc((size_t)16 * (o->nx > o->ny ? o->nx : o->ny), sizeof(double));
     o->ns = ns;
     if (!ns->qj_out || !ns->rk || !ns->src || !ns->sk) { orc_ns_free(o); return HYB_ERR_NOMEM; }
     return HYB_OK;
@@ -107,8 +111,75 @@ int orc_gsis_last_inner(orc *o) { return o->gsis_last_inner; }
 /* band of cells the synthetic solve updates */
 static void band(const orc *o, int *ilo, int *ihi, int *jlo, int *jhi)
 {
-    if (o->bc[0] == HYB_BC_PERIODIC) { *ilo = 1; *ihi = o->nx - 1; } else { *ilo = 3; *ihi = o->nx - 3; }
-    if (o->bc[1] == HYB_BC_PERIODIC) { *jlo = 1; *jhi = o->ny - 1; } else { *jlo = 3; *jhi = o->ny - 3; }
+    const int e = o->gsis.wall_band ? 1 : 3;
+    if (o->bc[0] == HYB_BC_PERIODIC) { *ilo = 1; *ihi = o->nx - 1; } else { *ilo = e; *ihi = o->nx - e; }
+    if (o->bc[1] == HYB_BC_PERIODIC) { *jlo = 1; *jhi = o->ny - 1; } else { *jlo = e; *jhi = o->ny - e; }
+}
+
+/* wall_band: cell k = 1, 2 into the domain and ghost k = 1, 2 outside, for
+ * face f and face cell m (faces 1 / 3: m = j, faces 2 / 4: m = i) */
+static void wall_pair(const orc *o, int f, int m, int k, size_t *ci, size_t *cg)
+{
+    if (f == 1) { *ci = C2(o, k, m); *cg = C2(o, 1 - k, m); }
+    else if (f == 3) { *ci = C2(o, o->nx - k, m); *cg = C2(o, o->nx - 1 + k, m); }
+    else if (f == 2) { *ci = C2(o, m, k); *cg = C2(o, m, 1 - k); }
+    else { *ci = C2(o, m, o->ny - k); *cg = C2(o, m, o->ny - 1 + k); }
+}
+
+/* wall_band: the kinetic state at each wall face, the mean of the first
+ * cell and its ghost (the S ghosts are the linear wall extrapolation of
+ * DETFPwall, so this is the extrapolated wall value) */
+static void wall_faces_store(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const double gam = o->prm.gamma, ma = o->prm.ma, cv = 1.0 / (gam * (gam - 1.0) * ma * ma);
+    const int mx = o->nx > o->ny ? o->nx : o->ny;
+    for (int f = 1; f <= 4; f++) {
+        if (o->bc[f - 1] != HYB_BC_WALL) continue;
+        const int n = (f == 1 || f == 3) ? o->ny - 1 : o->nx - 1;
+        for (int m = 1; m <= n; m++) {
+            size_t ci, cg;
+            wall_pair(o, f, m, 1, &ci, &cg);
+            double w[2][4];
+            for (int s2 = 0; s2 < 2; s2++) {
+                size_t c = s2 ? cg : ci;
+                double d = A4(ns->U, 0, c), u = A4(ns->U, 1, c) / d, v = A4(ns->U, 2, c) / d;
+                double t = (A4(ns->U, 3, c) - 0.5 * d * (u * u + v * v)) / (cv * d);
+                w[s2][0] = d; w[s2][1] = u; w[s2][2] = v; w[s2][3] = t;
+            }
+            for (int q = 0; q < 4; q++)
+                ns->wface[((size_t)(f - 1) * 4 + q) * mx + m] =
+                    getenv("ORC_W1") ? w[0][q] : 0.5 * (w[0][q] + w[1][q]);
+        }
+    }
+}
+
+/* wall_band: ghost layers 1, 2 by the no-slip reflection of boundary_wall
+ * (sub_boundary.f90:92-110): primitive ghost = 2 W - interior, W the frozen
+ * kinetic wall-face state */
+static void ns_wall_ghosts(orc *o)
+{
+    struct orc_ns *ns = o->ns;
+    const double gam = o->prm.gamma, ma = o->prm.ma, cv = 1.0 / (gam * (gam - 1.0) * ma * ma);
+    const int mx = o->nx > o->ny ? o->nx : o->ny;
+    for (int f = 1; f <= 4; f++) {
+        if (o->bc[f - 1] != HYB_BC_WALL) continue;
+        const int n = (f == 1 || f == 3) ? o->ny - 1 : o->nx - 1;
+        for (int m = 1; m <= n; m++)
+            for (int k = 1; k <= LAP; k++) {
+                size_t ci, cg;
+                wall_pair(o, f, m, k, &ci, &cg);
+                double d = A4(ns->U, 0, ci), u = A4(ns->U, 1, ci) / d, v = A4(ns->U, 2, ci) / d;
+                double t = (A4(ns->U, 3, ci) - 0.5 * d * (u * u + v * v)) / (cv * d);
+                const double *W = ns->wface + (size_t)(f - 1) * 4 * mx + m;
+                double d2 = 2.0 * W[0] - d, u2 = 2.0 * W[mx] - u, v2 = 2.0 * W[2 * mx] - v;
+                double t2 = 2.0 * W[3 * mx] - t;
+                A4(ns->U, 0, cg) = d2;
+                A4(ns->U, 1, cg) = d2 * u2;
+                A4(ns->U, 2, cg) = d2 * v2;
+                A4(ns->U, 3, cg) = d2 * (cv * t2 + 0.5 * (u2 * u2 + v2 * v2));
+            }
+    }
 }
 
 /* periodic ghost U from the band (the inner-boundary exchange of the NS
@@ -530,6 +601,13 @@ static void ns_adi(orc *o, int ilo, int ihi, int jlo, int jhi)
             b[k] = ALFA(cc, i, j);
             a[k] = (pery || j > jlo) ? 0.5 * ns->Lcj[cm] + ns->Lvj[cm] : 0.0;
             c[k] = (pery || j < jhi) ? 0.5 * ns->Lcj[cq] + ns->Lvj[cq] : 0.0;
+            /* wall_band: the reflected ghost beyond a wall moves with -dU of
+             * this cell, so its coupling joins the diagonal */
+            /* (the ghost takes this cell's spectral radii) */
+            if (o->gsis.wall_band && !pery && j == jlo && o->bc[1] == HYB_BC_WALL)
+                b[k] += 0.5 * ns->Lcj[cc] + ns->Lvj[cc];
+            if (o->gsis.wall_band && !pery && j == jhi && o->bc[3] == HYB_BC_WALL)
+                b[k] += 0.5 * ns->Lcj[cc] + ns->Lvj[cc];
         }
         for (int m = 0; m < 4; m++) {
             for (int k = 0; k < nj; k++) d[k] = A4(ns->Res, m, C2(o, i, jlo + k));
@@ -567,6 +645,160 @@ static void ns_adi(orc *o, int ilo, int ihi, int jlo, int jhi)
     free(a); free(b); free(c); free(d); free(x); free(w); free(d1); free(jt);
 }
 
+/* Jacobian of the Euler flux F.n (F.n as in comput_DFn, sub_LU_SGS.f90:122-144)
+ * at the conservative state U, row-major 4x4 */
+static void flux_jacobian(const double *U, double n1, double n2, double g, double *A)
+{
+    const double r = U[0], u = U[1] / r, v = U[2] / r, E = U[3];
+    const double a1 = g - 1.0, q2 = u * u + v * v, phi = 0.5 * a1 * q2;
+    const double p = a1 * (E - 0.5 * r * q2), H = (E + p) / r, un = u * n1 + v * n2;
+    const double J[16] = {0.0, n1, n2, 0.0,
+                          phi * n1 - u * un, un + u * n1 - a1 * u * n1, u * n2 - a1 * v * n1, a1 * n1,
+                          phi * n2 - v * un, v * n1 - a1 * u * n2, un + v * n2 - a1 * v * n2, a1 * n2,
+                          (phi - H) * un, H * n1 - a1 * u * un, H * n2 - a1 * v * un, g * un};
+    memcpy(A, J, sizeof(J));
+}
+
+/* x = M^-1 B for a 4x4 M and k right-hand columns (B row-major 4 x k),
+ * Gaussian elimination with partial pivoting; M is destroyed */
+static void solve4(double *M, double *B, int k)
+{
+    for (int c = 0; c < 4; c++) {
+        int pr = c;
+        for (int r = c + 1; r < 4; r++)
+            if (fabs(M[r * 4 + c]) > fabs(M[pr * 4 + c])) pr = r;
+        if (pr != c) {
+            for (int q = 0; q < 4; q++) { double t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t; }
+            for (int q = 0; q < k; q++) { double t = B[c * k + q]; B[c * k + q] = B[pr * k + q]; B[pr * k + q] = t; }
+        }
+        const double ip = 1.0 / M[c * 4 + c];
+        for (int r = c + 1; r < 4; r++) {
+            const double f = M[r * 4 + c] * ip;
+            if (f == 0.0) continue;
+            for (int q = c; q < 4; q++) M[r * 4 + q] -= f * M[c * 4 + q];
+            for (int q = 0; q < k; q++) B[r * k + q] -= f * B[c * k + q];
+        }
+    }
+    for (int c = 3; c >= 0; c--) {
+        const double ip = 1.0 / M[c * 4 + c];
+        for (int q = 0; q < k; q++) {
+            double t = B[c * k + q];
+            for (int r = c + 1; r < 4; r++) t -= M[c * 4 + r] * B[r * k + q];
+            B[c * k + q] = t * ip;
+        }
+    }
+}
+
+/* line-implicit inner solve along the wall-normal axis (ns_solver 2, no
+ * counterpart in the reference).  On every mesh line between the walls the
+ * matrix that du_LU_SGS_2D factorises (sub_LU_SGS.f90:26-111: diagonal
+ * alpha, neighbour blocks 0.5 (A s +- Lc) + Lv with A the Jacobian of the
+ * flux difference comput_DFn) is solved exactly by block-tridiagonal
+ * elimination; the neighbours along the other axis carry dU = 0 (line
+ * Jacobi).  The band edges stay explicit as in du_LU_SGS_2D. */
+static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
+{
+    struct orc_ns *ns = o->ns;
+    const double g = o->prm.gamma;
+    const int along_j = (o->bc[1] == HYB_BC_WALL);
+    const int n0 = along_j ? ilo : jlo, n1 = along_j ? ihi : jhi;     /* lines */
+    const int k0 = along_j ? jlo : ilo, k1 = along_j ? jhi : ihi;     /* cells on a line */
+    const int nk = k1 - k0 + 1;
+    double *G = malloc((size_t)nk * 16 * sizeof(double)), *gv = malloc((size_t)nk * 4 * sizeof(double));
+    if (!G || !gv) { free(G); free(gv); return HYB_ERR_NOMEM; }
+    for (int ln = n0; ln <= n1; ln++) {
+        for (int k = k0; k <= k1; k++) {
+            const int i = along_j ? ln : k, j = along_j ? k : ln;
+            const size_t c = C2(o, i, j);
+            double M[16], Bm[20];
+            const double alfa = o->vol[MI(o, i, j)] / ns->dt[c] + ns->Lci[c] + ns->Lcj[c] +
+                                2.0 * (ns->Lvi[c] + ns->Lvj[c]);
+            for (int q = 0; q < 16; q++) M[q] = 0.0;
+            for (int q = 0; q < 4; q++) M[q * 4 + q] = alfa;
+            /* right-hand sides: column 0..3 = upper coupling C, column 4 = r */
+            for (int q = 0; q < 20; q++) Bm[q] = 0.0;
+            for (int m = 0; m < 4; m++) Bm[m * 5 + 4] = A4(ns->Res, m, c);
+            /* wall_band: the ghost beyond a wall is the reflection 2 W - U
+             * of this cell (ns_wall_ghosts), dU_ghost = -dU here, so its
+             * coupling block joins the diagonal */
+            const int wlo = o->gsis.wall_band && k == k0 && o->bc[along_j ? 1 : 0] == HYB_BC_WALL;
+            const int whi = o->gsis.wall_band && k == k1 && o->bc[along_j ? 3 : 2] == HYB_BC_WALL;
+            if (k > k0 || wlo) {   /* lower neighbour: L = 0.5 (A_n s + Lc_n) + Lv_n */
+                const int ia = along_j ? i : i - 1, ja = along_j ? j - 1 : j;
+                const size_t cn = C2(o, ia, ja);
+                double Un[4], A[16];
+                get4(ns, ns->U, cn, Un);
+                const double n1f = along_j ? o->nj1[MI(o, i, j)] : o->ni1[MI(o, i, j)];
+                const double n2f = along_j ? o->nj2[MI(o, i, j)] : o->ni2[MI(o, i, j)];
+                const double sf = along_j ? o->sj[MI(o, i, j)] : o->si[MI(o, i, j)];
+                const size_t cr = wlo ? c : cn;   /* a ghost takes this cell's spectral radii */
+                const double lc = along_j ? ns->Lcj[cr] : ns->Lci[cr], lv = along_j ? ns->Lvj[cr] : ns->Lvi[cr];
+                flux_jacobian(Un, n1f, n2f, g, A);
+                double L[16];
+                for (int q = 0; q < 16; q++) L[q] = 0.5 * A[q] * sf;
+                for (int q = 0; q < 4; q++) L[q * 4 + q] += 0.5 * lc + lv;
+                if (wlo) {
+                    for (int q = 0; q < 16; q++) M[q] += L[q];
+                    goto upper;
+                }
+                /* M -= L G_{k-1}; r += L g_{k-1} */
+                const double *Gp = G + (size_t)(k - 1 - k0) * 16, *gp = gv + (size_t)(k - 1 - k0) * 4;
+                for (int r = 0; r < 4; r++) {
+                    for (int q = 0; q < 4; q++) {
+                        double t = 0.0;
+                        for (int m = 0; m < 4; m++) t += L[r * 4 + m] * Gp[m * 4 + q];
+                        M[r * 4 + q] -= t;
+                    }
+                    double t = 0.0;
+                    for (int m = 0; m < 4; m++) t += L[r * 4 + m] * gp[m];
+                    Bm[r * 5 + 4] += t;
+                }
+            }
+        upper:
+            if (k < k1 || whi) {   /* upper neighbour: C = -0.5 (A_n s - Lc_n) + Lv_n */
+                const int ia = along_j ? i : i + 1, ja = along_j ? j + 1 : j;
+                const size_t cn = C2(o, ia, ja);
+                double Un[4], A[16];
+                get4(ns, ns->U, cn, Un);
+                const double n1f = along_j ? o->nj1[MI(o, i, j)] : o->ni1[MI(o, i, j)];
+                const double n2f = along_j ? o->nj2[MI(o, i, j)] : o->ni2[MI(o, i, j)];
+                const double sf = along_j ? o->sj[MI(o, i, j + 1)] : o->si[MI(o, i + 1, j)];
+                const size_t cr = whi ? c : cn;
+                const double lc = along_j ? ns->Lcj[cr] : ns->Lci[cr], lv = along_j ? ns->Lvj[cr] : ns->Lvi[cr];
+                flux_jacobian(Un, n1f, n2f, g, A);
+                for (int r = 0; r < 4; r++)
+                    for (int q = 0; q < 4; q++) {
+                        const double cq = -0.5 * A[r * 4 + q] * sf + (r == q ? 0.5 * lc + lv : 0.0);
+                        if (whi) M[r * 4 + q] += cq;
+                        else Bm[r * 5 + q] = cq;
+                    }
+            }
+            solve4(M, Bm, 5);
+            double *Gk = G + (size_t)(k - k0) * 16, *gk = gv + (size_t)(k - k0) * 4;
+            for (int r = 0; r < 4; r++) {
+                for (int q = 0; q < 4; q++) Gk[r * 4 + q] = Bm[r * 5 + q];
+                gk[r] = Bm[r * 5 + 4];
+            }
+        }
+        /* back substitution dU_k = g_k + G_k dU_{k+1} */
+        double nxt[4] = {0, 0, 0, 0};
+        for (int k = k1; k >= k0; k--) {
+            const int i = along_j ? ln : k, j = along_j ? k : ln;
+            const double *Gk = G + (size_t)(k - k0) * 16, *gk = gv + (size_t)(k - k0) * 4;
+            double d[4];
+            for (int r = 0; r < 4; r++) {
+                double t = gk[r];
+                for (int q = 0; q < 4; q++) t += Gk[r * 4 + q] * nxt[q];
+                d[r] = t;
+            }
+            for (int r = 0; r < 4; r++) { A4(ns->dU, r, C2(o, i, j)) = d[r]; nxt[r] = d[r]; }
+        }
+    }
+    free(G);
+    free(gv);
+    return HYB_OK;
+}
+
 /* NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:4-40); returns the max
  * |Res(4)| over the band before the update (get_res, IO.f90:286-303) */
 static int ns_advance(orc *o, double *res4)
@@ -574,6 +806,7 @@ static int ns_advance(orc *o, double *res4)
     struct orc_ns *ns = o->ns;
     int ilo, ihi, jlo, jhi;
     band(o, &ilo, &ihi, &jlo, &jhi);
+    if (o->gsis.wall_band) ns_wall_ghosts(o);
     int rc = ns_prims(o);
     if (rc) return rc;
     ns_residual(o);
@@ -589,7 +822,10 @@ static int ns_advance(orc *o, double *res4)
         }
     *res4 = rmax;
     ns_lvc_dt(o);
-    if (o->gsis.ns_solver == 1) ns_adi(o, ilo, ihi, jlo, jhi);
+    if (o->gsis.ns_solver == 2) {
+        rc = ns_lines(o, ilo, ihi, jlo, jhi);
+        if (rc) return rc;
+    } else if (o->gsis.ns_solver == 1) ns_adi(o, ilo, ihi, jlo, jhi);
     else ns_lusgs(o, ilo, ihi, jlo, jhi);
     for (int j = jlo; j <= jhi; j++)
         for (int i = ilo; i <= ihi; i++)
@@ -630,6 +866,10 @@ int orc_gsis_solve(orc *o)
         for (int m = 0; m < 4; m++) A4(ns->U, m, c) = Uk[c * 4 + m];
     free(Uk);
     ns_periodic_ghosts(o);
+    if (o->gsis.wall_band) {
+        wall_faces_store(o);
+        ns_wall_ghosts(o);
+    }
     memcpy(ns->U2, ns->U, 4 * ns->nc * sizeof(double));
     /* source Q = R_K - R_NS(U_k) on the band */
     rc = ns_prims(o);
@@ -649,12 +889,23 @@ int orc_gsis_solve(orc *o)
     const int maxit = o->gsis.max_inner > 0 ? o->gsis.max_inner : 2000;
     while (res > tol && it < maxit) {
         rc = ns_advance(o, &res);
+        if (getenv("ORC_DEBUG")) fprintf(stderr, "inner %d res %.3e\n", it, res);
         if (rc) { ns->src_on = 0; return rc; }
         if (it == 0 && o->gsis.inner_rtol * res > tol) tol = o->gsis.inner_rtol * res;
         it++;
     }
     ns->src_on = 0;
     o->gsis_last_inner = it;
+    /* relax_pct: the NS change enters as r (U - U_k); the NS stress and heat
+     * flux of the final residual evaluation are scaled alike below */
+    const double rlx = o->gsis.relax_pct > 0 ? o->gsis.relax_pct / 100.0 : 1.0;
+    if (rlx != 1.0)
+        for (int j = jlo; j <= jhi; j++)
+            for (int i = ilo; i <= ihi; i++)
+                for (int m = 0; m < 4; m++) {
+                    const size_t c = C2(o, i, j);
+                    A4(ns->U, m, c) = A4(ns->U2, m, c) + rlx * (A4(ns->U, m, c) - A4(ns->U2, m, c));
+                }
     /* the band's Dirichlet edges make the NS density change non-conservative;
      * its volume-weighted mean is removed so that the correction adds no mass */
     double lam = 0.0;
@@ -690,14 +941,14 @@ int orc_gsis_solve(orc *o)
                                      A4(ns->tj_out, k, cj1));
                 double in = 0.25 * (o->tao_i_in[c * 4 + k] + o->tao_j_in[c * 4 + k] + o->tao_i_in[ci1 * 4 + k] +
                                     o->tao_j_in[cj1 * 4 + k]);
-                tao[k] = -1.0 * (out - in) * g2;
+                tao[k] = -rlx * (out - in) * g2;
             }
             for (int k = 0; k < 2; k++) {
                 double out = 0.25 * (ns->qi_out[k * ns->nc + c] + ns->qj_out[k * ns->nc + c] +
                                      ns->qi_out[k * ns->nc + ci1] + ns->qj_out[k * ns->nc + cj1]);
                 double in = 0.25 * (o->q_i_in[c * 2 + k] + o->q_j_in[c * 2 + k] + o->q_i_in[ci1 * 2 + k] +
                                     o->q_j_in[cj1 * 2 + k]);
-                q[k] = -1.0 * (out - in) * q2;
+                q[k] = -rlx * (out - in) * q2;
             }
             SG(o, 5, i, j) += tao[0];
             SG(o, 6, i, j) += tao[1];

@@ -175,6 +175,8 @@ class Oracle:
         gp.lusgs_planes = kw.get("plane_order", 0)
         gp.no_mass_projection = kw.get("no_mass_projection", 0)
         gp.correct_f = kw.get("correct_f", 0)
+        gp.wall_band = kw.get("wall_band", 0)
+        gp.relax_pct = kw.get("relax_pct", 0)
         rc = self.L.orc_gsis_configure(self.h, C.byref(gp))
         if rc != 0:
             raise RuntimeError(f"orc_gsis_configure failed: {rc}")

@@ -1,0 +1,110 @@
+"""GPU parity of the synthetic solve with the band reaching the walls and
+with the block line-implicit inner solver.
+
+wall_band extends the band of the GSIS coupling (Hybrid2D/src/Hybrid_Sub.f90:
+45-153, band 3..n-3 in sub_NS_singlegrid.f90:23-30) to the wall cells, with
+the reference's no-slip reflection of boundary_wall
+(Hybrid2D/src/sub_boundary.f90:51-118) about the kinetic state at the wall
+face.  ns_solver 2 solves the matrix of du_LU_SGS_2D
+(Hybrid2D/src/sub_LU_SGS.f90:26-111) exactly along each wall-normal line.
+The oracle (oracle/hyb_oracle_ns.c) restates both in FP64.  The GPU line
+solver eliminates in FP32 (it preconditions an FP64 residual), so its
+per-step states agree with the oracle to 1e-7 and its converged state to
+the same 1e-10 as every FP64 path.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+from test_gpu_parity import _cmp_state
+
+pytestmark = pytest.mark.gpu
+
+FIXED = dict(max_inner=12, inner_tol=0.0, inner_rtol=0.0)
+
+
+@pytest.fixture(scope="module")
+def cases_mod(pkg):
+    from hyb_gb300 import cases
+    return cases
+
+
+def _pair(case, precision, **gk):
+    from hyb_gb300 import abi
+    g = abi.Solver(case, precision=precision)
+    o = O.Oracle(case, threads=0)
+    g.init_maxwellian()
+    o.init_maxwellian()
+    o.convert_ns()
+    g.gsis(**gk)
+    o.gsis(**gk)
+    return g, o
+
+
+def _shape(cases_mod, shape, **kw):
+    if shape == "small":
+        return cases_mod.couette_small(ncy=32, nvx=16, nvy=16, **kw)
+    if shape == "transposed":
+        return cases_mod.couette_small(ncx=40, ncy=8, nvx=12, nvy=12, **kw)
+    return cases_mod.couette_small(ncx=16, ncy=96, nvx=12, nvy=12, t_pert=0.1, **kw)
+
+
+@pytest.mark.parametrize("shape", ["small", "transposed", "sine"])
+def test_wall_band_lusgs_matches_oracle(cases_mod, shape):
+    c = _shape(cases_mod, shape, dt=0.02)
+    g, o = _pair(c, 0, wall_band=1, correct_f=1, cfl=20.0, **FIXED)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    _cmp_state(c, g, o, 1e-10)
+
+
+@pytest.mark.parametrize("shape", ["small", "transposed", "sine"])
+def test_line_solver_matches_oracle(cases_mod, shape):
+    c = _shape(cases_mod, shape, dt=1.0e6, sweep_order=1, mass_pin=1)
+    g, o = _pair(c, 0, wall_band=1, correct_f=1, ns_solver=2, cfl=100.0, **FIXED)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    _cmp_state(c, g, o, 1e-7)
+
+
+def test_relaxed_correction_matches_oracle(cases_mod):
+    c = _shape(cases_mod, "small", dt=0.02)
+    g, o = _pair(c, 0, wall_band=1, correct_f=1, relax_pct=70, cfl=20.0, **FIXED)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    _cmp_state(c, g, o, 1e-10)
+
+
+def test_line_solver_gsis_converges_to_the_oracle_fixed_point(cases_mod):
+    """Kn 0.01 channel (4 x 128 cells, 48^2 velocities on [-6, 6], plates
+    +-0.5, walls 1 / 1.2) with the upwind-ordered kinetic step at dt 1e6,
+    the mass pin, the wall band and the line solver: residual 1e-8 within
+    120 outer iterations; run on to 1e-11, the converged moments equal the
+    oracle's run of the same iteration to 1e-10."""
+    c = cases_mod.Case(name="kn0.01-4x128", ncx=4, ncy=128, nvx=48, nvy=48, vmax=6.0, kn=0.01, uw=0.5,
+                       t_top=1.2, dt=1.0e6, sweep_order=1, mass_pin=1)
+    gk = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=300.0, max_inner=20, inner_tol=0.0, inner_rtol=1e-4)
+    g, o = _pair(c, 0, **gk)
+    it, it8 = 0, None
+    while it < 240:
+        rg = g.step(10)
+        ro = o.step(10)
+        it += 10
+        if it8 is None and rg["max_rms"] < 1e-8:
+            it8 = it
+        if max(rg["max_rms"], ro["max_rms"]) < 1e-11:
+            break
+    assert it8 is not None and it8 <= 120, (it8, rg)
+    assert rg["max_rms"] < 1e-11 and ro["max_rms"] < 1e-11, (it, rg, ro)
+    sg, _ = g.moments()
+    so = o.s_gkua()
+    n = (c.ny + 7, c.nx + 7, 11)
+    Sg = sg.reshape(n)[4:4 + c.ny - 1, 4:4 + c.nx - 1, :10]
+    So = so.reshape(n)[4:4 + c.ny - 1, 4:4 + c.nx - 1, :10]
+    for k in range(10):
+        d = np.abs(Sg[..., k] - So[..., k]).max()
+        assert d <= 1e-10 * max(np.abs(So[..., k]).max(), 1e-2), (k, d)
