@@ -18,7 +18,7 @@ EXPORTS = [
     "hyb_create", "hyb_destroy", "hyb_last_error", "hyb_version",
     "hyb_init_maxwellian", "hyb_upload_f", "hyb_download_f", "hyb_download_moments",
     "hyb_download_hot", "hyb_download_hoq", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
-    "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner",
+    "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner", "hyb_gsis_skipped",
     "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
     "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc", "hyb_autotune",
     "hyb_batch_create", "hyb_batch_destroy", "hyb_batch_last_error", "hyb_batch_size",
@@ -68,6 +68,7 @@ def load(path=None):
     L.hyb_detfp_res.argtypes = [vp, vp]
     L.hyb_gsis_configure.argtypes = [vp, vp]
     L.hyb_gsis_last_inner.argtypes = [vp, C.POINTER(ip)]
+    L.hyb_gsis_skipped.argtypes = [vp, C.POINTER(ip)]
     L.hyb_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.hyb_last_step_ms.argtypes = [vp, dp]
     L.hyb_stream.argtypes = [vp, C.POINTER(vp)]
@@ -232,6 +233,11 @@ class Solver:
     def gsis_last_inner(self):
         n = C.c_int(0)
         self._ck(self.L.hyb_gsis_last_inner(self.h, C.byref(n)), "gsis_last_inner")
+        return n.value
+
+    def gsis_skipped(self):
+        n = C.c_int(0)
+        self._ck(self.L.hyb_gsis_skipped(self.h, C.byref(n)), "gsis_skipped")
         return n.value
 
     # ---- state ---------------------------------------------------------------

@@ -779,6 +779,7 @@ int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp) {
     if (!ctx || !gp) return HYB_ERR_INVALID;
     ctx->gsis = *gp;
     ctx->gsis_outer = 0;
+    ctx->gsis_skipped = 0;
     ctx->warm_done = 0;
     if (gp->enable) return hyb::ns_create(ctx);
     return HYB_OK;
@@ -787,6 +788,12 @@ int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp) {
 int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner) {
     if (!ctx || !n_inner) return HYB_ERR_INVALID;
     *n_inner = ctx->gsis_last_inner;
+    return HYB_OK;
+}
+
+int hyb_gsis_skipped(const hyb_ctx *ctx, int *count) {
+    if (!ctx || !count) return HYB_ERR_INVALID;
+    *count = ctx->gsis_skipped;
     return HYB_OK;
 }
 

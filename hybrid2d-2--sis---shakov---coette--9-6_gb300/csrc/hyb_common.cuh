@@ -120,6 +120,7 @@ struct hyb_ctx {
     // GSIS
     hyb_gsis_params gsis;
     int gsis_last_inner;
+    int gsis_skipped;                      // corrections skipped since hyb_gsis_configure
     hyb_mlp *mlp;                          // learned closure for the warm start (not owned)
     int gsis_outer;                        // outer iterations since hyb_gsis_configure
     int warm_done;                         // the scheduled warm start has run (2: fell back)

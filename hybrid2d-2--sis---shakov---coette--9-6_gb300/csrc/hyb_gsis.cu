@@ -723,13 +723,15 @@ __global__ void k_ns_wallghost(NsDev D) {
 // On every mesh line between the walls the matrix du_LU_SGS_2D factorises
 // (sub_LU_SGS.f90:26-111: diagonal alpha, neighbour blocks 0.5 (A s +- Lc) +
 // Lv, A the Jacobian of the flux difference comput_DFn) is solved by
-// block-tridiagonal elimination with partial pivoting inside the 4x4 blocks;
-// the neighbours along the other axis carry dU = 0.  With wall_band the
-// reflected ghost moves with -dU of the wall cell, so its coupling block
-// joins that cell's diagonal.  One thread per line.  The elimination is in
-// FP32: it is the preconditioner of the inner iteration, whose residual and
-// update stay FP64, so it sets the rate but not the solution.  Scratch
-// D.lin holds G[16] and g[4] per cell as floats.
+// block-tridiagonal elimination; the lines go in red-black order (colour 0,
+// 1, 0), each with the current dU of its neighbouring lines on the right-hand
+// side (line Gauss-Seidel).  With wall_band the reflected ghost moves with
+// -dU of the wall cell, so its coupling block joins that cell's diagonal.
+// Lines of up to PCR_MAX cells are reduced by one CTA each (parallel cyclic
+// reduction, one row per thread, the line in shared memory); longer lines
+// by one thread each (sequential elimination, scratch in D.lin).  The
+// elimination is FP32: it preconditions the inner iteration, whose residual
+// and update stay FP64, so it sets the rate but not the solution.
 __device__ __forceinline__ void flux_jac(const double *U, double n1, double n2, double g, float *A) {
     const double r = U[0], u = U[1] / r, v = U[2] / r, E = U[3];
     const double a1 = g - 1.0, q2 = u * u + v * v, phi = 0.5 * a1 * q2;
@@ -781,117 +783,331 @@ __device__ __forceinline__ void solve4f(float *M, float *B) {
     }
 }
 
-__global__ void k_ns_blines(NsDev D) {
-    if (D.ctrl->done) return;
-    const bool along_j = !D.pery;
-    const int n0 = along_j ? D.ilo : D.jlo, n1 = along_j ? D.ihi : D.jhi;
-    const int k0 = along_j ? D.jlo : D.ilo, k1 = along_j ? D.jhi : D.ihi;
-    const int ln = n0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (ln > n1) return;
+// geometry of the lines: they run along the wall-normal axis; the lines
+// are numbered along the other axis
+struct LineGeo {
+    bool along_j, per;        // per: the line index is periodic
+    int n0, n1, k0, k1;       // lines n0..n1, cells k0..k1 on a line
+};
+__device__ __forceinline__ LineGeo line_geo(const NsDev &D) {
+    LineGeo G;
+    G.along_j = !D.pery;
+    G.per = G.along_j ? D.perx != 0 : D.pery != 0;
+    G.n0 = G.along_j ? D.ilo : D.jlo;
+    G.n1 = G.along_j ? D.ihi : D.jhi;
+    G.k0 = G.along_j ? D.jlo : D.ilo;
+    G.k1 = G.along_j ? D.jhi : D.ihi;
+    return G;
+}
+// the line of colour `col` served by block b: colour 0 = even offsets from
+// n0, colour 1 = odd offsets, colour 2 = the last line of an odd periodic
+// count (it meets line n0 across the seam); -1 past the end
+__device__ __forceinline__ int line_of(const LineGeo &G, int col, int b) {
+    const int nl = G.n1 - G.n0 + 1;
+    const bool odd_seam = G.per && (nl & 1);
+    if (col == 2) return (odd_seam && b == 0) ? G.n1 : -1;
+    const int ln = G.n0 + col + 2 * b;
+    if (ln > G.n1 || (odd_seam && ln == G.n1)) return -1;
+    return ln;
+}
+__host__ __device__ inline int lines_of_colour(int nl, bool per, int col) {
+    const bool odd_seam = per && (nl & 1);
+    if (col == 2) return odd_seam ? 1 : 0;
+    const int m = odd_seam ? nl - 1 : nl;
+    return col == 0 ? (m + 1) / 2 : m / 2;
+}
+
+// one row of the line system A dU_{k-1} + B dU_k + C dU_{k+1} = d, in the
+// oracle's terms A = -L, C = -C_up, B = alpha I (+ the wall ghost's block),
+// d = Res + the neighbouring lines' terms from their current dU
+__device__ void line_row(const NsDev &D, const LineGeo &G, int ln, int k, float *A, float *B, float *C, float *d) {
+    const bool aj = G.along_j;
+    const int i = aj ? ln : k, j = aj ? k : ln;
+    const size_t c = c2(D, i, j), nc = D.nc;
     const double g = D.gamma;
-    float *Gs = reinterpret_cast<float *>(D.lin);            // [16][nc]
-    float *gs = Gs + 16 * D.nc;                              // [4][nc]
-    for (int k = k0; k <= k1; k++) {
-        const int i = along_j ? ln : k, j = along_j ? k : ln;
-        const size_t c = c2(D, i, j);
-        const double alfa = D.vol[mi(D, i, j)] / D.dt[c] + D.Lci[c] + D.Lcj[c] + 2.0 * (D.Lvi[c] + D.Lvj[c]);
-        float M[16], Bm[20];
+    const float alfa = (float)(D.vol[mi(D, i, j)] / D.dt[c] + D.Lci[c] + D.Lcj[c] + 2.0 * (D.Lvi[c] + D.Lvj[c]));
 #pragma unroll
-        for (int q = 0; q < 16; q++) M[q] = 0.f;
+    for (int q = 0; q < 16; q++) { A[q] = 0.f; B[q] = 0.f; C[q] = 0.f; }
 #pragma unroll
-        for (int q = 0; q < 4; q++) M[q * 4 + q] = (float)alfa;
+    for (int q = 0; q < 4; q++) B[q * 4 + q] = alfa;
+    const bool walls = aj ? !D.pery : !D.perx;
+    const bool wlo = D.wall_band && walls && k == G.k0, whi = D.wall_band && walls && k == G.k1;
+    const double n1f = aj ? D.nj1[mi(D, i, j)] : D.ni1[mi(D, i, j)];
+    const double n2f = aj ? D.nj2[mi(D, i, j)] : D.ni2[mi(D, i, j)];
+    if (k > G.k0 || wlo) {   // lower neighbour: L = 0.5 (A s + Lc) + Lv
+        const size_t cn = aj ? c2(D, i, j - 1) : c2(D, i - 1, j), cr = wlo ? c : cn;
+        double Un[4];
 #pragma unroll
-        for (int q = 0; q < 20; q++) Bm[q] = 0.f;
+        for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * nc + cn];
+        const float sf = (float)(aj ? D.sj[mi(D, i, j)] : D.si[mi(D, i, j)]);
+        const float dg = (float)(0.5 * (aj ? D.Lcj[cr] : D.Lci[cr]) + (aj ? D.Lvj[cr] : D.Lvi[cr]));
+        float J[16];
+        flux_jac(Un, n1f, n2f, g, J);
 #pragma unroll
-        for (int m = 0; m < 4; m++) Bm[m * 5 + 4] = (float)D.Res[(size_t)m * D.nc + c];
-        const bool walls = along_j ? !D.pery : !D.perx;
-        const bool wlo = D.wall_band && walls && k == k0;
-        const bool whi = D.wall_band && walls && k == k1;
-        const double n1f = along_j ? D.nj1[mi(D, i, j)] : D.ni1[mi(D, i, j)];
-        const double n2f = along_j ? D.nj2[mi(D, i, j)] : D.ni2[mi(D, i, j)];
-        if (k > k0 || wlo) {   // lower neighbour: L = 0.5 (A s + Lc) + Lv
-            const size_t cn = along_j ? c2(D, i, j - 1) : c2(D, i - 1, j);
-            const size_t cr = wlo ? c : cn;
-            double Un[4];
+        for (int q = 0; q < 16; q++) {
+            const float L = 0.5f * J[q] * sf + ((q % 5) == 0 ? dg : 0.f);
+            if (wlo) B[q] += L;
+            else A[q] = -L;
+        }
+    }
+    if (k < G.k1 || whi) {   // upper neighbour: C_up = -0.5 (A s - Lc) + Lv
+        const size_t cn = aj ? c2(D, i, j + 1) : c2(D, i + 1, j), cr = whi ? c : cn;
+        double Un[4];
 #pragma unroll
-            for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * D.nc + cn];
-            const double sf = along_j ? D.sj[mi(D, i, j)] : D.si[mi(D, i, j)];
-            const double lc = along_j ? D.Lcj[cr] : D.Lci[cr], lv = along_j ? D.Lvj[cr] : D.Lvi[cr];
-            float A[16], L[16];
-            flux_jac(Un, n1f, n2f, g, A);
+        for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * nc + cn];
+        const float sf = (float)(aj ? D.sj[mi(D, i, j + 1)] : D.si[mi(D, i + 1, j)]);
+        const float dg = (float)(0.5 * (aj ? D.Lcj[cr] : D.Lci[cr]) + (aj ? D.Lvj[cr] : D.Lvi[cr]));
+        float J[16];
+        flux_jac(Un, n1f, n2f, g, J);
 #pragma unroll
-            for (int q = 0; q < 16; q++) L[q] = 0.5f * A[q] * (float)sf;
+        for (int q = 0; q < 16; q++) {
+            const float Cu = -0.5f * J[q] * sf + ((q % 5) == 0 ? dg : 0.f);
+            if (whi) B[q] += Cu;
+            else C[q] = -Cu;
+        }
+    }
+    // the neighbouring lines (the other axis's blocks of du_LU_SGS_2D)
+    float t[4] = {0.f, 0.f, 0.f, 0.f};
+    const int p = ln;
+    for (int side = 0; side < 2; side++) {
+        int q = side == 0 ? p - 1 : p + 1;
+        if (q < G.n0 || q > G.n1) {
+            if (!G.per) continue;
+            q = q < G.n0 ? G.n1 : G.n0;
+        }
+        const int in = aj ? q : i, jn = aj ? j : q;
+        const size_t cn = c2(D, in, jn);
+        double Un[4];
+        float dn[4], J[16];
 #pragma unroll
-            for (int q = 0; q < 4; q++) L[q * 4 + q] += (float)(0.5 * lc + lv);
-            if (wlo) {
+        for (int m = 0; m < 4; m++) {
+            Un[m] = D.U[(size_t)m * nc + cn];
+            dn[m] = (float)D.dU[(size_t)m * nc + cn];
+        }
+        const double m1 = aj ? D.ni1[mi(D, i, j)] : D.nj1[mi(D, i, j)];
+        const double m2 = aj ? D.ni2[mi(D, i, j)] : D.nj2[mi(D, i, j)];
+        const float dg = (float)(0.5 * (aj ? D.Lci[cn] : D.Lcj[cn]) + (aj ? D.Lvi[cn] : D.Lvj[cn]));
+        const float sf = (float)(side == 0 ? (aj ? D.si[mi(D, i, j)] : D.sj[mi(D, i, j)])
+                                           : (aj ? D.si[mi(D, i + 1, j)] : D.sj[mi(D, i, j + 1)]));
+        const float sg = side == 0 ? 0.5f : -0.5f;
+        flux_jac(Un, m1, m2, g, J);
 #pragma unroll
-                for (int q = 0; q < 16; q++) M[q] += L[q];
-            } else {
-                const size_t cp = along_j ? c2(D, i, j - 1) : c2(D, i - 1, j);
-                float Gp[16], gp[4];
+        for (int r = 0; r < 4; r++) {
+            float v = dg * dn[r];
 #pragma unroll
-                for (int q = 0; q < 16; q++) Gp[q] = Gs[(size_t)q * D.nc + cp];
+            for (int m = 0; m < 4; m++) v += sg * J[r * 4 + m] * sf * dn[m];
+            t[r] += v;
+        }
+    }
 #pragma unroll
-                for (int q = 0; q < 4; q++) gp[q] = gs[(size_t)q * D.nc + cp];
+    for (int m = 0; m < 4; m++) d[m] = (float)D.Res[(size_t)m * nc + c] + t[m];
+}
+
+// Inv = M^-1 (Gauss-Jordan with partial pivoting); M is destroyed
+__device__ __forceinline__ void inv4f(float *M, float *Inv) {
 #pragma unroll
-                for (int r = 0; r < 4; r++) {
+    for (int q = 0; q < 16; q++) Inv[q] = (q % 5) == 0 ? 1.f : 0.f;
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        float t = 0.f;
+    for (int c = 0; c < 4; c++) {
+        int pr = c;
 #pragma unroll
-                        for (int m = 0; m < 4; m++) t += L[r * 4 + m] * Gp[m * 4 + q];
-                        M[r * 4 + q] -= t;
-                    }
-                    float t = 0.f;
+        for (int r = c + 1; r < 4; r++)
+            if (fabsf(M[r * 4 + c]) > fabsf(M[pr * 4 + c])) pr = r;
 #pragma unroll
-                    for (int m = 0; m < 4; m++) t += L[r * 4 + m] * gp[m];
-                    Bm[r * 5 + 4] += t;
-                }
+        for (int q = 0; q < 4; q++) {
+            if (pr != c) {
+                float t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t;
+                t = Inv[c * 4 + q]; Inv[c * 4 + q] = Inv[pr * 4 + q]; Inv[pr * 4 + q] = t;
             }
         }
-        if (k < k1 || whi) {   // upper neighbour: C = -0.5 (A s - Lc) + Lv
-            const size_t cn = along_j ? c2(D, i, j + 1) : c2(D, i + 1, j);
-            const size_t cr = whi ? c : cn;
-            double Un[4];
+        const float ip = 1.f / M[c * 4 + c];
 #pragma unroll
-            for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * D.nc + cn];
-            const double sf = along_j ? D.sj[mi(D, i, j + 1)] : D.si[mi(D, i + 1, j)];
-            const double lc = along_j ? D.Lcj[cr] : D.Lci[cr], lv = along_j ? D.Lvj[cr] : D.Lvi[cr];
-            float A[16];
-            flux_jac(Un, n1f, n2f, g, A);
+        for (int q = 0; q < 4; q++) { M[c * 4 + q] *= ip; Inv[c * 4 + q] *= ip; }
 #pragma unroll
-            for (int r = 0; r < 4; r++)
+        for (int r = 0; r < 4; r++) {
+            if (r == c) continue;
+            const float f = M[r * 4 + c];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const float cq = -0.5f * A[r * 4 + q] * (float)sf + (r == q ? (float)(0.5 * lc + lv) : 0.f);
-                    if (whi) M[r * 4 + q] += cq;
-                    else Bm[r * 5 + q] = cq;
-                }
+            for (int q = 0; q < 4; q++) { M[r * 4 + q] -= f * M[c * 4 + q]; Inv[r * 4 + q] -= f * Inv[c * 4 + q]; }
+        }
+    }
+}
+
+__device__ __forceinline__ void mm4(const float *X, const float *Y, float *Z) {   // Z = X Y
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float t = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; m++) t += X[r * 4 + m] * Y[m * 4 + q];
+            Z[r * 4 + q] = t;
+        }
+}
+
+// Parallel cyclic reduction of one line per CTA, one row per thread (lines
+// of at most PCR_MAX cells).  Step with stride s: with a = -A_k B_{k-s}^-1
+// and c = -C_k B_{k+s}^-1, A' = a A_{k-s}, C' = c C_{k+s},
+// B' = B_k + a C_{k-s} + c A_{k+s}, d' = d_k + a d_{k-s} + c d_{k+s}; after
+// ceil(log2 n) steps every row is decoupled and dU_k = B_k^-1 d_k.
+constexpr int PCR_MAX = 512;
+__global__ void __launch_bounds__(PCR_MAX, 1) k_ns_lines_pcr(NsDev D, int col) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int ln = line_of(G, col, blockIdx.x);
+    if (ln < 0) return;
+    const int n = G.k1 - G.k0 + 1, k = threadIdx.x;
+    extern __shared__ float pcr_sm[];
+    float *sA = pcr_sm, *sB = sA + 16 * n, *sC = sB + 16 * n, *sD = sC + 16 * n, *sI = sD + 4 * n;
+    float A[16], B[16], C[16], d[4];
+    if (k < n) {
+        line_row(D, G, ln, G.k0 + k, A, B, C, d);
+#pragma unroll
+        for (int q = 0; q < 16; q++) { sA[k * 16 + q] = A[q]; sB[k * 16 + q] = B[q]; sC[k * 16 + q] = C[q]; }
+#pragma unroll
+        for (int q = 0; q < 4; q++) sD[k * 4 + q] = d[q];
+    }
+    __syncthreads();
+    for (int st = 1; st < n; st <<= 1) {
+        if (k < n) {
+            float M[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) M[q] = B[q];
+            inv4f(M, sI + k * 16);
+        }
+        __syncthreads();
+        if (k < n) {
+            float a[16], c[16], T[16];
+            const bool hl = k - st >= 0, hu = k + st < n;
+#pragma unroll
+            for (int q = 0; q < 16; q++) { a[q] = 0.f; c[q] = 0.f; }
+            if (hl) {
+                mm4(A, sI + (k - st) * 16, T);
+#pragma unroll
+                for (int q = 0; q < 16; q++) a[q] = -T[q];
+            }
+            if (hu) {
+                mm4(C, sI + (k + st) * 16, T);
+#pragma unroll
+                for (int q = 0; q < 16; q++) c[q] = -T[q];
+            }
+            float nA[16], nC[16];
+            if (hl) {
+                mm4(a, sA + (k - st) * 16, nA);
+                mm4(a, sC + (k - st) * 16, T);
+#pragma unroll
+                for (int q = 0; q < 16; q++) B[q] += T[q];
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int m = 0; m < 4; m++) d[r] += a[r * 4 + m] * sD[(k - st) * 4 + m];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; q++) nA[q] = 0.f;
+            }
+            if (hu) {
+                mm4(c, sC + (k + st) * 16, nC);
+                mm4(c, sA + (k + st) * 16, T);
+#pragma unroll
+                for (int q = 0; q < 16; q++) B[q] += T[q];
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int m = 0; m < 4; m++) d[r] += c[r * 4 + m] * sD[(k + st) * 4 + m];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; q++) nC[q] = 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 16; q++) { A[q] = nA[q]; C[q] = nC[q]; }
+        }
+        __syncthreads();
+        if (k < n) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) { sA[k * 16 + q] = A[q]; sB[k * 16 + q] = B[q]; sC[k * 16 + q] = C[q]; }
+#pragma unroll
+            for (int q = 0; q < 4; q++) sD[k * 4 + q] = d[q];
+        }
+        __syncthreads();
+    }
+    if (k < n) {
+        float M[16], Bi[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) M[q] = B[q];
+        inv4f(M, Bi);
+        const int i = G.along_j ? ln : G.k0 + k, j = G.along_j ? G.k0 + k : ln;
+        const size_t c = c2(D, i, j);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            float t = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; m++) t += Bi[r * 4 + m] * d[m];
+            D.dU[(size_t)r * D.nc + c] = (double)t;
+        }
+    }
+}
+
+// lines longer than PCR_MAX cells: block-tridiagonal elimination, one
+// thread per line; G[16] and g[4] per cell in the float view of D.lin
+__global__ void k_ns_lines_seq(NsDev D, int col) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int ln = line_of(G, col, blockIdx.x * blockDim.x + threadIdx.x);
+    if (ln < 0) return;
+    float *Gs = reinterpret_cast<float *>(D.lin);            // [16][nc]
+    float *gs = Gs + 16 * D.nc;                              // [4][nc]
+    size_t cp = 0;
+    for (int k = G.k0; k <= G.k1; k++) {
+        const int i = G.along_j ? ln : k, j = G.along_j ? k : ln;
+        const size_t c = c2(D, i, j);
+        float A[16], M[16], C[16], r[4], Bm[20];
+        line_row(D, G, ln, k, A, M, C, r);
+        // row: A x_{k-1} + M x_k + C x_{k+1} = r, x_{k-1} = g_{k-1} + G_{k-1} x_k
+        if (k > G.k0) {
+            float Gp[16], gp[4], T[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) Gp[q] = Gs[(size_t)q * D.nc + cp];
+#pragma unroll
+            for (int q = 0; q < 4; q++) gp[q] = gs[(size_t)q * D.nc + cp];
+            mm4(A, Gp, T);
+#pragma unroll
+            for (int q = 0; q < 16; q++) M[q] += T[q];
+#pragma unroll
+            for (int rr = 0; rr < 4; rr++)
+#pragma unroll
+                for (int m = 0; m < 4; m++) r[rr] -= A[rr * 4 + m] * gp[m];
+        }
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) Bm[rr * 5 + q] = -C[rr * 4 + q];
+            Bm[rr * 5 + 4] = r[rr];
         }
         solve4f<5>(M, Bm);
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
+        for (int rr = 0; rr < 4; rr++) {
 #pragma unroll
-            for (int q = 0; q < 4; q++) Gs[(size_t)(r * 4 + q) * D.nc + c] = Bm[r * 5 + q];
-            gs[(size_t)r * D.nc + c] = Bm[r * 5 + 4];
+            for (int q = 0; q < 4; q++) Gs[(size_t)(rr * 4 + q) * D.nc + c] = Bm[rr * 5 + q];
+            gs[(size_t)rr * D.nc + c] = Bm[rr * 5 + 4];
         }
+        cp = c;
     }
     float nxt[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k = k1; k >= k0; k--) {
-        const int i = along_j ? ln : k, j = along_j ? k : ln;
+    for (int k = G.k1; k >= G.k0; k--) {
+        const int i = G.along_j ? ln : k, j = G.along_j ? k : ln;
         const size_t c = c2(D, i, j);
         float d[4];
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            float t = gs[(size_t)r * D.nc + c];
+        for (int rr = 0; rr < 4; rr++) {
+            float t = gs[(size_t)rr * D.nc + c];
 #pragma unroll
-            for (int q = 0; q < 4; q++) t += Gs[(size_t)(r * 4 + q) * D.nc + c] * nxt[q];
-            d[r] = t;
+            for (int q = 0; q < 4; q++) t += Gs[(size_t)(rr * 4 + q) * D.nc + c] * nxt[q];
+            d[rr] = t;
         }
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            D.dU[(size_t)r * D.nc + c] = (double)d[r];
-            nxt[r] = d[r];
+        for (int rr = 0; rr < 4; rr++) {
+            D.dU[(size_t)rr * D.nc + c] = (double)d[rr];
+            nxt[rr] = d[rr];
         }
     }
 }
@@ -1365,8 +1581,9 @@ int ns_create(hyb_ctx *ctx) {
     ns_band(ctx, D);
     D.nc = (size_t)(D.nx + 3) * (D.ny + 3);
     const size_t nc = D.nc;
-    // see the pointer carve below; the last term holds the wall-face states
-    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6 + 1;
+    // see the pointer carve below; the wall-face states follow the last array
+    const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6;
+    const size_t nwf = (size_t)16 * (D.nx > D.ny ? D.nx : D.ny);
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
     if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
@@ -1381,14 +1598,14 @@ int ns_create(hyb_ctx *ctx) {
         return HYB_ERR_NOMEM;
     }
     cudaMemsetAsync(st->rk, 0, 4 * ncell * sizeof(double), ctx->stream);
-    if (cudaMalloc((void **)&st->buf, (size_t)ncomp * nc * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc((void **)&st->buf, ((size_t)ncomp * nc + nwf) * sizeof(double)) != cudaSuccess) {
         cudaFree(st->rk);
         cudaFree(ctx->d_rhs_gsis);
         ctx->d_rhs_gsis = nullptr;
         delete st;
         return HYB_ERR_NOMEM;
     }
-    cudaMemsetAsync(st->buf, 0, (size_t)ncomp * nc * sizeof(double), ctx->stream);
+    cudaMemsetAsync(st->buf, 0, ((size_t)ncomp * nc + nwf) * sizeof(double), ctx->stream);
     double *h = st->buf;
     D.U = h; h += 4 * nc; D.src = h; h += 4 * nc; D.U2 = h; h += 4 * nc; D.dU = h; h += 4 * nc; D.Res = h; h += 4 * nc;
     D.dt = h; h += nc; D.Lci = h; h += nc; D.Lcj = h; h += nc; D.Lvi = h; h += nc; D.Lvj = h; h += nc;
@@ -1398,7 +1615,7 @@ int ns_create(hyb_ctx *ctx) {
     D.ti_out = h; h += 4 * nc; D.qi_out = h; h += 2 * nc; D.tj_out = h; h += 4 * nc; D.qj_out = h; h += 2 * nc;
     D.lin = h; h += 16 * nc;
     D.sk = h; h += 6 * nc;
-    D.wface = h; h += nc;   // 16 * max(nx, ny) <= (nx + 3)(ny + 3) for nx, ny >= 3
+    D.wface = h; h += nwf;  // [4 faces][rho u v T][max(nx, ny)]
     const size_t nm = (size_t)ctx->nx * ctx->ny;
     if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
         cudaFree(st->buf);
@@ -1457,6 +1674,10 @@ int ns_create(hyb_ctx *ctx) {
     }
     D.ctrl = st->ctrl;
     st->have_graph = false;
+    // the line solver's reduction holds a line of up to PCR_MAX cells in
+    // shared memory (set before any capture)
+    cudaFuncSetAttribute(k_ns_lines_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(68 * PCR_MAX * sizeof(float)));
     {
         // enough blocks for one cell per thread, within what is co-resident
         int dev = 0, coop = 0, per_sm = 0, nsm = 0;
@@ -1497,8 +1718,19 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
     k_ns_faces<<<(nfj + bs - 1) / bs, bs, 0, s>>>(D, 1);
     k_ns_res<<<(ncell + bs - 1) / bs, bs, 0, s>>>(D);
     if (ctx->gsis.ns_solver == 2) {
-        const int nl = D.pery ? D.jhi - D.jlo + 1 : D.ihi - D.ilo + 1;
-        k_ns_blines<<<(nl + 31) / 32, 32, 0, s>>>(D);
+        // red-black line Gauss-Seidel: colour 0, 1, (2), 0
+        const bool aj = !D.pery;
+        const int nl = aj ? D.ihi - D.ilo + 1 : D.jhi - D.jlo + 1, nk = aj ? D.jhi - D.jlo + 1 : D.ihi - D.ilo + 1;
+        const bool per = aj ? D.perx != 0 : D.pery != 0;
+        const int order[4] = {0, 1, 2, 0};
+        for (int ph = 0; ph < 4; ph++) {
+            const int col = order[ph], cnt = lines_of_colour(nl, per, col);
+            if (cnt == 0) continue;
+            if (nk <= PCR_MAX)
+                k_ns_lines_pcr<<<cnt, PCR_MAX, (size_t)68 * nk * sizeof(float), s>>>(D, col);
+            else
+                k_ns_lines_seq<<<(cnt + 31) / 32, 32, 0, s>>>(D, col);
+        }
     } else if (ctx->gsis.ns_solver == 1) {
         const int ncol = D.ihi - D.ilo + 1, nrow = D.jhi - D.jlo + 1;
         k_ns_jlines<<<(4 * ncol + 63) / 64, 64, 0, s>>>(D);
@@ -1514,7 +1746,15 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
 }
 
 static int inner_launches(const hyb_ctx *ctx, const NsDev &D) {
-    const int solver = ctx->gsis.ns_solver == 2 ? 1 : (ctx->gsis.ns_solver == 1 ? 2 : 4);
+    int lines = 0;
+    if (ctx->gsis.ns_solver == 2) {
+        const bool aj = !D.pery;
+        const int nl = aj ? D.ihi - D.ilo + 1 : D.jhi - D.jlo + 1;
+        const bool per = aj ? D.perx != 0 : D.pery != 0;
+        lines = 2 * (lines_of_colour(nl, per, 0) > 0) + (lines_of_colour(nl, per, 1) > 0) +
+                (lines_of_colour(nl, per, 2) > 0);
+    }
+    const int solver = ctx->gsis.ns_solver == 2 ? lines : (ctx->gsis.ns_solver == 1 ? 2 : 4);
     return 6 + solver + (D.mlp_on ? 2 : 0) + (D.wall_band ? 1 : 0);
 }
 
@@ -1629,8 +1869,15 @@ int gsis_solve(hyb_ctx *ctx) {
         }
     }
     ctx->gsis_last_inner = st->h_ctrl->it;
+    if (st->h_ctrl->err == HYB_ERR_TEMPERATURE || st->h_ctrl->err == HYB_ERR_NONFINITE) {
+        // the NS state left the physical range: this outer iteration keeps
+        // its kinetic step uncorrected (the reference STOPs,
+        // sub_NS_singlegrid.f90:148-151)
+        ctx->gsis_skipped++;
+        return HYB_OK;
+    }
     if (st->h_ctrl->err) {
-        ctx->last_error = "synthetic solve: temperature below 0.1 or non-finite residual";
+        ctx->last_error = "synthetic solve: bounded wait expired";
         return st->h_ctrl->err;
     }
     if (D.relax != 1.0) {

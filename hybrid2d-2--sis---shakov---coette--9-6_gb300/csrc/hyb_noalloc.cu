@@ -9,15 +9,16 @@
 //
 // The velocity-slice partial sums live in the file-scope device array
 // g_detfp_scratch (16 MiB, HYB_NOALLOC_MAX_CELLS cells at one slice).  Host
-// code cannot pass the symbol itself to a kernel: its address is looked up
-// once per device with cudaGetSymbolAddress, with that device current, on the
-// first call made on the device.  All calls share the array; every partial is
-// written before it is read, so nothing needs clearing between calls, but
-// calls that overlap on the GPU (different streams) race on it.
+// code cannot pass the symbol itself to a kernel: every call looks up its
+// address with cudaGetSymbolAddress on the current device and context (no
+// allocation; the first call on a device also loads this library's device
+// code there, so make it before any stream capture).  All calls share the
+// array; every partial is written before it is read, so nothing needs
+// clearing between calls, but calls that overlap on the GPU (different
+// streams) race on it.
 #include <cuda_runtime.h>
 #include <math.h>
-
-#include <mutex>
+#include <stdint.h>
 
 #include "hyb_common.cuh"
 
@@ -26,18 +27,16 @@ namespace {
 constexpr size_t kScratchDoubles = (size_t)HYB_NOALLOC_MAX_CELLS * 10;
 static __device__ __align__(256) double g_detfp_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// moments of one velocity slice for the cells of one j-row (FRD layout
-// FRD(NRD,-3:nx+3,-3:ny+3,NVI,NVJ), GaussLegendre sums of GKUA_DETFP.f90:315-345)
+// moments of one velocity slice for one interior cell per thread (FRD layout
+// FRD(NRD,-3:nx+3,-3:ny+3,NVI,NVJ), GaussLegendre sums of GKUA_DETFP.f90:315-345);
+// the cells i fastest along a 1-D grid, the slice along grid z
 __global__ void k_detfp_na_part(const double *__restrict__ frd, int nx, int ny, int nvi, int nvj, int vs,
                                 const double *__restrict__ vi, const double *__restrict__ vj,
                                 const double *__restrict__ wi, const double *__restrict__ wj,
                                 double *__restrict__ part) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, slice = blockIdx.z;
-    if (i > nx - 1) return;
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= (size_t)(nx - 1) * (ny - 1)) return;
+    const int i = (int)(cell % (nx - 1)) + 1, j = (int)(cell / (nx - 1)) + 1, slice = blockIdx.z;
     const int pw = nx + 7;
     const size_t P = (size_t)(nx + 7) * (ny + 7);
     const size_t ix = (size_t)(i + 3) + (size_t)pw * (j + 3);
@@ -50,8 +49,8 @@ __global__ void k_detfp_na_part(const double *__restrict__ frd, int nx, int ny, 
         for (int iv = 0; iv < nvi; iv++) {
             const double vx = vi[iv], w = wi[iv] * wy;
             const size_t v = (size_t)iv + (size_t)nvi * jv;
-            const double2 gh = *reinterpret_cast<const double2 *>(frd + (v * P + ix) * 2);
-            const double g = gh.x, h = gh.y;
+            // two scalar loads: the caller's FRD needs only double alignment
+            const double g = frd[(v * P + ix) * 2], h = frd[(v * P + ix) * 2 + 1];
             const double vxg = vx * g, vyg = vy * g, vx2g = vx * vxg, vy2g = vy * vyg;
             const double b4 = h + vx2g + vy2g;
             s[0] += w * g;
@@ -110,21 +109,21 @@ __global__ void k_detfp_na_finish(int nx, int ny, int vs, const double *__restri
     if (cf) cf[hyb_c2(nx, i, j)] = (x1s <= (double)1.e-8f) ? cfc * S1 : cfc * S1 * pow(tt, x1s);
 }
 
-// device address of the scratch array for the current device (set up once)
+// device address of the scratch array in the current device and context,
+// looked up on every call (a cached address could belong to a context that
+// was reset or to another context of the same device)
 int scratch_for_current_device(double **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return HYB_ERR_NODEVICE;
-    if (dev < 0 || dev >= kMaxDevices) return HYB_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        double *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_detfp_scratch);
-        if (e != cudaSuccess || p == nullptr) return HYB_ERR_CUDA;
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    double *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_detfp_scratch);
+    if (e != cudaSuccess || p == nullptr) return HYB_ERR_CUDA;
+    *out = p;
     return HYB_OK;
 }
+
+// every device array is read or written as doubles
+inline bool double_aligned(const void *p) { return ((uintptr_t)p & (sizeof(double) - 1)) == 0; }
 
 }  // namespace
 
@@ -133,6 +132,11 @@ extern "C" int hyb_detfp_noalloc(int nx, int ny, int nvi, int nvj, const double 
                                  const hyb_params *p, double *s_gkua_dev, double *cf_dev, void *stream) {
     if (nx < 3 || ny < 3 || nvi < 1 || nvj < 1 || !frd_dev || !vi_dev || !vj_dev || !wi_dev || !wj_dev || !p ||
         !s_gkua_dev)
+        return HYB_ERR_INVALID;
+    // checked before any CUDA call: a misaligned pointer would fault the
+    // caller's context instead of returning
+    if (!double_aligned(frd_dev) || !double_aligned(vi_dev) || !double_aligned(vj_dev) || !double_aligned(wi_dev) ||
+        !double_aligned(wj_dev) || !double_aligned(s_gkua_dev) || (cf_dev && !double_aligned(cf_dev)))
         return HYB_ERR_INVALID;
     const size_t ncell = (size_t)(nx - 1) * (ny - 1);
     if (ncell > (size_t)HYB_NOALLOC_MAX_CELLS) return HYB_ERR_UNSUPPORTED;   // scratch would not hold one slice
@@ -145,7 +149,7 @@ extern "C" int hyb_detfp_noalloc(int nx, int ny, int nvi, int nvj, const double 
     if (vs > nvj) vs = nvj;
     if (vs < 1) vs = 1;
     cudaStream_t st = (cudaStream_t)stream;
-    dim3 blk(128), grd((unsigned)((nx - 1 + 127) / 128), (unsigned)(ny - 1), (unsigned)vs);
+    dim3 blk(128), grd((unsigned)((ncell + 127) / 128), 1, (unsigned)vs);
     k_detfp_na_part<<<grd, blk, 0, st>>>(frd_dev, nx, ny, nvi, nvj, vs, vi_dev, vj_dev, wi_dev, wj_dev, scratch);
     if (cudaGetLastError() != cudaSuccess) return HYB_ERR_CUDA;
     k_detfp_na_finish<<<(unsigned)((ncell + 255) / 256), 256, 0, st>>>(nx, ny, vs, scratch, p->cfc, p->x1s, p->r00,

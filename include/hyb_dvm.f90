@@ -137,6 +137,11 @@ module hyb_dvm
        type(c_ptr), value :: ctx
        integer(c_int), intent(out) :: n_inner
      end function
+     integer(c_int) function hyb_gsis_skipped(ctx, count) bind(c, name="hyb_gsis_skipped")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), intent(out) :: count
+     end function
      integer(c_int) function hyb_set_walls(ctx, face, wall_u, wall_v, wall_t) bind(c, name="hyb_set_walls")
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: ctx

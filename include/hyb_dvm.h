@@ -165,8 +165,11 @@ typedef struct hyb_gsis_params {
     int    ns_solver;       /* inner solver: 0 LU-SGS (du_LU_SGS_2D,
                                sub_LU_SGS.f90), 1 line-implicit ADI with the
                                LU-SGS diagonal and scalar couplings, exact
-                               along each mesh line (no counterpart in the
-                               reference)                                    */
+                               along each mesh line, 2 the LU-SGS matrix
+                               with its 4x4 flux-Jacobian blocks solved
+                               exactly along every wall-normal line, lines
+                               in red-black Gauss-Seidel order (1 and 2 have
+                               no counterpart in the reference)             */
     int    correct_f;       /* 1: after the moment correction also correct the
                                distribution, f += feq(S) - feq(S_k) on the band
                                (the reference corrects the moments only)     */
@@ -248,6 +251,12 @@ int hyb_detfp_res(hyb_ctx *ctx, hyb_residual *out);   /* DETFP_res         */
 int hyb_gsis_configure(hyb_ctx *ctx, const hyb_gsis_params *gp);
 /* Inner NS iterations used by the last outer iteration (Mesh%iter). */
 int hyb_gsis_last_inner(const hyb_ctx *ctx, int *n_inner);
+/* Outer iterations since hyb_gsis_configure whose synthetic correction was
+ * skipped because the NS state left the physical range (temperature below
+ * 0.1 or a non-finite residual): such an iteration keeps its kinetic step
+ * uncorrected, where the reference STOPs (sub_NS_singlegrid.f90:148-151).
+ * No counterpart in the reference. */
+int hyb_gsis_skipped(const hyb_ctx *ctx, int *count);
 
 /* Replace the diffuse-wall data of one wall face (1..4), one value per face
  * cell as in hyb_mesh.  The reference passes the wall velocity on every call
@@ -272,11 +281,14 @@ int hyb_set_walls(hyb_ctx *ctx, int face, const double *wall_u,
  *   cf_dev      CF on the (1-LAP:nx+LAP-1, 1-LAP:ny+LAP-1) extents, or NULL
  *   stream      cudaStream_t to launch on (NULL: default stream)
  * Limits: at most HYB_NOALLOC_MAX_CELLS interior cells, else
- * HYB_ERR_UNSUPPORTED.  Intermediate sums live in one fixed 16 MiB device
- * array of the library, held by every device that loads the library until
- * the process exits; the first call on a device looks up that array's
- * address (make it before any stream capture).  Calls share the array, so
- * calls that overlap on the GPU (e.g. on two streams) race. */
+ * HYB_ERR_UNSUPPORTED; every device pointer double-aligned (8 bytes), else
+ * HYB_ERR_INVALID before any launch.  Intermediate sums live in one fixed
+ * 16 MiB device array of the library, held by every device that loads the
+ * library until the process exits; each call looks up that array's address
+ * in the current context, and the first call on a device also loads the
+ * library's device code there (make it before any stream capture).  Calls
+ * share the array, so calls that overlap on the GPU (e.g. on two streams)
+ * race. */
 #define HYB_NOALLOC_MAX_CELLS 209715
 int hyb_detfp_noalloc(int nx, int ny, int nvi, int nvj, const double *frd_dev,
                       const double *vi_dev, const double *vj_dev,

@@ -1249,8 +1249,12 @@ int orc_step(orc *o, int n_iter, hyb_residual *r)
         orc_detfp(o);
         orc_convert_ns(o);
         if (o->gsis.enable) {
+            /* a synthetic solve that leaves the physical range corrects
+             * nothing: the kinetic step of this iteration stands (the
+             * reference STOPs, sub_NS_singlegrid.f90:148-151) */
             int rc = orc_gsis_solve(o);
-            if (rc) return rc;
+            if (rc == HYB_ERR_TEMPERATURE || rc == HYB_ERR_NONFINITE) o->gsis_skipped++;
+            else if (rc) return rc;
         }
     }
     if (r) orc_detfp_res(o, r);

@@ -62,6 +62,7 @@ double  orc_err(orc *o);                /* DETFP's CF-change diagnostic ERR     
 /* GSIS synthetic solve (hyb_oracle_ns.c) */
 int orc_gsis_configure(orc *o, const hyb_gsis_params *gp);
 int orc_gsis_last_inner(orc *o);
+int orc_gsis_skipped(orc *o);           /* corrections skipped since configure */
 int orc_ns_state(orc *o, double *U);                  /* U[4][(nx+3)(ny+3)] */
 int orc_ns_residual(orc *o, const double *U, double *res);
 

@@ -45,6 +45,8 @@ struct orc {
     struct orc_ns *ns;           /* GSIS synthetic solver state (hyb_oracle_ns.c) */
     hyb_gsis_params gsis;
     int gsis_last_inner;
+    int gsis_skipped;     /* outer iterations whose synthetic correction was
+                             skipped (NS state out of range)                */
 };
 
 /* ---- index helpers ------------------------------------------------------ */

@@ -41,7 +41,6 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
-#include <stdio.h>
 
 struct orc_ns {
     size_t nc;
@@ -102,11 +101,13 @@ int orc_gsis_configure(orc *o, const hyb_gsis_params *gp)
     if (!o || !gp) return HYB_ERR_INVALID;
     if (gp->enable && fabs(o->prm.gamma - 5.0 / 3.0) > 1e-9) return HYB_ERR_UNSUPPORTED;
     o->gsis = *gp;
+    o->gsis_skipped = 0;
     if (gp->enable) return ns_alloc(o);
     return HYB_OK;
 }
 
 int orc_gsis_last_inner(orc *o) { return o->gsis_last_inner; }
+int orc_gsis_skipped(orc *o) { return o->gsis_skipped; }
 
 /* band of cells the synthetic solve updates */
 static void band(const orc *o, int *ilo, int *ihi, int *jlo, int *jhi)
@@ -148,8 +149,7 @@ static void wall_faces_store(orc *o)
                 w[s2][0] = d; w[s2][1] = u; w[s2][2] = v; w[s2][3] = t;
             }
             for (int q = 0; q < 4; q++)
-                ns->wface[((size_t)(f - 1) * 4 + q) * mx + m] =
-                    getenv("ORC_W1") ? w[0][q] : 0.5 * (w[0][q] + w[1][q]);
+                ns->wface[((size_t)(f - 1) * 4 + q) * mx + m] = 0.5 * (w[0][q] + w[1][q]);
         }
     }
 }
@@ -694,8 +694,46 @@ static void solve4(double *M, double *B, int k)
  * matrix that du_LU_SGS_2D factorises (sub_LU_SGS.f90:26-111: diagonal
  * alpha, neighbour blocks 0.5 (A s +- Lc) + Lv with A the Jacobian of the
  * flux difference comput_DFn) is solved exactly by block-tridiagonal
- * elimination; the neighbours along the other axis carry dU = 0 (line
- * Jacobi).  The band edges stay explicit as in du_LU_SGS_2D. */
+ * elimination; the lines are taken in red-black order, each with the
+ * current dU of its neighbouring lines (line Gauss-Seidel).  The band edges
+ * stay explicit as in du_LU_SGS_2D, except a wall edge of wall_band, whose
+ * reflected ghost moves with -dU of the wall cell. */
+/* the other axis's neighbour terms of cell (i, j) from the current dU of
+ * the neighbouring lines (the i- or j-direction blocks of du_LU_SGS_2D,
+ * linearised: lower 0.5 (A s + Lc) + Lv, upper -0.5 (A s - Lc) + Lv) */
+static void cross_terms(orc *o, int i, int j, int along_j, int per, int lo, int hi, double *t)
+{
+    struct orc_ns *ns = o->ns;
+    const double g = o->prm.gamma;
+    for (int m = 0; m < 4; m++) t[m] = 0.0;
+    const int p = along_j ? i : j;
+    for (int side = 0; side < 2; side++) {
+        int q = side == 0 ? p - 1 : p + 1;
+        if (q < lo || q > hi) {
+            if (!per) continue;
+            q = q < lo ? hi : lo;
+        }
+        const int in = along_j ? q : i, jn = along_j ? j : q;
+        const size_t cn = C2(o, in, jn);
+        double Un[4], A[16], d[4];
+        get4(ns, ns->U, cn, Un);
+        get4(ns, ns->dU, cn, d);
+        const double n1f = along_j ? o->ni1[MI(o, i, j)] : o->nj1[MI(o, i, j)];
+        const double n2f = along_j ? o->ni2[MI(o, i, j)] : o->nj2[MI(o, i, j)];
+        const double lc = along_j ? ns->Lci[cn] : ns->Lcj[cn], lv = along_j ? ns->Lvi[cn] : ns->Lvj[cn];
+        double sf;
+        if (side == 0) sf = along_j ? o->si[MI(o, i, j)] : o->sj[MI(o, i, j)];
+        else sf = along_j ? o->si[MI(o, i + 1, j)] : o->sj[MI(o, i, j + 1)];
+        flux_jacobian(Un, n1f, n2f, g, A);
+        const double sg = side == 0 ? 0.5 : -0.5;
+        for (int r = 0; r < 4; r++) {
+            double v = (0.5 * lc + lv) * d[r];
+            for (int m = 0; m < 4; m++) v += sg * A[r * 4 + m] * sf * d[m];
+            t[r] += v;
+        }
+    }
+}
+
 static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
 {
     struct orc_ns *ns = o->ns;
@@ -703,10 +741,21 @@ static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
     const int along_j = (o->bc[1] == HYB_BC_WALL);
     const int n0 = along_j ? ilo : jlo, n1 = along_j ? ihi : jhi;     /* lines */
     const int k0 = along_j ? jlo : ilo, k1 = along_j ? jhi : ihi;     /* cells on a line */
-    const int nk = k1 - k0 + 1;
+    const int nk = k1 - k0 + 1, nl = n1 - n0 + 1;
+    const int per = along_j ? (o->bc[0] == HYB_BC_PERIODIC) : (o->bc[1] == HYB_BC_PERIODIC);
     double *G = malloc((size_t)nk * 16 * sizeof(double)), *gv = malloc((size_t)nk * 4 * sizeof(double));
     if (!G || !gv) { free(G); free(gv); return HYB_ERR_NOMEM; }
+    memset(ns->dU, 0, 4 * ns->nc * sizeof(double));
+    /* red-black line Gauss-Seidel: colour 0 (even offsets from n0), 1 (odd),
+     * 2 (the last line of an odd periodic count, which meets line n0 across
+     * the seam), then colour 0 again; a line takes the current dU of its
+     * neighbouring lines */
+    const int order[4] = {0, 1, 2, 0};
+    for (int ph = 0; ph < 4; ph++)
     for (int ln = n0; ln <= n1; ln++) {
+        int col = (ln - n0) & 1;
+        if (per && (nl & 1) && ln == n1) col = 2;
+        if (col != order[ph]) continue;
         for (int k = k0; k <= k1; k++) {
             const int i = along_j ? ln : k, j = along_j ? k : ln;
             const size_t c = C2(o, i, j);
@@ -717,7 +766,9 @@ static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
             for (int q = 0; q < 4; q++) M[q * 4 + q] = alfa;
             /* right-hand sides: column 0..3 = upper coupling C, column 4 = r */
             for (int q = 0; q < 20; q++) Bm[q] = 0.0;
-            for (int m = 0; m < 4; m++) Bm[m * 5 + 4] = A4(ns->Res, m, c);
+            double xt[4];
+            cross_terms(o, i, j, along_j, per, n0, n1, xt);
+            for (int m = 0; m < 4; m++) Bm[m * 5 + 4] = A4(ns->Res, m, c) + xt[m];
             /* wall_band: the ghost beyond a wall is the reflection 2 W - U
              * of this cell (ns_wall_ghosts), dU_ghost = -dU here, so its
              * coupling block joins the diagonal */
@@ -889,7 +940,6 @@ int orc_gsis_solve(orc *o)
     const int maxit = o->gsis.max_inner > 0 ? o->gsis.max_inner : 2000;
     while (res > tol && it < maxit) {
         rc = ns_advance(o, &res);
-        if (getenv("ORC_DEBUG")) fprintf(stderr, "inner %d res %.3e\n", it, res);
         if (rc) { ns->src_on = 0; return rc; }
         if (it == 0 && o->gsis.inner_rtol * res > tol) tol = o->gsis.inner_rtol * res;
         it++;

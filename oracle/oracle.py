@@ -52,6 +52,7 @@ def lib():
         L.orc_cfc_vhs.restype = C.c_double
         L.orc_gsis_configure.argtypes = [vp, vp]
         L.orc_gsis_last_inner.argtypes = [vp]
+        L.orc_gsis_skipped.argtypes = [vp]
         L.orc_ns_state.argtypes = [vp, dp]
         L.orc_ns_residual.argtypes = [vp, dp, dp]
         _lib = L
@@ -183,6 +184,9 @@ class Oracle:
 
     def gsis_last_inner(self):
         return self.L.orc_gsis_last_inner(self.h)
+
+    def gsis_skipped(self):
+        return self.L.orc_gsis_skipped(self.h)
 
     def ns_state(self):
         nc = (self.nx + 3) * (self.ny + 3)

@@ -108,3 +108,21 @@ def test_scan_axis_size_limits(lib, pkg, ncy, ok):
             lib.hyb_destroy(h)
     else:
         assert rc == T.HYB_ERR_UNSUPPORTED
+
+
+def test_detfp_noalloc_rejects_misaligned_pointers_before_any_launch(lib, pkg):
+    """hyb_detfp_noalloc reads and writes the caller's device arrays as
+    doubles: a pointer that is not 8-byte aligned (an offset array section,
+    say) is refused with HYB_ERR_INVALID before any CUDA call, so it never
+    reaches a kernel.  The pointers here are never dereferenced."""
+    from hyb_gb300 import cases, hyb_types as T
+    p = cases.couette_small(ncy=16, nvx=4, nvy=4).params()
+    good, odd = C.c_void_p(0x10000), C.c_void_p(0x10004)
+    for k in range(6):
+        ptrs = [good] * 6
+        ptrs[k] = odd
+        frd, vi, vj, wi, wj, s = ptrs
+        rc = lib.hyb_detfp_noalloc(5, 17, 4, 4, frd, vi, vj, wi, wj, C.byref(p), s, None, None)
+        assert rc == T.HYB_ERR_INVALID, k
+    rc = lib.hyb_detfp_noalloc(5, 17, 4, 4, good, good, good, good, good, C.byref(p), good, odd, None)
+    assert rc == T.HYB_ERR_INVALID

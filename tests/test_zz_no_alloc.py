@@ -30,6 +30,8 @@ def _cudart():
             L.cudaFree.argtypes = [C.c_void_p]
             L.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
             L.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+            L.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+            L.cudaDeviceSynchronize.argtypes = []
             return L
         except OSError:
             continue
@@ -96,6 +98,56 @@ def test_detfp_noalloc_matches_context_path(pkg, shape):
                 assert np.abs(a[..., k] - b[..., k]).max() <= 1e-12 * scale, (call, k)
             ca, cb = _cf_interior(c, cf_out), _cf_interior(c, cf_ref)
             assert np.abs(ca - cb).max() <= 1e-12 * np.abs(cb).max(), call
+    finally:
+        for b in bufs:
+            b.free()
+
+
+def _free_bytes(rt):
+    assert rt.cudaDeviceSynchronize() == 0
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+def test_detfp_noalloc_allocates_nothing_up_to_its_limit(pkg):
+    """Near HYB_NOALLOC_MAX_CELLS (409 x 512 cells) the scratch holds one
+    velocity slice, so each slice sums several velocity rows; the result
+    still matches the context path, and the device's free memory is the same
+    before and after calls at the smallest and the largest accepted sizes."""
+    from hyb_gb300 import abi, cases
+    rt = _cudart()
+    c = cases.couette_small(ncx=409, ncy=512, nvx=6, nvy=6, dt=0.02)
+    assert c.cells <= MAX_CELLS and 2 * c.cells > MAX_CELLS
+    g = abi.Solver(c, precision=0)
+    g.init_maxwellian()
+    g.step(1)
+    frd = g.download_f()
+    s_ref, cf_ref = g.moments()
+    g.close()
+    small = cases.couette_small(ncy=16, nvx=4, nvy=4)
+    vi, wi, vj, wj = (np.ascontiguousarray(a, dtype=np.float64) for a in c.vgrid())
+    bufs = [DevBuf(rt, a) for a in (frd, vi, vj, wi, wj, np.zeros_like(s_ref), np.zeros_like(cf_ref))]
+    dfrd, dvi, dvj, dwi, dwj, ds, dcf = bufs
+    p = c.params()
+    L = abi.load()
+    try:
+        args = (c.nx, c.ny, c.nvx, c.nvy, dfrd.p, dvi.p, dvj.p, dwi.p, dwj.p, C.byref(p), ds.p, dcf.p, None)
+        assert L.hyb_detfp_noalloc(*args) == 0            # first call on the device: set-up
+        free0 = _free_bytes(rt)
+        for call in range(2):
+            ds.fill(0xFF)
+            assert L.hyb_detfp_noalloc(*args) == 0
+            # the small mesh reads the same (larger) buffers: any valid sub-range will do
+            assert L.hyb_detfp_noalloc(small.nx, small.ny, 4, 4, dfrd.p, dvi.p, dvj.p, dwi.p, dwj.p, C.byref(p),
+                                       dcf.p, None, None) == 0
+            ds.fill(0xFF)
+            assert L.hyb_detfp_noalloc(*args) == 0
+            a, b = _interior(c, ds.get(s_ref)), _interior(c, s_ref)
+            for k in range(10):
+                scale = max(np.abs(b[..., k]).max(), 1e-3)
+                assert np.abs(a[..., k] - b[..., k]).max() <= 1e-12 * scale, (call, k)
+        assert _free_bytes(rt) == free0
     finally:
         for b in bufs:
             b.free()
