@@ -15,12 +15,12 @@ LIB_PATH = os.path.join(HERE, "_build", "libhyb_gb300.so")
 
 # every symbol declared in include/hyb_dvm.h
 EXPORTS = [
-    "hyb_create", "hyb_destroy", "hyb_last_error", "hyb_version",
+    "hyb_create", "hyb_destroy", "hyb_last_error", "hyb_version", "hyb_set_precision",
     "hyb_init_maxwellian", "hyb_upload_f", "hyb_download_f", "hyb_download_moments",
     "hyb_download_hot", "hyb_download_hoq", "hyb_step", "hyb_phy_boundary", "hyb_kinetic_step", "hyb_detfp",
     "hyb_convert_ns", "hyb_detfp_res", "hyb_gsis_configure", "hyb_gsis_last_inner", "hyb_gsis_skipped",
     "hyb_launch_count", "hyb_last_step_ms", "hyb_stream", "hyb_set_walls",
-    "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc", "hyb_autotune",
+    "hyb_profile_enable", "hyb_profile_read", "hyb_detfp_noalloc", "hyb_autotune", "hyb_test_stall",
     "hyb_batch_create", "hyb_batch_destroy", "hyb_batch_last_error", "hyb_batch_size",
     "hyb_batch_instance", "hyb_batch_init_maxwellian", "hyb_batch_autotune", "hyb_batch_step",
     "hyb_batch_last_step_ms", "hyb_batch_launch_count",
@@ -69,6 +69,8 @@ def load(path=None):
     L.hyb_gsis_configure.argtypes = [vp, vp]
     L.hyb_gsis_last_inner.argtypes = [vp, C.POINTER(ip)]
     L.hyb_gsis_skipped.argtypes = [vp, C.POINTER(ip)]
+    L.hyb_test_stall.argtypes = [vp, ip, C.c_longlong]
+    L.hyb_set_precision.argtypes = [vp, ip]
     L.hyb_launch_count.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.hyb_last_step_ms.argtypes = [vp, dp]
     L.hyb_stream.argtypes = [vp, C.POINTER(vp)]
@@ -234,6 +236,14 @@ class Solver:
         n = C.c_int(0)
         self._ck(self.L.hyb_gsis_last_inner(self.h, C.byref(n)), "gsis_last_inner")
         return n.value
+
+    def set_precision(self, precision):
+        """Promote a mixed context to FP64 on the device (hyb_set_precision)."""
+        self._ck(self.L.hyb_set_precision(self.h, precision), "set_precision")
+
+    def test_stall(self, site, spin_cycles):
+        """Arm a planted wait that nothing completes for the next step."""
+        self._ck(self.L.hyb_test_stall(self.h, site, spin_cycles), "test_stall")
 
     def gsis_skipped(self):
         n = C.c_int(0)

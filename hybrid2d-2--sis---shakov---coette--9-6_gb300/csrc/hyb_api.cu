@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "hyb_common.cuh"
+#include "hyb_device.cuh"
 
 namespace hyb {
 size_t hot_doubles(int nx, int ny);
@@ -169,6 +170,45 @@ inline size_t dev_cell(const hyb_ctx *c, int i, int j) {
     return (size_t)(b - 1) * c->PA + (a - 1);
 }
 
+// cell volumes and face normals times lengths in the sweep's (a,b) layout
+void kinetic_geometry(const hyb_ctx *c, std::vector<double> &vol, std::vector<double> &gA1,
+                      std::vector<double> &gA2, std::vector<double> &gB1, std::vector<double> &gB2) {
+    const size_t ncell = (size_t)c->Nb * c->PA;
+    vol.assign(ncell, 1.0);
+    gA1.assign((size_t)c->Nb * (c->PA + 1), 0.0);
+    gA2.assign(gA1.size(), 0.0);
+    gB1.assign((size_t)(c->Nb + 1) * c->PA, 0.0);
+    gB2.assign(gB1.size(), 0.0);
+    const int nx = c->nx;
+    for (int b = 1; b <= c->Nb; b++)
+        for (int a = 1; a <= c->Na; a++) {
+            int i = c->scan_is_j ? b : a, j = c->scan_is_j ? a : b;
+            vol[(size_t)(b - 1) * c->PA + (a - 1)] = c->vol[MI(nx, i, j)];
+        }
+    for (int b = 1; b <= c->Nb; b++)
+        for (int q = 1; q <= c->Na + 1; q++) {
+            size_t k = (size_t)(b - 1) * (c->PA + 1) + (q - 1);
+            if (c->scan_is_j) {   // j-face (i=b, j=q)
+                gA1[k] = c->nj1[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
+                gA2[k] = c->nj2[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
+            } else {              // i-face (i=q, j=b)
+                gA1[k] = c->ni1[MI(nx, q, b)] * c->si[MI(nx, q, b)];
+                gA2[k] = c->ni2[MI(nx, q, b)] * c->si[MI(nx, q, b)];
+            }
+        }
+    for (int q = 1; q <= c->Nb + 1; q++)
+        for (int a = 1; a <= c->Na; a++) {
+            size_t k = (size_t)(q - 1) * c->PA + (a - 1);
+            if (c->scan_is_j) {   // i-face (i=q, j=a)
+                gB1[k] = c->ni1[MI(nx, q, a)] * c->si[MI(nx, q, a)];
+                gB2[k] = c->ni2[MI(nx, q, a)] * c->si[MI(nx, q, a)];
+            } else {              // j-face (i=a, j=q)
+                gB1[k] = c->nj1[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
+                gB2[k] = c->nj2[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
+            }
+        }
+}
+
 // Sweep layout of a mesh: the scan axis is the longer one that fits one CTA
 // row (<= 1024 cells); cells per sweep thread (cpt) tile the scan axis
 // exactly; the padded row PA holds 32 * cpt-cell chunks and a thread group
@@ -315,36 +355,9 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         return rc;
     }
     // geometry in the (a,b) layout
-    std::vector<double> vol(ncell, 1.0), gA1((size_t)c->Nb * (c->PA + 1), 0.0), gA2(gA1.size(), 0.0);
-    std::vector<double> gB1((size_t)(c->Nb + 1) * c->PA, 0.0), gB2(gB1.size(), 0.0);
+    std::vector<double> vol, gA1, gA2, gB1, gB2;
+    kinetic_geometry(c, vol, gA1, gA2, gB1, gB2);
     const int nx = c->nx;
-    for (int b = 1; b <= c->Nb; b++)
-        for (int a = 1; a <= c->Na; a++) {
-            int i = c->scan_is_j ? b : a, j = c->scan_is_j ? a : b;
-            vol[(size_t)(b - 1) * c->PA + (a - 1)] = c->vol[MI(nx, i, j)];
-        }
-    for (int b = 1; b <= c->Nb; b++)
-        for (int q = 1; q <= c->Na + 1; q++) {
-            size_t k = (size_t)(b - 1) * (c->PA + 1) + (q - 1);
-            if (c->scan_is_j) {   // j-face (i=b, j=q)
-                gA1[k] = c->nj1[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
-                gA2[k] = c->nj2[MI(nx, b, q)] * c->sj[MI(nx, b, q)];
-            } else {              // i-face (i=q, j=b)
-                gA1[k] = c->ni1[MI(nx, q, b)] * c->si[MI(nx, q, b)];
-                gA2[k] = c->ni2[MI(nx, q, b)] * c->si[MI(nx, q, b)];
-            }
-        }
-    for (int q = 1; q <= c->Nb + 1; q++)
-        for (int a = 1; a <= c->Na; a++) {
-            size_t k = (size_t)(q - 1) * c->PA + (a - 1);
-            if (c->scan_is_j) {   // i-face (i=q, j=a)
-                gB1[k] = c->ni1[MI(nx, q, a)] * c->si[MI(nx, q, a)];
-                gB2[k] = c->ni2[MI(nx, q, a)] * c->si[MI(nx, q, a)];
-            } else {              // j-face (i=a, j=q)
-                gB1[k] = c->nj1[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
-                gB2[k] = c->nj2[MI(nx, a, q)] * c->sj[MI(nx, a, q)];
-            }
-        }
     // uniform Cartesian spacing: one face speed per axis and one volume
     {
         auto same = [](const std::vector<double> &x, size_t n0, size_t n, size_t stride, size_t len) {
@@ -420,6 +433,8 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         return HYB_ERR_UNSUPPORTED;
     }
     c->gsis.enable = 0;
+    c->spin_cycles = HYB_SPIN_CYCLES;
+    c->stall_site = HYB_STALL_NONE;
     // launch-shape override, "cpt,vpb,minb"
     if (const char *e = getenv("HYB_SWEEP_SHAPE")) {
         int a = 0, b = 0, d = 0;
@@ -431,6 +446,87 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
     }
     *out = c;
     return HYB_OK;
+}
+
+// FP32 -> FP64, element by element (every FP32 value is exact in FP64)
+__global__ void k_widen(const float *__restrict__ src, double *__restrict__ dst, size_t n) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        dst[k] = (double)src[k];
+}
+
+// Promotes a mixed-precision context to FP64 on the device: f is widened in
+// place of the FP32 array, the other precision-typed buffers are made anew
+// (wall slots, RHS and Shakhov parameters are recomputed from f by the next
+// passes, the geometry is uploaded again) and DETFP is rerun on the FP64 f.
+int hyb_set_precision(hyb_ctx *ctx, int precision) {
+    if (!ctx) return HYB_ERR_INVALID;
+    if (precision == ctx->precision) return HYB_OK;
+    if (precision != HYB_PREC_FP64 || ctx->precision != HYB_PREC_MIXED) return HYB_ERR_UNSUPPORTED;
+    if (ctx->in_batch) {
+        ctx->last_error = "set_precision: the instance belongs to a batch";
+        return HYB_ERR_UNSUPPORTED;
+    }
+    cudaSetDevice(ctx->dev);
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    const size_t ncell = (size_t)ctx->Nb * ctx->PA, fsz = (size_t)ctx->nv * 2 * ncell;
+    double *f64 = nullptr;
+    if (cudaMalloc((void **)&f64, fsz * sizeof(double)) != cudaSuccess) {
+        ctx->last_error = "set_precision: device allocation of the FP64 distribution failed";
+        return HYB_ERR_NOMEM;
+    }
+    k_widen<<<152 * 8, 256, 0, ctx->stream>>>((const float *)ctx->d_f, f64, fsz);
+    ctx->launches++;
+    HYB_CK(cudaGetLastError());
+    HYB_CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_f);
+    ctx->d_f = f64;
+    // the other buffers of the distribution's type, at FP64 size
+    auto remake = [&](void **p, size_t n) -> int {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        if (cudaMalloc(p, n * sizeof(double)) != cudaSuccess) {
+            ctx->last_error = "set_precision: device allocation failed";
+            return HYB_ERR_NOMEM;
+        }
+        return cudaMemsetAsync(*p, 0, n * sizeof(double), ctx->stream) == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+    };
+    int rc = remake(&ctx->d_rhs, fsz);
+    for (int f = 0; f < 4 && !rc; f++) {
+        if (!ctx->d_fw[f]) continue;
+        int on_scan = ctx->scan_is_j ? (f == 1 || f == 3) : (f == 0 || f == 2);
+        rc = remake(&ctx->d_fw[f], (size_t)ctx->nv * 2 * (on_scan ? ctx->Nb : ctx->PA));
+    }
+    if (!rc) rc = remake(&ctx->d_eqp, 8 * ncell);
+    if (!rc) rc = remake(&ctx->d_vol, ncell);
+    if (!rc) rc = remake(&ctx->d_gA1, (size_t)ctx->Nb * (ctx->PA + 1));
+    if (!rc) rc = remake(&ctx->d_gA2, (size_t)ctx->Nb * (ctx->PA + 1));
+    if (!rc) rc = remake(&ctx->d_gB1, (size_t)(ctx->Nb + 1) * ctx->PA);
+    if (!rc) rc = remake(&ctx->d_gB2, (size_t)(ctx->Nb + 1) * ctx->PA);
+    if (rc) return rc;
+    ctx->precision = HYB_PREC_FP64;
+    ctx->prm.precision = HYB_PREC_FP64;
+    ctx->real_size = sizeof(double);
+    std::vector<double> vol, gA1, gA2, gB1, gB2;
+    kinetic_geometry(ctx, vol, gA1, gA2, gB1, gB2);
+    rc = upload_real(ctx, ctx->d_vol, vol);
+    if (!rc) rc = upload_real(ctx, ctx->d_gA1, gA1);
+    if (!rc) rc = upload_real(ctx, ctx->d_gA2, gA2);
+    if (!rc) rc = upload_real(ctx, ctx->d_gB1, gB1);
+    if (!rc) rc = upload_real(ctx, ctx->d_gB2, gB2);
+    if (rc) return rc;
+    // launch shapes chosen for FP32 rows no longer apply
+    ctx->sw_cpt = ctx->sw_vpb = ctx->sw_minb = 0;
+    if (ctx->gsis.enable) {   // the synthetic solve's RHS store has the distribution's type
+        hyb::ns_destroy(ctx);
+        rc = hyb::ns_create(ctx);
+        if (rc) return rc;
+    }
+    rc = hyb_phy_boundary(ctx);
+    if (!rc) rc = hyb_detfp(ctx);
+    if (!rc) rc = hyb_convert_ns(ctx);
+    if (!rc) HYB_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->rhs_valid = 0;
+    return rc;
 }
 
 int hyb_destroy(hyb_ctx *ctx) {
@@ -551,8 +647,30 @@ int collect_profile(hyb_ctx *ctx, size_t nev) {
 
 extern "C" {
 
+static int step_impl(hyb_ctx *ctx, int n_iter, hyb_residual *out);
+
 int hyb_step(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
     if (!ctx || n_iter < 1) return HYB_ERR_INVALID;
+    const int rc = step_impl(ctx, n_iter, out);
+    // a planted wait (hyb_test_stall) lasts one step
+    if (ctx->stall_site != HYB_STALL_NONE) {
+        cudaStreamSynchronize(ctx->stream);
+        ctx->stall_site = HYB_STALL_NONE;
+        ctx->spin_cycles = HYB_SPIN_CYCLES;
+    }
+    return rc;
+}
+
+int hyb_test_stall(hyb_ctx *ctx, int site, long long spin_cycles) {
+    if (!ctx || spin_cycles <= 0) return HYB_ERR_INVALID;
+    if (site != HYB_STALL_NONE && site != HYB_STALL_SWEEP_ROW && site != HYB_STALL_NS_BARRIER)
+        return HYB_ERR_INVALID;
+    ctx->stall_site = site;
+    ctx->spin_cycles = site == HYB_STALL_NONE ? HYB_SPIN_CYCLES : spin_cycles;
+    return HYB_OK;
+}
+
+static int step_impl(hyb_ctx *ctx, int n_iter, hyb_residual *out) {
     cudaSetDevice(ctx->dev);
     size_t evi = 0;
     ctx->prof_stage.clear();

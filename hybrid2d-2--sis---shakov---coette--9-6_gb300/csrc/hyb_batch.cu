@@ -517,6 +517,7 @@ int hyb_batch_create(int n, const hyb_mesh *meshes, const hyb_vgrid *vgrids, con
             hyb_batch_destroy(b);
             return rc;
         }
+        c->in_batch = 1;
         b->inst.push_back(c);
     }
     cudaSetDevice(b->dev);

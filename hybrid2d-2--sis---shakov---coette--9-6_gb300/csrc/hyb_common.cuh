@@ -65,6 +65,8 @@ struct KinArgs {
     // mass_pin: the updated f is multiplied by *mscale (m0 / M of the state
     // the step starts from); nullptr: no scale
     const double *mscale;
+    long long spin;        // limit of every bounded wait, SM clocks
+    int stall_row;         // hyb_test_stall: this row's copy is never issued (0: none)
 };
 
 }  // namespace hyb
@@ -121,6 +123,9 @@ struct hyb_ctx {
     hyb_gsis_params gsis;
     int gsis_last_inner;
     int gsis_skipped;                      // corrections skipped since hyb_gsis_configure
+    long long spin_cycles;                 // limit of the device's bounded waits
+    int in_batch;                          // owned by a hyb_batch (its graphs hold the buffers)
+    int stall_site;                        // hyb_test_stall: planted wait of the next step (0: none)
     hyb_mlp *mlp;                          // learned closure for the warm start (not owned)
     int gsis_outer;                        // outer iterations since hyb_gsis_configure
     int warm_done;                         // the scheduled warm start has run (2: fell back)

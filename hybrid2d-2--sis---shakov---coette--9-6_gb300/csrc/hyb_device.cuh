@@ -46,13 +46,14 @@ __device__ __forceinline__ void fence_async_shared() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// bounded wait: returns false when the spin limit ran out
-// (about two seconds of SM clock; the normal wait is well under a microsecond)
+// bounded wait: returns false when `limit` SM clocks ran out (the default,
+// HYB_SPIN_CYCLES, is about two seconds; the normal wait is well under a
+// microsecond; hyb_test_stall shortens it for one step)
 #define HYB_SPIN_CYCLES 4000000000LL
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, long long limit) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (clock64() - t0 < HYB_SPIN_CYCLES)
+    while (clock64() - t0 < limit)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

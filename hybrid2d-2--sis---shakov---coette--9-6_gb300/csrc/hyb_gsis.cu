@@ -54,6 +54,8 @@ struct NsCtrl {
     double lam;                    // volume mean of the band's density change
     unsigned bar_count;            // grid barrier of the cooperative inner loop: arrivals
     unsigned bar_gen;              // and completed barriers
+    long long spin;                // limit of the barrier's bounded wait, SM clocks
+    int stall;                     // hyb_test_stall: block 0 never arrives
 };
 
 struct NsDev {
@@ -1203,14 +1205,15 @@ __device__ bool ns_grid_sync(NsCtrl *C) {
         const unsigned g = *gen;
         __threadfence();
         int good = 1;
-        if (atomicAdd(&C->bar_count, 1u) == gridDim.x - 1) {
+        // (hyb_test_stall: block 0 skips its arrival, so no barrier completes)
+        if (!(C->stall && blockIdx.x == 0) && atomicAdd(&C->bar_count, 1u) == gridDim.x - 1) {
             atomicExch(&C->bar_count, 0u);
             __threadfence();
             atomicAdd(&C->bar_gen, 1u);
         } else {
             const long long t0 = clock64();
             while (*gen == g) {
-                if (*err == HYB_ERR_TIMEOUT || clock64() - t0 > HYB_SPIN_CYCLES) {
+                if (*err == HYB_ERR_TIMEOUT || clock64() - t0 > C->spin) {
                     atomicExch(&C->err, HYB_ERR_TIMEOUT);
                     good = 0;
                     break;
@@ -1819,6 +1822,8 @@ int gsis_solve(hyb_ctx *ctx) {
     c0.max_it = ctx->gsis.max_inner > 0 ? ctx->gsis.max_inner : 2000;
     c0.tol = ctx->gsis.inner_tol;
     c0.rtol = ctx->gsis.inner_rtol;
+    c0.spin = ctx->spin_cycles;
+    c0.stall = ctx->stall_site == HYB_STALL_NS_BARRIER;
     *st->h_ctrl = c0;
     HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
     if (D.wall_band) {
@@ -1917,6 +1922,7 @@ int gsis_warm_start(hyb_ctx *ctx) {
     c0.max_it = ctx->gsis.mlp_warm_inner > 0 ? ctx->gsis.mlp_warm_inner : 2000;
     c0.tol = 0.0;
     c0.rtol = ctx->gsis.mlp_warm_rtol > 0 ? ctx->gsis.mlp_warm_rtol : 1e-3;
+    c0.spin = ctx->spin_cycles;
     *st->h_ctrl = c0;
     HYB_CK(cudaMemcpyAsync(st->ctrl, st->h_ctrl, sizeof(NsCtrl), cudaMemcpyHostToDevice, s));
     if (W.wall_band) {

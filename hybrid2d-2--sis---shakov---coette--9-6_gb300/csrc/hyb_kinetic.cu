@@ -195,6 +195,7 @@ struct MomArgs {
     const double *vx, *vy, *w;
     int nvi, nv, Na, Nb, PA, nx, ny, scan_is_j, vs, nloc_max, *err;
     double cfc, cpr, x1s, r00, t00;
+    long long spin;     // limit of the bounded waits, SM clocks
 };
 
 constexpr int MOM_NST = 3;
@@ -372,12 +373,12 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
         const int k = n % MOM_NST;
         // refill the slot freed by slot n-1 with slot n+NST-1
         if (t == 0 && ok && n + MOM_NST - 1 < nslot) {
-            if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1)))
+            if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1), M.spin))
                 ok = false;
             else
                 issue(issued++);
         }
-        if (ok && !mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1))) ok = false;
+        if (ok && !mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1), M.spin)) ok = false;
         if (act && ok) {
             const int cnt = min(VPS, nloc - n * VPS);
             const real *gs = stage + (size_t)k * VPS * 2 * PA + (a0 - 1);
@@ -446,7 +447,7 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
             atomicExch(M.err, HYB_ERR_TIMEOUT);
             // the last NST issued slots may still be in flight: wait (bounded)
             for (int n = issued > MOM_NST ? issued - MOM_NST : 0; n < issued; n++)
-                mbar_wait_bounded(&full[n % MOM_NST], (uint32_t)((n / MOM_NST) & 1));
+                mbar_wait_bounded(&full[n % MOM_NST], (uint32_t)((n / MOM_NST) & 1), M.spin);
         }
         return;
     }
@@ -868,6 +869,7 @@ static MomArgs mom_args(hyb_ctx *ctx, const void *f, size_t *smem, int *mc) {
     M.vs = moments_slices(ctx);
     M.nloc_max = (ctx->nvj + M.vs - 1) / M.vs * ctx->nvi;
     M.err = ctx->d_err;
+    M.spin = ctx->spin_cycles;
     M.cfc = ctx->prm.cfc;
     M.cpr = ctx->prm.cpr;
     M.x1s = ctx->prm.x1s;

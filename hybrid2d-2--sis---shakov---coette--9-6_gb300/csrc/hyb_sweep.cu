@@ -74,6 +74,8 @@ static void fill_args(hyb_ctx *ctx, int store_rhs, KinArgs<real> &A) {
     A.dt = (real)ctx->prm.dt;
     A.err = ctx->d_err;
     A.mscale = (ctx->prm.mass_pin && store_rhs != 2) ? ctx->d_mass + 1 : nullptr;
+    A.spin = ctx->spin_cycles;
+    A.stall_row = (ctx->stall_site == HYB_STALL_SWEEP_ROW && store_rhs != 2) ? (ctx->Nb < 3 ? ctx->Nb : 3) : 0;
 }
 
 static int sweep_dispatch(hyb_ctx *ctx, int store_rhs, bool launch) {

@@ -134,9 +134,9 @@ __device__ __forceinline__ real flux_whi(real s, real f1, real f2, real f3) {
 // within 1..Nb, so each is a real copy) were issued and never waited for;
 // wait (bounded) for each before the CTA leaves.  Out of line, so that the
 // row loop's register allocation does not carry this path.
-static __device__ __noinline__ void sweep_drain(uint64_t *bars, int stop, int Nb) {
+static __device__ __noinline__ void sweep_drain(uint64_t *bars, int stop, int Nb, int stall_row, long long spin) {
     for (int bp = stop + 3; bp <= Nb && bp <= stop + RING - 4; bp++)
-        mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1));
+        if (bp != stall_row) mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1), spin);
 }
 
 // the sweep of the CTA's velocity block vblk (velocities vblk * vpb + g)
@@ -224,6 +224,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     auto issue_row = [&](int bp) {
         int s = (bp + 1) % RING;
         int pr = phys_row(bp);
+        if (bp == A.stall_row) return;            // hyb_test_stall: a wait nothing completes
         if (pr > 0 && bp <= Nb) {
             mbar_arrive_expect_tx(&bars[s], 2 * row_bytes);
             const real *src = A.f + vrow0 + (size_t)(pr - 1) * PA;
@@ -260,11 +261,11 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     auto wait_row = [&](int bp) {
         if (!vok) return;
         if (bp > Nb) {
-            if (perB && !mbar_wait_bounded(&bars[RING + (bp - Nb - 1)], 0)) timeout = true;
+            if (perB && !mbar_wait_bounded(&bars[RING + (bp - Nb - 1)], 0, A.spin)) timeout = true;
             return;
         }
         if (phys_row(bp) == 0) return;
-        if (!mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1))) timeout = true;
+        if (!mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1), A.spin)) timeout = true;
     };
     // scan-axis halo cells of the thread (wrapped on a periodic axis; on a
     // wall axis they are only read by the standard faces, which never reach
@@ -512,7 +513,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
         }
         if (__syncthreads_or(timeout)) {
             if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
-            if (producer) sweep_drain(bars, b, Nb);
+            if (producer) sweep_drain(bars, b, Nb, A.stall_row, A.spin);
             return;
         }
         // every thread is past this row's reads, so the slot of row b-3 is free

@@ -25,6 +25,10 @@ HYB_SCHEME_WENO3 = 3
 HYB_PREC_FP64 = 0
 HYB_PREC_MIXED = 1
 
+HYB_STALL_NONE = 0
+HYB_STALL_SWEEP_ROW = 1
+HYB_STALL_NS_BARRIER = 2
+
 HYB_SWEEP_REFERENCE = 0
 HYB_SWEEP_UPWIND = 1
 

@@ -14,6 +14,7 @@ module hyb_dvm
   integer(c_int), parameter :: HYB_SCHEME_UP1 = 0, HYB_SCHEME_NND = 1, HYB_SCHEME_WENO3 = 3
   integer(c_int), parameter :: HYB_PREC_FP64 = 0, HYB_PREC_MIXED = 1
   integer(c_int), parameter :: HYB_SWEEP_REFERENCE = 0, HYB_SWEEP_UPWIND = 1
+  integer(c_int), parameter :: HYB_STALL_NONE = 0, HYB_STALL_SWEEP_ROW = 1, HYB_STALL_NS_BARRIER = 2
   integer(c_int), parameter :: HYB_NSUM = 11, HYB_NRD = 2
   integer(c_int), parameter :: HYB_NOALLOC_MAX_CELLS = 209715
 
@@ -141,6 +142,17 @@ module hyb_dvm
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
        integer(c_int), intent(out) :: count
+     end function
+     integer(c_int) function hyb_set_precision(ctx, precision) bind(c, name="hyb_set_precision")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: precision
+     end function
+     integer(c_int) function hyb_test_stall(ctx, site, spin_cycles) bind(c, name="hyb_test_stall")
+       import :: c_int, c_ptr, c_long_long
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: site
+       integer(c_long_long), value :: spin_cycles
      end function
      integer(c_int) function hyb_set_walls(ctx, face, wall_u, wall_v, wall_t) bind(c, name="hyb_set_walls")
        import :: c_int, c_ptr, c_double

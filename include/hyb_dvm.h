@@ -200,6 +200,15 @@ typedef struct hyb_ctx hyb_ctx;
 int hyb_create(const hyb_mesh *mesh, const hyb_vgrid *vgrid,
                const hyb_params *params, hyb_ctx **out);
 int hyb_destroy(hyb_ctx *ctx);
+/* Switches a context from HYB_PREC_MIXED to HYB_PREC_FP64 on the device
+ * (no counterpart in the reference): the FP32 distribution is widened in a
+ * new FP64 array, the other buffers of its type are made again at FP64 size,
+ * and the moments are recomputed; iterations after the call run the FP64
+ * path from that state.  A mixed run can thus finish its convergence in FP64
+ * without a host round trip of f.  Only MIXED -> FP64 (HYB_ERR_UNSUPPORTED
+ * otherwise, and for instances of a hyb_batch); the same precision is a
+ * no-op.  Allocates device memory. */
+int hyb_set_precision(hyb_ctx *ctx, int precision);
 /* Human-readable text of the last error on this context (never NULL). */
 const char *hyb_last_error(const hyb_ctx *ctx);
 /* Library version / build string. */
@@ -295,6 +304,26 @@ int hyb_detfp_noalloc(int nx, int ny, int nvi, int nvj, const double *frd_dev,
                       const double *wi_dev, const double *wj_dev,
                       const hyb_params *p, double *s_gkua_dev, double *cf_dev,
                       void *stream);
+
+/* ---- failure injection for tests (no counterpart in the reference) ------ */
+/* Arms one planted wait that nothing completes for the next hyb_step, with
+ * every bounded device wait of that step limited to spin_cycles SM clocks
+ * (> 0; the default limit is about two seconds).  site:
+ *   HYB_STALL_SWEEP_ROW   the kinetic sweep never issues the bulk copy of
+ *                         one row, so every CTA's wait on that row's
+ *                         mbarrier runs out; the CTAs drain the copies they
+ *                         issued and return before writing f;
+ *   HYB_STALL_NS_BARRIER  block 0 of the synthetic solve's cooperative
+ *                         inner loop (LU-SGS on meshes of up to 65,536
+ *                         cells, band 3..n-3) never arrives at the grid
+ *                         barrier, so every block's wait runs out.
+ * The step returns HYB_ERR_TIMEOUT; the planted wait and the short limit
+ * are then cleared, and the context stays usable (after a sweep stall f is
+ * as it was before the step).  HYB_STALL_NONE disarms. */
+#define HYB_STALL_NONE        0
+#define HYB_STALL_SWEEP_ROW   1
+#define HYB_STALL_NS_BARRIER  2
+int hyb_test_stall(hyb_ctx *ctx, int site, long long spin_cycles);
 
 /* ---- timing / introspection -------------------------------------------- */
 /* Per-stage device timing with CUDA events on the context's stream.  While

@@ -1,8 +1,10 @@
 """Generates tests/golden/*.json from the reference's own shipped files.
 
-Run in the container that holds the reference checkout (path given as the
-first argument, default /root/reference).  Nothing at test time reads the
-reference; the tests read only the JSON written here.
+Run where a checkout of the reference is available, with its path as the
+only argument (or in the HYB_REFERENCE environment variable):
+    python tests/golden/make_golden.py <reference checkout>
+Nothing at test time reads the reference; the tests read only the JSON
+written here.
 
 flow2d_gkua_step0.json
     Hybrid2D/output/flow2d-GKUA.dat is the moment field the reference wrote
@@ -24,7 +26,9 @@ import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYB_REFERENCE")
+if not ref:
+    sys.exit("usage: make_golden.py <reference checkout>  (or set HYB_REFERENCE)")
 here = os.path.dirname(os.path.abspath(__file__))
 src = os.path.join(ref, "Hybrid2D", "output", "flow2d-GKUA.dat")
 rows = []
