@@ -136,7 +136,7 @@ __device__ __forceinline__ real flux_whi(real s, real f1, real f2, real f3) {
 // row loop's register allocation does not carry this path.
 static __device__ __noinline__ void sweep_drain(uint64_t *bars, int stop, int Nb, int stall_row, long long spin) {
     for (int bp = stop + 3; bp <= Nb && bp <= stop + RING - 4; bp++)
-        if (bp != stall_row) mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1), spin);
+        if (stall_row <= 0 || bp != stall_row) mbar_wait_bounded(&bars[(bp + 1) % RING], (uint32_t)(((bp + 1) / RING) & 1), spin);
 }
 
 // the sweep of the CTA's velocity block vblk (velocities vblk * vpb + g)
@@ -224,7 +224,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     auto issue_row = [&](int bp) {
         int s = (bp + 1) % RING;
         int pr = phys_row(bp);
-        if (bp == A.stall_row) return;            // hyb_test_stall: a wait nothing completes
+        if (A.stall_row > 0 && bp == A.stall_row) return;   // hyb_test_stall: a wait nothing completes
         if (pr > 0 && bp <= Nb) {
             mbar_arrive_expect_tx(&bars[s], 2 * row_bytes);
             const real *src = A.f + vrow0 + (size_t)(pr - 1) * PA;
