@@ -10,6 +10,10 @@ is cell-velocity updates per second (cells x velocity nodes x iterations /
 time).  Inputs (f, 2.1 GB) are larger than L2, so no flush is needed between
 steps.  N > 1 runs independent replicas, one per GPU (the path is not
 sharded across GPUs); value is the sum over ranks.
+
+--impl reference times the FP64 oracle (the CPU restatement of the
+reference's kinetic path; no Fortran compiler exists on either machine) on
+the same workload, full velocity grid included, on all host cores.
 """
 import argparse
 import json
@@ -30,6 +34,10 @@ GE.load_package()
 from hyb_gb300 import abi, cases  # noqa: E402
 
 METRIC = "cell-velocity updates/s (plain kinetic iteration)"
+# what the mixed path computes in which type
+PREC_MIXED = ("fp32 f, fluxes, equilibrium and sweeps; moments: fp32 products summed in fp32 over blocks of 8 "
+              "velocities, the blocks Kahan-compensated in fp32, velocity slices folded in float-float, the "
+              "primitive conversion and residual in fp64")
 UNIT = "cell*velocity updates/s"
 
 
@@ -107,28 +115,39 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(case, seconds=10.0, max_seconds=30.0, threads=0):
-    """Oracle (CPU restatement of the reference path) on the same mesh with a
-    16x16 velocity subset; returns cell-velocity updates/s and the sample."""
+def cpu_oracle(case, threads):
+    """The FP64 oracle (CPU restatement of the reference path) on the same
+    mesh and the same full velocity grid as the GPU run."""
     from oracle import oracle as O
     import copy
     c = copy.deepcopy(case)
-    c.nvx = c.nvy = 16
     c.precision = 0
-    nthreads = threads or (os.cpu_count() or 1)
-    o = O.Oracle(c, threads=nthreads)
+    o = O.Oracle(c, threads=threads)
     o.init_maxwellian()
-    o.step(1)
+    return c, o
+
+
+def cpu_sample(case, seconds=10.0, threads=0, oracle=None):
+    """Cell-velocity updates/s of the oracle on the full workload, over whole
+    iterations until `seconds` have passed (at least one)."""
+    nthreads = threads or (os.cpu_count() or 1)
+    if oracle is None:
+        c, o = cpu_oracle(case, nthreads)
+    else:
+        c, o = oracle
+        from oracle import oracle as O
+        O.lib().orc_set_threads(nthreads)
     n = 0
     t0 = time.perf_counter()
     while True:
         o.step(1)
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or el >= max_seconds:
+        if el >= seconds:
             break
     val = c.cells * c.nv * n / el
-    return val, nthreads, f"{c.ncx}x{c.ncy} cells x 16x16 velocities, {n} FP64 oracle iterations, {el:.1f}s"
+    return val, nthreads, (f"{c.ncx}x{c.ncy} cells x {c.nvx}x{c.nvy} velocities (the full workload), "
+                           f"{n} FP64 oracle iterations, {el:.1f}s")
 
 
 def cpu_model():
@@ -185,18 +204,13 @@ def dist_max(world, x):
 
 def run_reference(args, world, rank):
     """The reference arm: the CPU restatement of the reference's kinetic path
-    (the Fortran reference has no compiler here) on the machine's host cores."""
+    (the Fortran reference has no compiler here) on the machine's host cores, on
+    the same mesh and velocity grid as the GPU arm."""
     if rank != 0:
         return 0
     case = make_case(args.config)
-    from oracle import oracle as O
-    import copy
-    c = copy.deepcopy(case)
-    c.nvx = c.nvy = 16
-    c.precision = 0
     nthreads = os.cpu_count() or 1
-    o = O.Oracle(c, threads=nthreads)
-    o.init_maxwellian()
+    c, o = cpu_oracle(case, nthreads)
     for _ in range(args.warmup):
         o.step(1)
     t0 = time.perf_counter()
@@ -210,9 +224,9 @@ def run_reference(args, world, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": case.name, "cells": case.cells, "velocities": case.nv,
-                   "sample": f"same mesh, 16x16 velocity subset per step"},
+                   "sample": "the full workload: same mesh, same velocity grid, one outer iteration per step"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{c.ncx}x{c.ncy} cells x 16x16 velocities per step, FP64 oracle, "
+                         "sample": f"{c.ncx}x{c.ncy} cells x {c.nvx}x{c.nvy} velocities per step, FP64 oracle, "
                                    f"{nthreads} OpenMP threads"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -220,68 +234,104 @@ def run_reference(args, world, rank):
     return 0
 
 
-def time_to_residual(tol=1e-8, max_iters=8000, chunk=50):
-    """Wall time and outer iterations to max RMS residual <= tol on the Kn 0.1
-    channel (4x64 cells, 32x32 NC, NND, dt 0.01), for the plain kinetic
-    iteration and the synthetic-solve variants; device-synchronised wall
-    clock around the hyb_step calls (residual read every `chunk` steps)."""
-    from hyb_gb300 import closure
+def _ttr_run(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
+             wall_s=None):
+    """One run to max RMS residual <= tol (DETFP_res): device-synchronised
+    wall clock around the hyb_step calls, the residual read every `chunk`
+    outer iterations.  promote: a mixed run continues in FP64 on the device
+    (hyb_set_precision) once its FP32 residual stops falling.  An FP32 run
+    without promotion that has not improved for 1000 iterations below 1e-4
+    sits on its rounding floor and is stopped.  wall_s caps the wall time."""
+    from hyb_gb300 import closure, hyb_types as T
+    s = abi.Solver(case, precision=prec)
+    s.init_maxwellian()
+    if gsis is not None:
+        if learned:
+            s.attach_mlp(closure.load())
+        s.gsis(**gsis)
+    it, r, prev, promoted, best, best_it, stalled = 0, None, None, None, None, 0, False
+    t0 = time.perf_counter()
+    while it < max_iters:
+        r = s.step(chunk)
+        it += chunk
+        res = r["max_rms"]
+        if res <= tol or not np.isfinite(res):
+            break
+        if wall_s is not None and time.perf_counter() - t0 > wall_s:
+            break
+        if best is None or res < 0.9 * best:
+            best, best_it = res, it
+        elif prec == T.HYB_PREC_MIXED and not promote and res < 1e-4 and it - best_it >= 1000:
+            stalled = True
+            break
+        if promote and promoted is None and prev is not None and res < 1e-3 and res > 0.9 * prev:
+            s.set_precision(T.HYB_PREC_FP64)
+            promoted = it
+        prev = res
+    el = time.perf_counter() - t0
+    S = s.moments()[0].reshape(case.ny + 7, case.nx + 7, 11)[4:4 + case.ny - 1, 4:4 + case.nx - 1, :4]
+    out = {"seconds": round(el, 3), "iterations": it, "ms_per_iteration": round(1000.0 * el / it, 3),
+           "residual": r["max_rms"], "reached": bool(r["max_rms"] <= tol),
+           "precision": "mixed" if prec == T.HYB_PREC_MIXED else "fp64"}
+    if promote:
+        out["fp64_from_iteration"] = promoted
+    if stalled:
+        out["stalled_on_fp32_floor"] = True
+    if gsis is not None:
+        out["skipped_corrections"] = s.gsis_skipped()
+    s.close()
+    return out, S
+
+
+def time_to_residual(tol=1e-8, large=True):
+    """Time to residual 1e-8.  The Kn 0.1 channel (4x64 cells, 32^2 NC,
+    plates +-0.2): the reference's own iteration (forward sweep in index
+    order with the Jacobi-like backward step, dt 0.01), the upwind-ordered
+    iteration at dt 1e6 with the mass pin, and the synthetic-solve variants,
+    each FP64 and mixed (finished in FP64 on the device).  The large case
+    (128x512 cells, 64^2 on [-6,6], Kn 0.01): the synthetic solve in FP64 and
+    mixed for a bounded number of outer iterations (1e-8 is out of reach in
+    minutes there), which gives the cost of an outer iteration of each and
+    the residual each reaches.  Field differences are stated against the
+    FP64 run of the same iteration."""
+    from hyb_gb300 import hyb_types as T
+    M, D = T.HYB_PREC_MIXED, T.HYB_PREC_FP64
+    ref = lambda: cases.couette_small(dt=0.01)
+    upw = lambda: cases.couette_small(dt=1.0e6, sweep_order=1, mass_pin=1)
     gs = dict(max_inner=40, inner_tol=0.0, inner_rtol=1e-2, cfl=20.0, ns_solver=0, correct_f=1)
-    # "switch" variants run FP32 f until the residual reaches `switch_at`
-    # (or stops falling) and continue the same state in an FP64 context
-    # the learned warm start after 20 outer iterations, 400 inner iterations
-    # of the closed NS equations (2000 cost more than they saved)
     gl = dict(gs, mlp_warm_after=20, mlp_warm_inner=400)
-    variants = [("plain_fp64", 0, None, False), ("gsis_fp64", 0, gs, False), ("gsis_mixed", 1, gs, False),
-                ("gsis_mixed_learned", 1, gl, False),
-                ("gsis_mixed_then_fp64", 1, gs, True), ("gsis_mixed_learned_then_fp64", 1, gl, True)]
-    net = closure.load()
-    out = {}
-    switch_at = 3e-6
-    for name, prec, g, switch in variants:
-        c = cases.couette_small(dt=0.01)
-        s = abi.Solver(c, precision=prec)
-        s.init_maxwellian()
-        if g is not None:
-            s.attach_mlp(net)
-            s.gsis(**g)
-        it, r, prev, switched_at = 0, None, None, None
-        best, best_it, stalled = None, 0, False
-        t0 = time.perf_counter()
-        while it < max_iters:
-            r = s.step(chunk)
-            it += chunk
-            if r["max_rms"] <= tol:
-                break
-            # an FP32 run that has stopped falling below 1e-4 for 1000
-            # iterations sits on its rounding floor: stop and report it
-            if best is None or r["max_rms"] < 0.9 * best:
-                best, best_it = r["max_rms"], it
-            elif prec == 1 and not switch and r["max_rms"] < 1e-4 and it - best_it >= 1000:
-                stalled = True
-                break
-            if switch and switched_at is None and (r["max_rms"] <= switch_at or (
-                    r["max_rms"] < 1e-4 and prev is not None and r["max_rms"] > 0.9 * prev)):
-                f = s.download_f()
-                s.close()
-                s = abi.Solver(c, precision=0)
-                s.upload_f(f)
-                s.gsis(**{k: v for k, v in g.items() if k != "mlp_warm_after"})
-                switched_at = it
-            prev = r["max_rms"]
-        el = time.perf_counter() - t0
-        u = s.moments()[0].reshape(c.ny + 7, c.nx + 7, 11)[4:4 + c.ny - 1, 4:4 + c.nx - 1, 1]
-        out[name] = {"seconds": round(el, 3), "iterations": it, "residual": r["max_rms"],
-                     "reached": bool(r["max_rms"] <= tol), "u_mid_wall": float(u[-1].mean())}
-        if switch:
-            out[name]["fp64_from_iteration"] = switched_at
-        if stalled:
-            out[name]["stalled_on_fp32_floor"] = True
-        s.close()
-    ref = out["plain_fp64"]["u_mid_wall"]
-    for v in out.values():
-        v["u_wall_rel_diff_vs_plain"] = abs(v["u_mid_wall"] - ref) / abs(ref)
-    return {"workload": "couette-4x64-nv32-kn0.1, NND, dt 0.01", "tol": tol, "chunk": chunk, "runs": out}
+    small = [("plain_fp64_reference_iteration", ref, D, None, False, False),
+             ("plain_mixed_reference_iteration_to_fp64", ref, M, None, True, False),
+             ("plain_fp64_upwind", upw, D, None, False, False),
+             ("plain_mixed_upwind_to_fp64", upw, M, None, True, False),
+             ("gsis_fp64", ref, D, gs, False, False),
+             ("gsis_mixed_to_fp64", ref, M, gs, True, False),
+             ("gsis_mixed_learned_to_fp64", ref, M, gl, True, True)]
+    out, fields = {}, {}
+    for name, mk, prec, g, promote, learned in small:
+        out[name], fields[name] = _ttr_run(name, mk(), prec, g, promote, learned, tol=tol)
+    # field error of each run against the FP64 run of the same iteration
+    base = {"reference": fields["plain_fp64_reference_iteration"], "upwind": fields["plain_fp64_upwind"],
+            "gsis": fields["gsis_fp64"]}
+    for name, S in fields.items():
+        b = base["upwind" if "upwind" in name else ("gsis" if name.startswith("gsis") else "reference")]
+        out[name]["field_rel_err_vs_fp64"] = {
+            k: float(np.abs(S[..., q] - b[..., q]).max() / max(np.abs(b[..., q]).max(), 1e-3))
+            for q, k in enumerate(("rho", "u", "v", "T"))}
+    res = {"workload": "couette-4x64-nv32-kn0.1, NND", "tol": tol, "runs": out}
+    if large:
+        gl2 = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0,
+                   inner_rtol=1e-8, relax_pct=70)
+        lg = {}
+        for name, prec, cap in (("gsis_fp64", D, 150), ("gsis_mixed", M, 150)):
+            c = cases.couette_large(dt=1.0e6, sweep_order=1, mass_pin=1, precision=prec)
+            lg[name], _ = _ttr_run(name, c, prec, gl2, False, False, tol=tol, max_iters=cap, chunk=10)
+        lg["outer_iteration_cost_ratio_fp64_over_mixed"] = (lg["gsis_fp64"]["ms_per_iteration"] /
+                                                            lg["gsis_mixed"]["ms_per_iteration"])
+        res["large"] = {"workload": "couette-128x512-nv64-kn0.01, upwind order dt 1e6, mass pin; GSIS band to "
+                                    "the walls, line solver (16 inner, CFL 600), correction relaxed to 0.7",
+                        "cap_iterations": 150, "runs": lg}
+    return res
 
 
 def run_gb300(args, world, rank, local):
@@ -339,6 +389,28 @@ def run_gb300(args, world, rank, local):
     e2e_s = dist_max(world, time.perf_counter() - t0)
     e2e = world * units / e2e_s
     s.close()
+    # ---- the same workload through the FP64 path ------------------------------
+    fp64 = None
+    if case.precision == 1 and not args.no_fp64:
+        import copy
+        c64 = copy.deepcopy(case)
+        c64.precision = 0
+        s64 = abi.Solver(c64, device=local)
+        s64.init_maxwellian()
+        for _ in range(args.warmup):
+            s64.step(1, residual=False)
+        s64.profile(True)
+        dist_barrier(world)
+        n64 = max(3, args.steps // 4)
+        s64.step(n64, residual=False)
+        ms64 = dist_max(world, s64.last_ms())
+        p64 = s64.profile_read()
+        s64.close()
+        fp64 = {"value": world * case.cells * case.nv * n64 / (ms64 / 1000.0), "unit": UNIT, "steps": n64,
+                "ms_per_step": ms64 / n64, "dtype": "f64",
+                "stage_ms_per_step": {k: round(v_[0] / n64, 4) for k, v_ in p64.items() if v_[1]},
+                "note": "GB300 issues FP64 at 2 lanes per clock per SM: the FP64 sweep is bound by FP64 "
+                        "arithmetic, not by HBM"}
     if rank != 0:
         return 0
     stage_ms = {k: round(v_[0] / args.steps, 4) for k, v_ in prof.items() if v_[1]}
@@ -349,7 +421,7 @@ def run_gb300(args, world, rank, local):
         "dtype": "f32" if case.precision == 1 else "f64",
         "data": "synthetic (seeded analytic Couette set-up; no dataset)",
         "config": {"workload": case.name, "cells": case.cells, "velocities": case.nv,
-                   "precision": "fp32 f/fluxes/sweeps, fp64 moments" if case.precision == 1 else "fp64",
+                   "precision": PREC_MIXED if case.precision == 1 else "fp64",
                    "scheme": "NND", "dt": case.dt, "parallelism": f"replicas x{world}",
                    "sweep_shape": {"cells_per_thread": shape[0], "velocities_per_cta": shape[1]},
                    "l2": "inputs larger than L2 (f is %.2f GB)" % (case.cells * case.nv * 2 * rs / 1e9)},
@@ -359,19 +431,26 @@ def run_gb300(args, world, rank, local):
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "alg_bytes_per_cell_velocity": b_alg,
                      "ms_per_launch": per_launch_s * 1000.0},
-        "whole_step_basis": {"bytes_per_unit": 40, "note": "whole kinetic step on the 5*NRD*s definition",
-                         "achieved_gbs": 40.0 * units / (ms / 1000.0) / 1e9 / world,
-                         "frac": 40.0 * units / (ms / 1000.0) / 1e9 / world / peak},
+        "whole_step": {"bytes_per_unit": 6 * rs,
+                       "note": "bytes the step moves per cell-velocity: the fused sweep reads and writes G, H "
+                               "(4 s), the moment pass reads them (2 s)",
+                       "achieved_gbs": 6 * rs * units / (ms / 1000.0) / 1e9 / world,
+                       "frac": 6 * rs * units / (ms / 1000.0) / 1e9 / world / peak},
         "stage_ms_per_step": stage_ms,
         "gpu_launches": launches,
         "clocks": clk,
         "last_residual": res["max_rms"],
     }
+    if fp64 is not None:
+        line["fp64"] = fp64
     if not args.no_ttr and rank == 0:
-        line["time_to_residual"] = time_to_residual()
+        line["time_to_residual"] = time_to_residual(large=not args.no_ttr_large)
     if not args.no_cpu:
-        cv, cores, sample = cpu_sample(case, seconds=args.cpu_seconds)
-        cv1, _, sample1 = cpu_sample(case, seconds=args.cpu_seconds / 2, threads=1)
+        orc = cpu_oracle(case, os.cpu_count() or 1)
+        orc[1].step(1)
+        cv, cores, sample = cpu_sample(case, seconds=args.cpu_seconds, oracle=orc)
+        cv1, _, sample1 = cpu_sample(case, seconds=1.0, threads=1, oracle=orc)
+        del orc
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                                 "value_1_thread": cv1, "sample_1_thread": sample1,
                                 "nproc": os.cpu_count(), "cpu_model": cpu_model()}
@@ -379,7 +458,7 @@ def run_gb300(args, world, rank, local):
         # the plain iteration count measured on the GPU (FP64 parity makes
         # the two runs take the same iterations)
         it_s = cpu_channel_iteration_s()
-        ttr = line.get("time_to_residual", {}).get("runs", {}).get("plain_fp64")
+        ttr = line.get("time_to_residual", {}).get("runs", {}).get("plain_fp64_reference_iteration")
         line["cpu_baseline"]["channel_plain_fp64_s_per_iteration"] = it_s
         if ttr and ttr.get("reached"):
             line["cpu_baseline"]["channel_plain_fp64_to_1e-8_s_extrapolated"] = it_s * ttr["iterations"]
@@ -473,6 +552,8 @@ def main():
     ap.add_argument("--config", default="large", choices=["large", "small", "sine", "prof", "batch"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ttr", action="store_true", help="skip the time-to-residual runs")
+    ap.add_argument("--no-ttr-large", action="store_true", help="time to residual on the small channel only")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 throughput of the same workload")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:

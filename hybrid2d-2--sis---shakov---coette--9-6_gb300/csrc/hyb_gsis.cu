@@ -95,6 +95,7 @@ struct NsState {
     cudaGraphExec_t graph;
     bool have_graph;
     float *mlp_buf;         // closure features and outputs
+    void *fpar;             // Shakhov parameters of the distribution correction [14][Nb*PA] (real)
     int coop_blocks;        // blocks of the cooperative inner loop (0: not available)
 };
 
@@ -734,17 +735,17 @@ __global__ void k_ns_wallghost(NsDev D) {
 // by one thread each (sequential elimination, scratch in D.lin).  The
 // elimination is FP32: it preconditions the inner iteration, whose residual
 // and update stay FP64, so it sets the rate but not the solution.
-__device__ __forceinline__ void flux_jac(const double *U, double n1, double n2, double g, float *A) {
-    const double r = U[0], u = U[1] / r, v = U[2] / r, E = U[3];
-    const double a1 = g - 1.0, q2 = u * u + v * v, phi = 0.5 * a1 * q2;
-    const double p = a1 * (E - 0.5 * r * q2), H = (E + p) / r, un = u * n1 + v * n2;
-    A[0] = 0.f; A[1] = (float)n1; A[2] = (float)n2; A[3] = 0.f;
-    A[4] = (float)(phi * n1 - u * un); A[5] = (float)(un + u * n1 - a1 * u * n1);
-    A[6] = (float)(u * n2 - a1 * v * n1); A[7] = (float)(a1 * n1);
-    A[8] = (float)(phi * n2 - v * un); A[9] = (float)(v * n1 - a1 * u * n2);
-    A[10] = (float)(un + v * n2 - a1 * v * n2); A[11] = (float)(a1 * n2);
-    A[12] = (float)((phi - H) * un); A[13] = (float)(H * n1 - a1 * u * un);
-    A[14] = (float)(H * n2 - a1 * v * un); A[15] = (float)(g * un);
+
+// the same Jacobian from a state already rounded to FP32, in FP32 (the line
+// solver's blocks)
+__device__ __forceinline__ void flux_jacf(const float *U, float n1, float n2, float g, float *A) {
+    const float r = U[0], ir = 1.f / r, u = U[1] * ir, v = U[2] * ir, E = U[3];
+    const float a1 = g - 1.f, q2 = u * u + v * v, phi = 0.5f * a1 * q2;
+    const float p = a1 * (E - 0.5f * r * q2), H = (E + p) * ir, un = u * n1 + v * n2;
+    A[0] = 0.f; A[1] = n1; A[2] = n2; A[3] = 0.f;
+    A[4] = phi * n1 - u * un; A[5] = un + u * n1 - a1 * u * n1; A[6] = u * n2 - a1 * v * n1; A[7] = a1 * n1;
+    A[8] = phi * n2 - v * un; A[9] = v * n1 - a1 * u * n2; A[10] = un + v * n2 - a1 * v * n2; A[11] = a1 * n2;
+    A[12] = (phi - H) * un; A[13] = H * n1 - a1 * u * un; A[14] = H * n2 - a1 * v * un; A[15] = g * un;
 }
 
 // X = M^-1 B, M 4x4, B 4 x K (row-major), partial pivoting; M destroyed
@@ -753,14 +754,19 @@ __device__ __forceinline__ void solve4f(float *M, float *B) {
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         int pr = c;
+        float best = fabsf(M[c * 4 + c]);
 #pragma unroll
-        for (int r = c + 1; r < 4; r++)
-            if (fabsf(M[r * 4 + c]) > fabsf(M[pr * 4 + c])) pr = r;
-        if (pr != c) {
+        for (int r = c + 1; r < 4; r++) {
+            const float v = fabsf(M[r * 4 + c]);
+            if (v > best) { best = v; pr = r; }
+        }
 #pragma unroll
-            for (int q = 0; q < 4; q++) { float t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t; }
+        for (int r = c + 1; r < 4; r++) {   // compile-time indices keep M, B in registers
+            if (r != pr) continue;
 #pragma unroll
-            for (int q = 0; q < K; q++) { float t = B[c * K + q]; B[c * K + q] = B[pr * K + q]; B[pr * K + q] = t; }
+            for (int q = 0; q < 4; q++) { float t = M[c * 4 + q]; M[c * 4 + q] = M[r * 4 + q]; M[r * 4 + q] = t; }
+#pragma unroll
+            for (int q = 0; q < K; q++) { float t = B[c * K + q]; B[c * K + q] = B[r * K + q]; B[r * K + q] = t; }
         }
         const float ip = 1.f / M[c * 4 + c];
 #pragma unroll
@@ -826,7 +832,7 @@ __device__ void line_row(const NsDev &D, const LineGeo &G, int ln, int k, float 
     const bool aj = G.along_j;
     const int i = aj ? ln : k, j = aj ? k : ln;
     const size_t c = c2(D, i, j), nc = D.nc;
-    const double g = D.gamma;
+    const float g = (float)D.gamma;
     const float alfa = (float)(D.vol[mi(D, i, j)] / D.dt[c] + D.Lci[c] + D.Lcj[c] + 2.0 * (D.Lvi[c] + D.Lvj[c]));
 #pragma unroll
     for (int q = 0; q < 16; q++) { A[q] = 0.f; B[q] = 0.f; C[q] = 0.f; }
@@ -834,17 +840,17 @@ __device__ void line_row(const NsDev &D, const LineGeo &G, int ln, int k, float 
     for (int q = 0; q < 4; q++) B[q * 4 + q] = alfa;
     const bool walls = aj ? !D.pery : !D.perx;
     const bool wlo = D.wall_band && walls && k == G.k0, whi = D.wall_band && walls && k == G.k1;
-    const double n1f = aj ? D.nj1[mi(D, i, j)] : D.ni1[mi(D, i, j)];
-    const double n2f = aj ? D.nj2[mi(D, i, j)] : D.ni2[mi(D, i, j)];
+    const float n1f = (float)(aj ? D.nj1[mi(D, i, j)] : D.ni1[mi(D, i, j)]);
+    const float n2f = (float)(aj ? D.nj2[mi(D, i, j)] : D.ni2[mi(D, i, j)]);
     if (k > G.k0 || wlo) {   // lower neighbour: L = 0.5 (A s + Lc) + Lv
         const size_t cn = aj ? c2(D, i, j - 1) : c2(D, i - 1, j), cr = wlo ? c : cn;
-        double Un[4];
+        float Un[4];
 #pragma unroll
-        for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * nc + cn];
+        for (int m = 0; m < 4; m++) Un[m] = (float)D.U[(size_t)m * nc + cn];
         const float sf = (float)(aj ? D.sj[mi(D, i, j)] : D.si[mi(D, i, j)]);
         const float dg = (float)(0.5 * (aj ? D.Lcj[cr] : D.Lci[cr]) + (aj ? D.Lvj[cr] : D.Lvi[cr]));
         float J[16];
-        flux_jac(Un, n1f, n2f, g, J);
+        flux_jacf(Un, n1f, n2f, g, J);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const float L = 0.5f * J[q] * sf + ((q % 5) == 0 ? dg : 0.f);
@@ -854,13 +860,13 @@ __device__ void line_row(const NsDev &D, const LineGeo &G, int ln, int k, float 
     }
     if (k < G.k1 || whi) {   // upper neighbour: C_up = -0.5 (A s - Lc) + Lv
         const size_t cn = aj ? c2(D, i, j + 1) : c2(D, i + 1, j), cr = whi ? c : cn;
-        double Un[4];
+        float Un[4];
 #pragma unroll
-        for (int m = 0; m < 4; m++) Un[m] = D.U[(size_t)m * nc + cn];
+        for (int m = 0; m < 4; m++) Un[m] = (float)D.U[(size_t)m * nc + cn];
         const float sf = (float)(aj ? D.sj[mi(D, i, j + 1)] : D.si[mi(D, i + 1, j)]);
         const float dg = (float)(0.5 * (aj ? D.Lcj[cr] : D.Lci[cr]) + (aj ? D.Lvj[cr] : D.Lvi[cr]));
         float J[16];
-        flux_jac(Un, n1f, n2f, g, J);
+        flux_jacf(Un, n1f, n2f, g, J);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             const float Cu = -0.5f * J[q] * sf + ((q % 5) == 0 ? dg : 0.f);
@@ -879,20 +885,19 @@ __device__ void line_row(const NsDev &D, const LineGeo &G, int ln, int k, float 
         }
         const int in = aj ? q : i, jn = aj ? j : q;
         const size_t cn = c2(D, in, jn);
-        double Un[4];
-        float dn[4], J[16];
+        float Un[4], dn[4], J[16];
 #pragma unroll
         for (int m = 0; m < 4; m++) {
-            Un[m] = D.U[(size_t)m * nc + cn];
+            Un[m] = (float)D.U[(size_t)m * nc + cn];
             dn[m] = (float)D.dU[(size_t)m * nc + cn];
         }
-        const double m1 = aj ? D.ni1[mi(D, i, j)] : D.nj1[mi(D, i, j)];
-        const double m2 = aj ? D.ni2[mi(D, i, j)] : D.nj2[mi(D, i, j)];
+        const float m1 = (float)(aj ? D.ni1[mi(D, i, j)] : D.nj1[mi(D, i, j)]);
+        const float m2 = (float)(aj ? D.ni2[mi(D, i, j)] : D.nj2[mi(D, i, j)]);
         const float dg = (float)(0.5 * (aj ? D.Lci[cn] : D.Lcj[cn]) + (aj ? D.Lvi[cn] : D.Lvj[cn]));
         const float sf = (float)(side == 0 ? (aj ? D.si[mi(D, i, j)] : D.sj[mi(D, i, j)])
                                            : (aj ? D.si[mi(D, i + 1, j)] : D.sj[mi(D, i, j + 1)]));
         const float sg = side == 0 ? 0.5f : -0.5f;
-        flux_jac(Un, m1, m2, g, J);
+        flux_jacf(Un, m1, m2, g, J);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             float v = dg * dn[r];
@@ -912,14 +917,20 @@ __device__ __forceinline__ void inv4f(float *M, float *Inv) {
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         int pr = c;
+        float best = fabsf(M[c * 4 + c]);
 #pragma unroll
-        for (int r = c + 1; r < 4; r++)
-            if (fabsf(M[r * 4 + c]) > fabsf(M[pr * 4 + c])) pr = r;
+        for (int r = c + 1; r < 4; r++) {
+            const float v = fabsf(M[r * 4 + c]);
+            if (v > best) { best = v; pr = r; }
+        }
+        // row swap with compile-time indices only (keeps M in registers)
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (pr != c) {
-                float t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t;
-                t = Inv[c * 4 + q]; Inv[c * 4 + q] = Inv[pr * 4 + q]; Inv[pr * 4 + q] = t;
+        for (int r = c + 1; r < 4; r++) {
+            if (r != pr) continue;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                float t = M[c * 4 + q]; M[c * 4 + q] = M[r * 4 + q]; M[r * 4 + q] = t;
+                t = Inv[c * 4 + q]; Inv[c * 4 + q] = Inv[r * 4 + q]; Inv[r * 4 + q] = t;
             }
         }
         const float ip = 1.f / M[c * 4 + c];
@@ -1462,9 +1473,11 @@ __device__ __forceinline__ void shakhov_params(double r, double u, double v, dou
     p[6] = (real)(cpt * qy);
 }
 
+// the Shakhov parameters of the corrected and of the kinetic moments, once
+// per band cell: par[q][cell], q < 7 new, q >= 7 old (cells off the band
+// are not read)
 template <typename real>
-__global__ void k_gsis_fcorr(NsDev D, real *f, const double *vx, const double *vy, int nvi, int nv, int Na, int Nb,
-                             double cpr) {
+__global__ void k_gsis_fparams(NsDev D, real *__restrict__ par, int Na, int Nb, double cpr) {
     const int PA = D.PA;
     const size_t ncell = (size_t)Nb * PA;
     const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1479,6 +1492,30 @@ __global__ void k_gsis_fcorr(NsDev D, real *f, const double *vx, const double *v
                          pn);
     shakhov_params<real>(D.sk[c], D.sk[nc + c], D.sk[2 * nc + c], D.sk[3 * nc + c], D.sk[4 * nc + c],
                          D.sk[5 * nc + c], cpr, po);
+#pragma unroll
+    for (int q = 0; q < 7; q++) {
+        par[(size_t)q * ncell + cell] = pn[q];
+        par[(size_t)(7 + q) * ncell + cell] = po[q];
+    }
+}
+
+template <typename real>
+__global__ void k_gsis_fcorr(NsDev D, real *f, const real *__restrict__ par, const double *vx, const double *vy,
+                             int nvi, int nv, int Na, int Nb) {
+    const int PA = D.PA;
+    const size_t ncell = (size_t)Nb * PA;
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= ncell) return;
+    const int a = (int)(cell % PA) + 1, b = (int)(cell / PA) + 1;
+    if (a > Na) return;
+    const int i = D.scan_is_j ? b : a, j = D.scan_is_j ? a : b;
+    if (i < D.ilo || i > D.ihi || j < D.jlo || j > D.jhi) return;
+    real pn[7], po[7];
+#pragma unroll
+    for (int q = 0; q < 7; q++) {
+        pn[q] = par[(size_t)q * ncell + cell];
+        po[q] = par[(size_t)(7 + q) * ncell + cell];
+    }
     const real fl = Consts<real>::floor_();
     const int nsl = gridDim.y, per = (nv + nsl - 1) / nsl;
     const int v0 = blockIdx.y * per, v1 = min(nv, v0 + per);
@@ -1536,6 +1573,7 @@ void ns_destroy(hyb_ctx *ctx) {
     if (st->h_ctrl) cudaFreeHost(st->h_ctrl);
     if (st->rk) cudaFree(st->rk);
     if (st->mlp_buf) cudaFree(st->mlp_buf);
+    if (st->fpar) cudaFree(st->fpar);
     if (ctx->d_rhs_gsis) cudaFree(ctx->d_rhs_gsis);
     ctx->d_rhs_gsis = nullptr;
     delete st;
@@ -1676,6 +1714,14 @@ int ns_create(hyb_ctx *ctx) {
         return HYB_ERR_NOMEM;
     }
     D.ctrl = st->ctrl;
+    if (cudaMalloc(&st->fpar, (size_t)14 * ncell * sizeof(double)) != cudaSuccess) {
+        st->fpar = nullptr;
+        cudaFree(st->buf); cudaFree(st->geo); cudaFree(st->rk); cudaFree(st->mlp_buf); cudaFree(st->ctrl);
+        cudaFreeHost(st->h_ctrl); cudaFree(ctx->d_rhs_gsis);
+        ctx->d_rhs_gsis = nullptr;
+        delete st;
+        return HYB_ERR_NOMEM;
+    }
     st->have_graph = false;
     // the line solver's reduction holds a line of up to PCR_MAX cells in
     // shared memory (set before any capture)
@@ -1771,18 +1817,24 @@ static int finish_correction(hyb_ctx *ctx, NsDev &D, bool correct_f) {
     k_gsis_finish<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     if (correct_f) {
-        // about four velocities per thread: the two Shakhov evaluations per
-        // velocity are FP64 exponentials, and small meshes need the velocity
-        // axis for parallelism
-        const int nsl = ctx->nv / 4 < 1 ? 1 : (ctx->nv / 4 > 4096 ? 4096 : ctx->nv / 4);
-        dim3 grd((unsigned)((ncell + 255) / 256), (unsigned)nsl);
-        if (ctx->precision == HYB_PREC_FP64)
-            k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
-                                                     ctx->Na, ctx->Nb, ctx->prm.cpr);
-        else
-            k_gsis_fcorr<float><<<grd, 256, 0, s>>>(D, (float *)ctx->d_f, ctx->d_vx, ctx->d_vy, ctx->nvi, ctx->nv,
-                                                    ctx->Na, ctx->Nb, ctx->prm.cpr);
-        ctx->launches++;
+        // the cells' parameters once, then a few velocities per thread (the
+        // two Shakhov evaluations per velocity; small meshes need the
+        // velocity axis for parallelism)
+        NsState *st = (NsState *)ctx->ns;
+        const unsigned gcell = (unsigned)((ncell + 255) / 256);
+        const int want = (int)((size_t)152 * 2048 * 4 / (ncell + 1));   // about four threads' worth per SM lane
+        const int nsl = want < 1 ? 1 : (want > ctx->nv ? ctx->nv : want);
+        dim3 grd(gcell, (unsigned)nsl);
+        if (ctx->precision == HYB_PREC_FP64) {
+            k_gsis_fparams<double><<<gcell, 256, 0, s>>>(D, (double *)st->fpar, ctx->Na, ctx->Nb, ctx->prm.cpr);
+            k_gsis_fcorr<double><<<grd, 256, 0, s>>>(D, (double *)ctx->d_f, (const double *)st->fpar, ctx->d_vx,
+                                                     ctx->d_vy, ctx->nvi, ctx->nv, ctx->Na, ctx->Nb);
+        } else {
+            k_gsis_fparams<float><<<gcell, 256, 0, s>>>(D, (float *)st->fpar, ctx->Na, ctx->Nb, ctx->prm.cpr);
+            k_gsis_fcorr<float><<<grd, 256, 0, s>>>(D, (float *)ctx->d_f, (const float *)st->fpar, ctx->d_vx,
+                                                    ctx->d_vy, ctx->nvi, ctx->nv, ctx->Na, ctx->Nb);
+        }
+        ctx->launches += 2;
     }
     if (ctx->precision == HYB_PREC_FP64)
         k_gsis_eqp<double><<<(unsigned)((ncell + 255) / 256), 256, 0, s>>>(D.S, D.nc, D.nx, (double *)ctx->d_eqp,
