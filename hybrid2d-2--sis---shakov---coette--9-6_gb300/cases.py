@@ -131,6 +131,10 @@ class Case:
     stretch: float = 0.0     # >0: tanh clustering of the y nodes towards both plates
     sweep_order: int = T.HYB_SWEEP_REFERENCE   # order of the kinetic implicit step
     mass_pin: int = 0        # 1: hold the total mass of f at its initial value
+    # boundary kind of faces 1..4 (x low, y low, x high, y high); the Couette
+    # channel is periodic in x with plates at the y faces.  Walls on the x
+    # faces are at rest at t_bottom (face 1) and t_top (face 3)
+    bcs: tuple = (T.HYB_BC_PERIODIC, T.HYB_BC_WALL, T.HYB_BC_PERIODIC, T.HYB_BC_WALL)
     extra: dict = field(default_factory=dict)
 
     # ---- derived arrays -------------------------------------------------
@@ -173,6 +177,10 @@ class Case:
         v[3] = np.zeros(self.ncx)
         t[1] = self.t_bottom * pert
         t[3] = self.t_top * pert
+        for f, tw in ((0, self.t_bottom), (2, self.t_top)):
+            u[f] = np.zeros(self.ncy)
+            v[f] = np.zeros(self.ncy)
+            t[f] = np.full(self.ncy, tw)
         return u, v, t
 
     def vgrid(self):
@@ -217,7 +225,7 @@ class Case:
         m = T.HybMesh()
         m.nx, m.ny = self.nx, self.ny
         m.x, m.y = T.dptr(x), T.dptr(y)
-        bcs = [T.HYB_BC_PERIODIC, T.HYB_BC_WALL, T.HYB_BC_PERIODIC, T.HYB_BC_WALL]
+        bcs = list(self.bcs)
         for f in range(4):
             m.bc[f] = bcs[f]
             if bcs[f] == T.HYB_BC_WALL:

@@ -323,7 +323,7 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
         size_t n = on_scan ? c->Nb : c->PA;
         ALLOC(c->d_fw[f], (size_t)c->nv * 2 * n * rs);
     }
-    if (rc == HYB_OK) ALLOC(c->d_eqp, 8 * ncell * rs);
+    if (rc == HYB_OK) ALLOC(c->d_eqp, hyb_eqp_elems(ncell) * rs);
     if (rc == HYB_OK) ALLOC(c->d_vol, ncell * rs);
     if (rc == HYB_OK) ALLOC(c->d_gA1, (size_t)c->Nb * (c->PA + 1) * rs);
     if (rc == HYB_OK) ALLOC(c->d_gA2, (size_t)c->Nb * (c->PA + 1) * rs);
@@ -444,6 +444,9 @@ int hyb_create(const hyb_mesh *m, const hyb_vgrid *vg, const hyb_params *p, hyb_
             c->sw_minb = d;
         }
     }
+    // HYB_SWEEP_GENERIC=1 keeps every sweep on the generic kernel (A/B
+    // timing and identity checks of the specialised FP32 NND sweep)
+    if (const char *e = getenv("HYB_SWEEP_GENERIC")) c->sw_generic = atoi(e) != 0;
     *out = c;
     return HYB_OK;
 }
@@ -496,7 +499,7 @@ int hyb_set_precision(hyb_ctx *ctx, int precision) {
         int on_scan = ctx->scan_is_j ? (f == 1 || f == 3) : (f == 0 || f == 2);
         rc = remake(&ctx->d_fw[f], (size_t)ctx->nv * 2 * (on_scan ? ctx->Nb : ctx->PA));
     }
-    if (!rc) rc = remake(&ctx->d_eqp, 8 * ncell);
+    if (!rc) rc = remake(&ctx->d_eqp, hyb_eqp_elems(ncell));
     if (!rc) rc = remake(&ctx->d_vol, ncell);
     if (!rc) rc = remake(&ctx->d_gA1, (size_t)ctx->Nb * (ctx->PA + 1));
     if (!rc) rc = remake(&ctx->d_gA2, (size_t)ctx->Nb * (ctx->PA + 1));

@@ -10,7 +10,8 @@
 //                                        to a multiple of 32 (128-B rows)
 //   fw_*   : real[Nv][NRD][n]           wall slot values (the reference's
 //                                        ghost index -3 / n+3)
-//   eqp    : real4[2][Nb*PA]            Shakhov parameters per cell
+//   eqp    : real[Nb*PA/128][8][128]    Shakhov parameters, blocks of 128
+//                                        cells (hyb_eqp_at)
 //   S      : double[NSUM][(nx+3)(ny+3)] moments on the reference extents
 //                                        (1-LAP:n+LAP-1), i fastest
 #pragma once
@@ -49,7 +50,7 @@ struct KinArgs {
     int no_update;         // 1: compute (and store) the RHS only, f is left as is
     const real *fw_alo, *fw_ahi;   // wall slots at the scan-axis ends [Nv][2][Nb]
     const real *fw_blo, *fw_bhi;   // wall slots at the march-axis ends [Nv][2][PA]
-    const real *eqp;      // [8][Nb*PA]: crt, u, v, invT, hT, cqx, cqy, cf
+    const real *eqp;      // hyb_eqp_at(cell, q), q: crt, u, v, invT, hT, cqx, cqy, cf
     const real *vol;      // [Nb*PA] cell volume
     // face normal * length, per face: scan faces [Nb][PA+1] (2 comps), march
     // faces [Nb+1][PA] (2 comps)
@@ -80,6 +81,7 @@ struct hyb_ctx {
     int nx, ny, ncx, ncy, nvi, nvj, nv;
     int scan_is_j, Na, Nb, PA, cpt;         // cpt: largest scan cells per sweep thread
     int sw_cpt, sw_vpb, sw_minb;             // chosen sweep launch shape (0: default)
+    int sw_generic;                          // 1: never the specialised FP32 NND sweep
     int bc[4];
     hyb_params prm;
     std::string last_error;
@@ -144,6 +146,20 @@ struct hyb_ctx {
 // C2 index on the (1-LAP:n+LAP-1) extents
 __host__ __device__ inline size_t hyb_c2(int nx, int i, int j) {
     return (size_t)(i + 1) + (size_t)(nx + 3) * (size_t)(j + 1);
+}
+
+// Shakhov parameter q (0..7) of sweep cell c = (b-1)*PA + (a-1).  Blocks of
+// HYB_EQP_BLK consecutive cells hold their eight parameters together,
+// [c/128][q][c%128]: a warp of the sweep (128 cells at 4 per thread) reads
+// parameter q of its cells as one contiguous 512-byte span (FP32), and each
+// thread finds its eight parameters at fixed offsets q * 128 from one
+// pointer.  The array holds hyb_eqp_elems(Nb*PA) values.
+#define HYB_EQP_BLK 128
+__host__ __device__ inline size_t hyb_eqp_at(size_t c, int q) {
+    return ((c >> 7) << 10) + ((size_t)q << 7) + (c & 127);
+}
+__host__ __device__ inline size_t hyb_eqp_elems(size_t ncell) {
+    return (size_t)8 * ((ncell + HYB_EQP_BLK - 1) / HYB_EQP_BLK * HYB_EQP_BLK);
 }
 
 // launch helpers implemented in the .cu files

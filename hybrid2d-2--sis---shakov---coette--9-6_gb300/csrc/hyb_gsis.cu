@@ -1544,13 +1544,13 @@ __global__ void k_gsis_eqp(const double *S, size_t nc, int nx, real *eqp, int Na
     size_t c = hyb_c2(nx, i, j);
     double S1 = S[c], u = S[nc + c], vv = S[2 * nc + c], tt = S[3 * nc + c], qx = S[7 * nc + c], qy = S[8 * nc + c];
     double cpt = cpr / (S1 * tt * tt);
-    eqp[0 * ncell + cell] = (real)(S1 / (HYB_PI * tt));
-    eqp[1 * ncell + cell] = (real)u;
-    eqp[2 * ncell + cell] = (real)vv;
-    eqp[3 * ncell + cell] = (real)(1.0 / tt);
-    eqp[4 * ncell + cell] = (real)(tt / 2.0);
-    eqp[5 * ncell + cell] = (real)(cpt * qx);
-    eqp[6 * ncell + cell] = (real)(cpt * qy);
+    eqp[hyb_eqp_at(cell, 0)] = (real)(S1 / (HYB_PI * tt));
+    eqp[hyb_eqp_at(cell, 1)] = (real)u;
+    eqp[hyb_eqp_at(cell, 2)] = (real)vv;
+    eqp[hyb_eqp_at(cell, 3)] = (real)(1.0 / tt);
+    eqp[hyb_eqp_at(cell, 4)] = (real)(tt / 2.0);
+    eqp[hyb_eqp_at(cell, 5)] = (real)(cpt * qx);
+    eqp[hyb_eqp_at(cell, 6)] = (real)(cpt * qy);
 }
 
 // ---- host ----------------------------------------------------------------------

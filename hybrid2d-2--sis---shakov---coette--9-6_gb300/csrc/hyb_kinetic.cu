@@ -481,7 +481,6 @@ __global__ void __launch_bounds__(NARROW ? 256 : 512, NARROW ? 3 : 1)
 
 template <typename real>
 __device__ __forceinline__ void moments_finish_body(const MomArgs &M, int lpc, int blk) {
-    const size_t ncell = (size_t)M.Nb * M.PA;
     SliceSum<real> acc[10];
     size_t cell;
     bool own;
@@ -522,14 +521,14 @@ __device__ __forceinline__ void moments_finish_body(const MomArgs &M, int lpc, i
     // Shakhov parameters of the next kinetic step (Get_Feq uses S1, S4 = T)
     real *ep = (real *)M.eqp;
     double cpt = M.cpr / (S1 * tt * tt);
-    ep[0 * ncell + cell] = (real)(S1 / (HYB_PI * tt));
-    ep[1 * ncell + cell] = (real)u;
-    ep[2 * ncell + cell] = (real)vv;
-    ep[3 * ncell + cell] = (real)(1.0 / tt);
-    ep[4 * ncell + cell] = (real)(tt / 2.0);
-    ep[5 * ncell + cell] = (real)(cpt * qx);
-    ep[6 * ncell + cell] = (real)(cpt * qy);
-    ep[7 * ncell + cell] = (real)cf;
+    ep[hyb_eqp_at(cell, 0)] = (real)(S1 / (HYB_PI * tt));
+    ep[hyb_eqp_at(cell, 1)] = (real)u;
+    ep[hyb_eqp_at(cell, 2)] = (real)vv;
+    ep[hyb_eqp_at(cell, 3)] = (real)(1.0 / tt);
+    ep[hyb_eqp_at(cell, 4)] = (real)(tt / 2.0);
+    ep[hyb_eqp_at(cell, 5)] = (real)(cpt * qx);
+    ep[hyb_eqp_at(cell, 6)] = (real)(cpt * qy);
+    ep[hyb_eqp_at(cell, 7)] = (real)cf;
 }
 
 template <typename real>

@@ -42,12 +42,16 @@ namespace hyb {
 
 constexpr int RING = 8;   // staged rows per velocity
 
+// shared memory of one velocity group; staged rows are sized with 16 bytes
+// of pad at each end, which the specialised FP32 sweep (hyb_sweep_nnd.cuh)
+// fills with wrapped halo cells
 template <typename real>
 __host__ __device__ inline size_t sweep_group_bytes(int PA, int TPV) {
     size_t nw = (size_t)TPV / 32;
+    size_t rs = (size_t)PA + 2 * 16 / sizeof(real);
     size_t b = 128;                                    // RING+2 mbarriers
-    b += (size_t)RING * 2 * PA * sizeof(real);         // staged rows
-    b += (size_t)2 * 2 * PA * sizeof(real);            // rows Nb+1, Nb+2 (periodic)
+    b += (size_t)RING * 2 * rs * sizeof(real);         // staged rows
+    b += (size_t)2 * 2 * rs * sizeof(real);            // rows Nb+1, Nb+2 (periodic)
     b += (size_t)2 * 2 * TPV * sizeof(real);           // first-cell dF per thread
     b += (size_t)2 * nw * 3 * sizeof(real);            // warp aggregates
     return (b + 127) / 128 * 128;
@@ -316,7 +320,17 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
     const real fl = Consts<real>::floor_();
     const real msc = A.mscale ? (real)*A.mscale : real(1);
     const real *ep = A.eqp;
-    const size_t ncell = (size_t)Nb * PA;
+    // CPT consecutive Shakhov parameters of the chunk (in the logical order)
+    auto lde = [&](const real *p, real *o) {
+        if (!ra) {
+            Vec<real, CPT>::ld(p, o);
+        } else {
+            real t[CPT];
+            Vec<real, CPT>::ld(p, t);
+#pragma unroll
+            for (int k = 0; k < CPT; k++) o[k] = t[CPT - 1 - k];
+        }
+    };
 
     for (int bp = -1; bp <= 2; bp++) wait_row(bp);
     // the copies of rows 1, 2 for rows Nb+1, Nb+2 read f rows that the
@@ -396,14 +410,17 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
             const size_t prow0 = (size_t)(prow(b) - 1) * PA;    // physical row start
             const size_t cell0 = prow0 + pa0;
             real e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT], vl[CPT];
-            ldc(ep + 0 * ncell + prow0, e_crt);
-            ldc(ep + 1 * ncell + prow0, e_u);
-            ldc(ep + 2 * ncell + prow0, e_v);
-            ldc(ep + 3 * ncell + prow0, e_it);
-            ldc(ep + 4 * ncell + prow0, e_ht);
-            ldc(ep + 5 * ncell + prow0, e_qx);
-            ldc(ep + 6 * ncell + prow0, e_qy);
-            ldc(ep + 7 * ncell + prow0, e_cf);
+            // the CPT cells of the chunk lie in one block of the parameter
+            // layout (pa0 is a multiple of CPT, CPT divides the block)
+            const real *ec = ep + hyb_eqp_at(cell0, 0);
+            lde(ec + 0 * HYB_EQP_BLK, e_crt);
+            lde(ec + 1 * HYB_EQP_BLK, e_u);
+            lde(ec + 2 * HYB_EQP_BLK, e_v);
+            lde(ec + 3 * HYB_EQP_BLK, e_it);
+            lde(ec + 4 * HYB_EQP_BLK, e_ht);
+            lde(ec + 5 * HYB_EQP_BLK, e_qx);
+            lde(ec + 6 * HYB_EQP_BLK, e_qy);
+            lde(ec + 7 * HYB_EQP_BLK, e_cf);
             if (!UNI) Vec<real, CPT>::ld(A.vol + cell0, vl);
             // the next row's Shakhov parameters towards L1 while this row
             // computes (one prefetch per 128-byte line)
@@ -411,7 +428,7 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
                 const size_t nxt = (size_t)(prow(b + 1) - 1) * PA + pa0;
 #pragma unroll
                 for (int q = 0; q < 8; q++)
-                    asm volatile("prefetch.global.L1 [%0];" ::"l"(ep + q * ncell + nxt));
+                    asm volatile("prefetch.global.L1 [%0];" ::"l"(ep + hyb_eqp_at(nxt, q)));
             }
             if (stdB) {
                 real p0[CPT], p1[CPT], q0[CPT], q1[CPT];

@@ -1,8 +1,10 @@
 // hyb_sweep_f32.cu -- FP32-distribution instantiations of the fused sweep.
 #include "hyb_sweep.cuh"
+#include "hyb_sweep_nnd.cuh"
 
 namespace hyb {
 int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb, bool launch) {
+    if (!ctx->sw_generic && sweep_nnd4_applies(ctx, A, cpt)) return sweep_nnd4_dispatch(ctx, A, vpb, launch);
     return sweep_launch_real<float>(ctx, A, cpt, vpb, launch);
 }
 size_t sweep_group_bytes_f32(int PA, int tpv) { return sweep_group_bytes<float>(PA, tpv); }

@@ -1,0 +1,476 @@
+// hyb_sweep_nnd.cuh -- the fused kinetic step (GKUA_Residual.f90:4-469) for
+// its most common form: FP32 distributions, a uniform Cartesian mesh, the
+// reference order, the NND scheme and 4 scan cells per thread.  The work
+// decomposition, the affine scan and the backward step are those of
+// sweep_body (hyb_sweep.cuh); what differs is how a row is read and how the
+// face values are formed, so that a thread spends its instructions on the
+// arithmetic of its cells rather than on addressing and operand selection:
+//
+// * Staged rows carry 16 bytes of pad on each side.  On a periodic scan axis
+//   the producer copies the two wrapped halo cells of each end into the pads
+//   (cp.async.bulk of the 16-byte blocks at the other end), so a thread reads
+//   its window f(a0-2 .. a0+5) at fixed offsets from its own chunk: one
+//   16-byte and two 8-byte shared loads per component.
+// * The Shakhov parameters of the thread's cells are read at fixed offsets
+//   from one pointer into the blocked layout (hyb_eqp_at; a warp's 128 cells
+//   are one block, each parameter a contiguous 512-byte span), which advances
+//   one row per step; each lane prefetches one 128-byte line of its warp's
+//   block of the next row into L1.
+// * March faces: the three rows of the upwind stencil are chosen per row by
+//   pointer (rows b-1, b, b+1 for a positive face speed, b+2, b+1, b for a
+//   negative one), so one limiter formula serves both directions with no
+//   per-value selects.  The value is the one RHSFDVsub forms
+//   (GKUA_Residual.f90:155-185) with the same operations in the same order.
+// * Scan faces: NND's left state of face q is f(q-1) + 0.5 mm(D(q-1), D(q-2))
+//   and its right state f(q) - 0.5 mm(D(q-1), D(q)) with D(k) = f(k+1) - f(k)
+//   (GKUA_Residual.f90:160-175).  Both use the limited slope of one cell,
+//   sigma(k) = mm(D(k), D(k-1)), so the thread forms sigma once per window
+//   cell and the upwind face value f(k) + h sigma(k), h = +-0.5 by the sign of
+//   the face speed; the face takes the value of its upwind cell.  FMINMD is
+//   symmetric, so these are the reference's values (the sign of a zero slope
+//   aside, which cannot change a sum).
+// * Periodicity of each axis and the axis roles are template parameters.
+#pragma once
+#include "hyb_sweep.cuh"
+
+namespace hyb {
+
+constexpr int NND_PAD = 4;   // floats of pad before and after a staged row
+
+template <bool PERA, bool PERB, bool SJ>
+__device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
+    constexpr int CPT = 4;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int PA = A.PA, Na = A.Na, Nb = A.Nb;
+    const int TPV = PA / CPT;
+    const int RS = PA + 2 * NND_PAD;             // floats per staged component row
+    const int g = threadIdx.y, t = threadIdx.x;
+    const int pa0 = t * CPT;                     // first cell of the thread, 0-based
+    const int lane = t & 31, warp = t >> 5, nw = TPV >> 5;
+    const int v = vblk * blockDim.y + g;
+    const bool vok = v < A.nv;
+    const bool act = vok && pa0 < Na;            // chunks are all-in or all-out
+    const bool producer = (t == 0) && vok;
+
+    unsigned char *base = smem_raw + (size_t)g * sweep_group_bytes<float>(PA, TPV);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base);
+    float *ring = reinterpret_cast<float *>(base + 128);
+    float *wrap = ring + (size_t)RING * 2 * RS;
+    float *dlf = wrap + (size_t)2 * 2 * RS;      // [2][2][TPV]
+    float *agg = dlf + (size_t)2 * 2 * TPV;      // [2][nw][3]
+
+    const size_t rstride = (size_t)Nb * PA;
+    const size_t vrow0 = vok ? (size_t)v * 2 * rstride : 0;
+    const uint32_t main_bytes = (uint32_t)(Na * sizeof(float));   // Na is a multiple of 4
+    const uint32_t tx = 2u * (main_bytes + (PERA ? 32u : 0u));
+
+    // ---- velocity and face speeds (uniform mesh) --------------------------------
+    const int iv = vok ? v % A.nvi : 0, jv = vok ? v / A.nvi : 0;
+    const float vx = vok ? (float)A.vx[iv] : 0.f, vy = vok ? (float)A.vy[jv] : 0.f;
+    const float sA = vx * A.gA1[0] + vy * A.gA2[0];
+    const float sB = vx * A.gB1[0] + vy * A.gB2[0];
+    const float vol = A.vol[0];
+    const float ivol = 1.f / vol;
+    const float abase = vol / A.dt + (posp(sA) - negp(sA) + posp(sB) - negp(sB));
+    const bool upA = sA > 0.f, upB = sB > 0.f;
+    const float hA = upA ? 0.5f : -0.5f;
+    const float pA = posp(sA), pB = posp(sB);
+    const float cA = -negp(sA), cB = -negp(sB);
+
+    // ---- staged rows ---------------------------------------------------------
+    auto phys_row = [&](int bp) -> int {
+        if (bp >= 1 && bp <= Nb) return bp;
+        if (PERB && bp <= 0) return bp + Nb;
+        return 0;
+    };
+    // f row pr (1..Nb) into a staged row whose cell 0 is at dst
+    auto copy_row = [&](float *dst, int pr, uint64_t *bar) {
+        const float *src = A.f + vrow0 + (size_t)(pr - 1) * PA;
+        mbar_arrive_expect_tx(bar, tx);
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            float *d = dst + r * RS;
+            const float *s = src + r * rstride;
+            bulk_g2s(d, s, main_bytes, bar);
+            if (PERA) {
+                bulk_g2s(d - NND_PAD, s + Na - NND_PAD, 16, bar);   // cells Na-4 .. Na-1 before cell 0
+                bulk_g2s(d + Na, s, 16, bar);                       // cells 0 .. 3 after cell Na-1
+            }
+        }
+    };
+    auto issue_row = [&](int bp) {
+        const int s = (bp + 1) & (RING - 1);
+        const int pr = phys_row(bp);
+        if (A.stall_row > 0 && bp == A.stall_row) return;   // hyb_test_stall: a wait nothing completes
+        if (pr > 0 && bp <= Nb) copy_row(ring + (size_t)s * 2 * RS + NND_PAD, pr, &bars[s]);
+        else mbar_arrive(&bars[s]);                          // keeps the slot's phase count
+    };
+    if (producer) {
+        for (int s = 0; s < RING + 2; s++) mbar_init(&bars[s], 1);
+        fence_async_shared();
+    }
+    __syncthreads();
+    if (producer) {
+        for (int bp = -1; bp <= RING - 3; bp++) issue_row(bp);
+        if (PERB)
+            for (int w = 0; w < 2; w++) copy_row(wrap + (size_t)w * 2 * RS + NND_PAD, w + 1, &bars[RING + w]);
+    }
+    // cell 0 of the G row of logical row bp (H is RS further)
+    auto rowp = [&](int bp) -> const float * {
+        if (PERB && bp > Nb) return wrap + (size_t)(bp - Nb - 1) * 2 * RS + NND_PAD;
+        return ring + (size_t)((bp + 1) & (RING - 1)) * 2 * RS + NND_PAD;
+    };
+    bool timeout = false;
+    auto wait_row = [&](int bp) {
+        if (!vok) return;
+        if (bp > Nb) {
+            if (PERB && !mbar_wait_bounded(&bars[RING + (bp - Nb - 1)], 0, A.spin)) timeout = true;
+            return;
+        }
+        if (phys_row(bp) == 0) return;
+        const unsigned k = (unsigned)(bp + 1);
+        if (!mbar_wait_bounded(&bars[k & (RING - 1)], (k / RING) & 1u, A.spin)) timeout = true;
+    };
+    auto ld4 = [](const float *p, float *o) {
+        const float4 x = *reinterpret_cast<const float4 *>(p);
+        o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w;
+    };
+    auto st4 = [](float *p, const float *o) { *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]); };
+    // march-face flux at the thread's cells from the upwind stencil rows
+    // x1, x2, x3 (GKUA_Residual.f90:155-185 with the mirrored inputs of a
+    // negative speed)
+    auto march_flux = [&](const float *x1, const float *x2, const float *x3, float *FG, float *FH) {
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            float a[4], m[4], c[4];
+            ld4(x1 + r * RS + pa0, a);
+            ld4(x2 + r * RS + pa0, m);
+            ld4(x3 + r * RS + pa0, c);
+            float *F = r ? FH : FG;
+#pragma unroll
+            for (int k = 0; k < 4; k++) F[k] = sB * (m[k] + 0.5f * fminmd(c[k] - m[k], m[k] - a[k]));
+        }
+    };
+    // march-face flux through face q next to a wall of the march axis
+    // (faces 1, 2, Nb, Nb+1; GKUA_Residual.f90:196-257)
+    auto march_wall = [&](int q, float *FG, float *FH) {
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            float *F = r ? FH : FG;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int o = r * RS + pa0 + k;
+                if (q == 1) F[k] = sB * A.fw_blo[((size_t)v * 2 + r) * PA + pa0 + k];
+                else if (q == Nb + 1) F[k] = sB * A.fw_bhi[((size_t)v * 2 + r) * PA + pa0 + k];
+                else if (q == 2) F[k] = flux_wlo<HYB_SCHEME_NND>(sB, rowp(1)[o], rowp(2)[o], rowp(3)[o]);
+                else if (q == Nb) F[k] = flux_whi<HYB_SCHEME_NND>(sB, rowp(Nb)[o], rowp(Nb - 1)[o], rowp(Nb - 2)[o]);
+                else F[k] = flux_std<HYB_SCHEME_NND>(sB, rowp(q - 2)[o], rowp(q - 1)[o], rowp(q)[o], rowp(q + 1)[o]);
+            }
+        }
+    };
+
+    // ---- carried state per cell --------------------------------------------------
+    float dG[CPT], dH[CPT];            // forward values of the previous row
+    float iap[CPT];                    // 1/alpha of the previous row
+    float FBl_G[CPT], FBl_H[CPT];      // march flux through face b
+#pragma unroll
+    for (int k = 0; k < CPT; k++) {
+        dG[k] = dH[k] = 0.f;
+        iap[k] = 1.f;
+        FBl_G[k] = FBl_H[k] = 0.f;
+    }
+    const float fl = Consts<float>::floor_();
+    const float msc = A.mscale ? (float)*A.mscale : 1.f;
+    // this thread's parameters in row 1: PA is a multiple of the 128-cell
+    // block, so a row is PA / 128 whole blocks (8 * PA values)
+    const float *epr = A.eqp + hyb_eqp_at((size_t)pa0, 0);
+    const size_t ep_row = (size_t)8 * PA;
+    // line `lane` of the warp's block in the next row (the block starts
+    // 4 * lane values before this thread's parameters)
+    const size_t ep_pf = ep_row + (size_t)28 * lane;
+    float *fst = A.f + vrow0 + pa0;                      // row 1 of the update
+    float *rst = A.rhs ? A.rhs + vrow0 + pa0 : nullptr;  // row 1 of the RHS store
+
+    for (int bp = -1; bp <= 2; bp++) wait_row(bp);
+    // the copies of rows 1, 2 for rows Nb+1, Nb+2 read f rows that the
+    // backward step overwrites from step 2 on: they complete before any write
+    if (PERB) {
+        wait_row(Nb + 1);
+        wait_row(Nb + 2);
+    }
+    if (act) {
+        if (PERB) march_flux(upB ? rowp(-1) : rowp(2), upB ? rowp(0) : rowp(1), upB ? rowp(1) : rowp(0), FBl_G, FBl_H);
+        else march_wall(1, FBl_G, FBl_H);
+    }
+    const bool need_scan = __syncthreads_or(vok && upA) != 0;
+
+    for (int b = 1; b <= Nb; b++) {
+        // each thread waits on the row's mbarrier itself (that wait makes the
+        // bulk copy visible); a timed-out wait is acted on at the row's one
+        // block barrier below, before anything is written to f
+        if (b + 2 <= Nb) wait_row(b + 2);
+        float pc[CPT], cG[CPT], cH[CPT], ia[CPT], FBh_G[CPT], FBh_H[CPT];
+        float fo0[CPT], fo1[CPT];          // f of row b-1 (for the backward update)
+        float P = 1.f, CGt = 0.f, CHt = 0.f;
+        if (act) {
+            const float *rm = rowp(b - 1), *r0 = rowp(b), *rp = rowp(b + 1), *rq = rowp(b + 2);
+            // window f(a0-2 .. a0+5) of both components
+            float wG[8], wH[8];
+            {
+                const float2 lg = *reinterpret_cast<const float2 *>(r0 + pa0 - 2);
+                const float2 hg = *reinterpret_cast<const float2 *>(r0 + pa0 + 4);
+                const float2 lh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 - 2);
+                const float2 hh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 + 4);
+                wG[0] = lg.x; wG[1] = lg.y; wG[6] = hg.x; wG[7] = hg.y;
+                wH[0] = lh.x; wH[1] = lh.y; wH[6] = hh.x; wH[7] = hh.y;
+                ld4(r0 + pa0, wG + 2);
+                ld4(r0 + RS + pa0, wH + 2);
+            }
+            // scan-face fluxes through faces a0 .. a0+4 (window cells m+1 | m+2)
+            float FA_G[CPT + 1], FA_H[CPT + 1];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const float *w = r ? wH : wG;
+                float *F = r ? FA_H : FA_G;
+                float D[7], val[7];
+#pragma unroll
+                for (int k = 0; k < 7; k++) D[k] = w[k + 1] - w[k];
+#pragma unroll
+                for (int k = 1; k < 7; k++) val[k] = w[k] + hA * fminmd(D[k], D[k - 1]);
+#pragma unroll
+                for (int m = 0; m <= CPT; m++) F[m] = sA * (upA ? val[m + 1] : val[m + 2]);
+            }
+            if (!PERA) {
+                // faces 1, 2 and Na, Na+1 next to the walls of the scan axis
+                // (GKUA_Residual.f90:196-257)
+                if (pa0 == 0) {
+                    FA_G[0] = sA * A.fw_alo[((size_t)v * 2 + 0) * Nb + (b - 1)];
+                    FA_H[0] = sA * A.fw_alo[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[1] = flux_wlo<HYB_SCHEME_NND>(sA, wG[2], wG[3], wG[4]);
+                    FA_H[1] = flux_wlo<HYB_SCHEME_NND>(sA, wH[2], wH[3], wH[4]);
+                }
+                if (pa0 + CPT == Na) {
+                    FA_G[3] = flux_whi<HYB_SCHEME_NND>(sA, wG[5], wG[4], wG[3]);
+                    FA_H[3] = flux_whi<HYB_SCHEME_NND>(sA, wH[5], wH[4], wH[3]);
+                    FA_G[4] = sA * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
+                    FA_H[4] = sA * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                }
+            }
+            float m0[CPT], m1[CPT];
+            ld4(rm + pa0, m0);
+            ld4(rm + RS + pa0, m1);
+            // Shakhov parameters of the thread's cells
+            float e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT];
+            ld4(epr + 0 * HYB_EQP_BLK, e_crt);
+            ld4(epr + 1 * HYB_EQP_BLK, e_u);
+            ld4(epr + 2 * HYB_EQP_BLK, e_v);
+            ld4(epr + 3 * HYB_EQP_BLK, e_it);
+            ld4(epr + 4 * HYB_EQP_BLK, e_ht);
+            ld4(epr + 5 * HYB_EQP_BLK, e_qx);
+            ld4(epr + 6 * HYB_EQP_BLK, e_qy);
+            ld4(epr + 7 * HYB_EQP_BLK, e_cf);
+            if (b < Nb) asm volatile("prefetch.global.L1 [%0];" ::"l"(epr + ep_pf));
+            // march faces b+1
+            if (PERB || (b >= 2 && b <= Nb - 2)) march_flux(upB ? rm : rq, upB ? r0 : rp, upB ? rp : r0, FBh_G, FBh_H);
+            else march_wall(b + 1, FBh_G, FBh_H);
+            float rG[CPT], rH[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                fo0[k] = m0[k];
+                fo1[k] = m1[k];
+                float divG, divH;
+                if (SJ) {
+                    divG = (FBh_G[k] - FBl_G[k]) + FA_G[k + 1] - FA_G[k];
+                    divH = (FBh_H[k] - FBl_H[k]) + FA_H[k + 1] - FA_H[k];
+                } else {
+                    divG = (FA_G[k + 1] - FA_G[k]) + FBh_G[k] - FBl_G[k];
+                    divH = (FA_H[k + 1] - FA_H[k]) + FBh_H[k] - FBl_H[k];
+                }
+                // Shakhov equilibrium (GKUA_Residual.f90:441-458)
+                const float viu = vx - e_u[k], vjv = vy - e_v[k];
+                const float vij2 = (viu * viu + vjv * vjv) * e_it[k];
+                const float fvx = e_qx[k] * viu + e_qy[k] * vjv;
+                const float gdv = e_crt[k] * sweep_exp<float>(-vij2);
+                const float geq = gdv * (1.f + fvx * (2.f * vij2 - 4.f));
+                const float heq = (e_ht[k] * gdv) * (1.f + fvx * (2.f * vij2 - 2.f));
+                rG[k] = -divG * ivol + e_cf[k] * (geq - wG[k + 2]);
+                rH[k] = -divH * ivol + e_cf[k] * (heq - wH[k + 2]);
+                // LU-SGS forward element (GKUA_Residual.f90:39-57)
+                const float alfa = abase + vol * e_cf[k];
+                ia[k] = sweep_rcp<float>(alfa);
+                pc[k] = pA * ia[k];
+                cG[k] = (vol * rG[k] + pB * dG[k]) * ia[k];
+                cH[k] = (vol * rH[k] + pB * dH[k]) * ia[k];
+                // thread-local composition of the affine maps
+                CGt = cG[k] + pc[k] * CGt;
+                CHt = cH[k] + pc[k] * CHt;
+                P = pc[k] * P;
+            }
+            if (rst) {
+                st4(rst, rG);
+                st4(rst + rstride, rH);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < CPT; k++) pc[k] = cG[k] = cH[k] = ia[k] = FBh_G[k] = FBh_H[k] = fo0[k] = fo1[k] = 0.f;
+            P = 0.f;
+        }
+        epr += ep_row;
+        if (rst) rst += PA;
+        float Pe = 1.f, Ge = 0.f, He = 0.f;
+        float *aggb = agg + (size_t)(b & 1) * nw * 3;
+        if (need_scan) {
+            // inclusive warp scan of the composed maps (earlier lanes first)
+            float Pi = P, Gi = CGt, Hi = CHt;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const float pu = __shfl_up_sync(0xffffffffu, Pi, off);
+                const float gu = __shfl_up_sync(0xffffffffu, Gi, off);
+                const float hu = __shfl_up_sync(0xffffffffu, Hi, off);
+                if (lane >= off) {
+                    Gi = Gi + Pi * gu;
+                    Hi = Hi + Pi * hu;
+                    Pi = Pi * pu;
+                }
+            }
+            Pe = __shfl_up_sync(0xffffffffu, Pi, 1);
+            Ge = __shfl_up_sync(0xffffffffu, Gi, 1);
+            He = __shfl_up_sync(0xffffffffu, Hi, 1);
+            if (lane == 0) { Pe = 1.f; Ge = 0.f; He = 0.f; }
+            if (lane == 31) {
+                aggb[warp * 3 + 0] = Pi;
+                aggb[warp * 3 + 1] = Gi;
+                aggb[warp * 3 + 2] = Hi;
+            }
+        }
+        if (__syncthreads_or(timeout)) {
+            if (t == 0 && g == 0) atomicExch(A.err, HYB_ERR_TIMEOUT);
+            if (producer) sweep_drain(bars, b, Nb, A.stall_row, A.spin);
+            return;
+        }
+        // every thread is past this row's reads, so the slot of row b-3 is free
+        if (producer) issue_row(b + RING - 3);
+        float xG = Ge, xH = He;                              // dF just before cell a0
+        if (need_scan && warp > 0) {
+            float carG = 0.f, carH = 0.f;
+            for (int w = 0; w < warp; w++) {
+                const float pw = aggb[w * 3 + 0];
+                carG = aggb[w * 3 + 1] + pw * carG;
+                carH = aggb[w * 3 + 2] + pw * carH;
+            }
+            xG = Ge + Pe * carG;
+            xH = He + Pe * carH;
+        }
+        float nG[CPT], nH[CPT];
+#pragma unroll
+        for (int k = 0; k < CPT; k++) {
+            xG = cG[k] + pc[k] * xG;
+            xH = cH[k] + pc[k] * xH;
+            nG[k] = xG;
+            nH[k] = xH;
+        }
+        float *dlb = dlf + (size_t)(b & 1) * 2 * TPV;
+        dlb[t] = act ? nG[0] : 0.f;
+        dlb[TPV + t] = act ? nH[0] : 0.f;
+        // backward + update of row b-1 (GKUA_Residual.f90:64-109)
+        if (b > 1) {
+            if (act && !A.no_update) {
+                const float *dlp = dlf + (size_t)((b - 1) & 1) * 2 * TPV;
+                const bool has_next = (pa0 + CPT < Na);
+                const float lastG = has_next ? dlp[t + 1] : 0.f, lastH = has_next ? dlp[TPV + t + 1] : 0.f;
+                float uG[CPT], uH[CPT];
+#pragma unroll
+                for (int k = 0; k < CPT; k++) {
+                    const float nxG = (k + 1 < CPT) ? dG[k + 1] : lastG;
+                    const float nxH = (k + 1 < CPT) ? dH[k + 1] : lastH;
+                    const float fg = msc * (fo0[k] + (dG[k] + (cA * nxG + cB * nG[k]) * iap[k]));
+                    const float fh = msc * (fo1[k] + (dH[k] + (cA * nxH + cB * nH[k]) * iap[k]));
+                    uG[k] = fg < fl ? fl : fg;
+                    uH[k] = fh < fl ? fl : fh;
+                }
+                st4(fst, uG);
+                st4(fst + rstride, uH);
+            }
+            fst += PA;
+        }
+#pragma unroll
+        for (int k = 0; k < CPT; k++) {
+            dG[k] = nG[k];
+            dH[k] = nH[k];
+            iap[k] = ia[k];
+            FBl_G[k] = FBh_G[k];
+            FBl_H[k] = FBh_H[k];
+        }
+    }
+    __syncthreads();
+    if (act && !A.no_update) {   // backward + update of the last row (downstream values are 0)
+        const float *dlp = dlf + (size_t)(Nb & 1) * 2 * TPV;
+        const bool has_next = (pa0 + CPT < Na);
+        const float *o0 = rowp(Nb);
+        float f0[CPT], f1[CPT], uG[CPT], uH[CPT];
+        ld4(o0 + pa0, f0);
+        ld4(o0 + RS + pa0, f1);
+#pragma unroll
+        for (int k = 0; k < CPT; k++) {
+            const float nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : 0.f);
+            const float nxH = (k + 1 < CPT) ? dH[k + 1] : (has_next ? dlp[TPV + t + 1] : 0.f);
+            const float fg = msc * (f0[k] + (dG[k] + (cA * nxG) * iap[k]));
+            const float fh = msc * (f1[k] + (dH[k] + (cA * nxH) * iap[k]));
+            uG[k] = fg < fl ? fl : fg;
+            uH[k] = fh < fl ? fl : fh;
+        }
+        st4(fst, uG);
+        st4(fst + rstride, uH);
+    }
+    // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
+    // for above, so no copy is in flight when the CTA exits
+}
+
+template <bool PERA, bool PERB, bool SJ>
+__global__ void __launch_bounds__(256, 2) k_sweep_nnd4(KinArgs<float> A) {
+    sweep_nnd4<PERA, PERB, SJ>(A, blockIdx.x);
+}
+
+template <bool PERA, bool PERB, bool SJ>
+int sweep_nnd4_launch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
+    const int tpv = ctx->PA / 4;
+    const size_t smem = sweep_group_bytes<float>(ctx->PA, tpv) * vpb;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sweep_nnd4<PERA, PERB, SJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    if (!launch) return HYB_OK;
+    dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
+    k_sweep_nnd4<PERA, PERB, SJ><<<grd, blk, smem, ctx->stream>>>(A);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("k_sweep_nnd4: ") + cudaGetErrorString(e);
+        return HYB_ERR_CUDA;
+    }
+    return HYB_OK;
+}
+
+// the specialised sweep covers FP32, uniform meshes, the reference order, NND
+// and 4 cells per thread; returns false when the context is outside that
+inline bool sweep_nnd4_applies(const hyb_ctx *ctx, const KinArgs<float> &A, int cpt) {
+    return cpt == 4 && ctx->uniform && ctx->prm.sweep_order == HYB_SWEEP_REFERENCE && A.scheme == HYB_SCHEME_NND &&
+           A.Na % 4 == 0 && A.PA % HYB_EQP_BLK == 0;
+}
+
+inline int sweep_nnd4_dispatch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
+    const bool pa = A.bca_lo == AX_PERIODIC, pb = A.bcb_lo == AX_PERIODIC, sj = A.scan_is_j != 0;
+    if (pa) {
+        if (pb) return sj ? sweep_nnd4_launch<true, true, true>(ctx, A, vpb, launch)
+                          : sweep_nnd4_launch<true, true, false>(ctx, A, vpb, launch);
+        return sj ? sweep_nnd4_launch<true, false, true>(ctx, A, vpb, launch)
+                  : sweep_nnd4_launch<true, false, false>(ctx, A, vpb, launch);
+    }
+    if (pb) return sj ? sweep_nnd4_launch<false, true, true>(ctx, A, vpb, launch)
+                      : sweep_nnd4_launch<false, true, false>(ctx, A, vpb, launch);
+    return sj ? sweep_nnd4_launch<false, false, true>(ctx, A, vpb, launch)
+              : sweep_nnd4_launch<false, false, false>(ctx, A, vpb, launch);
+}
+
+}  // namespace hyb

@@ -36,10 +36,11 @@ def _pair(abi, case, precision):
     return g, o
 
 
-@pytest.mark.parametrize("precision,order", [(0, 0), (1, 0), (0, 1)])
-def test_sweep_row_wait_runs_out_and_context_recovers(mods, precision, order):
+@pytest.mark.parametrize("precision,order,ncy", [(0, 0, 32), (1, 0, 32), (0, 1, 32), (1, 0, 128)])
+def test_sweep_row_wait_runs_out_and_context_recovers(mods, precision, order, ncy):
+    """ncy = 128 runs the specialised FP32 NND sweep (4 cells per thread)."""
     abi, cases, T = mods
-    c = cases.couette_small(ncy=32, nvx=16, nvy=16, dt=0.05 if order == 0 else 1.0e6, sweep_order=order)
+    c = cases.couette_small(ncy=ncy, nvx=16, nvy=16, dt=0.05 if order == 0 else 1.0e6, sweep_order=order)
     g, o = _pair(abi, c, precision)
     g.step(2)
     o.step(2)

@@ -6,7 +6,8 @@ whose device memory is reserved by another allocator).  The test plays such a
 caller: it owns the device buffers (allocated here, by the test) and checks
 the entry point's S_GKUA and CF against the context path's hyb_detfp output
 for the same distribution, on two calls in a row, within the FP64 parity
-tolerance of the other GPU tests (1e-12 relative).
+tolerance of the other GPU tests (1e-12 relative), and its S_GKUA against the
+oracle's DETFP of the same distribution.
 
 Kept in its own file, collected last, so that a failure here cannot hide the
 other GPU tests in a run that stops at the first failure.
@@ -79,6 +80,11 @@ def test_detfp_noalloc_matches_context_path(pkg, shape):
     frd = g.download_f()
     s_ref, cf_ref = g.moments()          # the context path: hyb_detfp on the same f
     g.close()
+    from oracle.oracle import Oracle
+    o = Oracle(c)
+    o.upload_f(frd)
+    o.detfp()
+    s_orc = o.s_gkua()
     vi, wi, vj, wj = (np.ascontiguousarray(a, dtype=np.float64) for a in c.vgrid())
     bufs = [DevBuf(rt, a) for a in (frd, vi, vj, wi, wj, np.zeros_like(s_ref), np.zeros_like(cf_ref))]
     dfrd, dvi, dvj, dwi, dwj, ds, dcf = bufs
@@ -96,6 +102,10 @@ def test_detfp_noalloc_matches_context_path(pkg, shape):
             for k in range(10):
                 scale = max(np.abs(b[..., k]).max(), 1e-3)
                 assert np.abs(a[..., k] - b[..., k]).max() <= 1e-12 * scale, (call, k)
+            a, b = _interior(c, s_out), _interior(c, s_orc)
+            for k in range(10):
+                scale = max(np.abs(b[..., k]).max(), 1e-3)
+                assert np.abs(a[..., k] - b[..., k]).max() <= 1e-12 * scale, ("oracle", call, k)
             ca, cb = _cf_interior(c, cf_out), _cf_interior(c, cf_ref)
             assert np.abs(ca - cb).max() <= 1e-12 * np.abs(cb).max(), call
     finally:
