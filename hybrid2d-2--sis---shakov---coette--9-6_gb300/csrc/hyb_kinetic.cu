@@ -460,6 +460,164 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
         for (int c = 0; c < MC; c++) store_part<real>(M.part, ((size_t)slice * NM + q) * ncell + cell0 + c, ks[q][c]);
 }
 
+// ---- FP32 moment pass, two cells per thread, packed pairs -------------------
+// The DETFP moments (NM = 10) or moments 1-4 of a stored RHS (NM = 4) of FP32
+// distributions.  Same ring, slices, block sums and Kahan sums as
+// moments_body; the arithmetic differs in form only:
+// * the weight of each moment per velocity (w, w vx, w vy, vx^2 + vy^2,
+//   w vx^2, w vy^2, w vx vy) is formed once per CTA and stored twice over, so
+//   that a packed FP32 pair reads it from shared memory as a register pair;
+// * the two cells of a thread are summed as one packed pair, one FFMA2 per
+//   moment and velocity (w vx^2 G is (w vx^2) G here, w vx (vx G) there: FP32
+//   rounding of the products differs, the sums are the same moments).
+// The Kahan terms stay in registers: at 80 registers (three CTAs per SM) a
+// few of them spill around the block flushes, which measured faster than
+// keeping the compensations in shared memory (0.54 against 0.75 ms on the
+// 128x512 x 64^2 Couette case).
+constexpr int MOMF2_COEF = 16;   // floats per velocity in the weight table
+
+__host__ __device__ inline size_t mom_f2_coef_bytes(int nloc_max) {
+    return ((size_t)MOMF2_COEF * nloc_max * sizeof(float) + 127) / 128 * 128;
+}
+__host__ __device__ inline size_t mom_f2_smem_bytes(int PA, int nloc_max) {
+    return 256 + mom_f2_coef_bytes(nloc_max) + (size_t)MOM_NST * MomVps<float>::v * 2 * PA * sizeof(float);
+}
+
+__device__ __forceinline__ float2 m2_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 m2_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 m2_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+template <int NM>
+__device__ __forceinline__ void moments_body_f2(const MomArgs &M, int bidx, int slice) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int VPS = MomVps<float>::v;
+    constexpr int FLUSH = 8 / VPS;                  // slots per block of 8 velocities
+    const int PA = M.PA, t = threadIdx.x, TPV = blockDim.x;
+    const int b = bidx + 1;
+    const int a0 = t * 2 + 1;
+    const bool act = a0 <= M.Na;
+    const int nvi = M.nvi, nvj = M.nv / M.nvi;
+    const int jv0 = (int)((long long)nvj * slice / M.vs), jv1 = (int)((long long)nvj * (slice + 1) / M.vs);
+    const int v0 = jv0 * nvi, nloc = (jv1 - jv0) * nvi;
+    const int nslot = (nloc + VPS - 1) / VPS;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
+    uint64_t *empty = full + MOM_NST;
+    float *coef = reinterpret_cast<float *>(smem_raw + 256);          // [nloc][16]
+    float *stage = reinterpret_cast<float *>(smem_raw + 256 + mom_f2_coef_bytes(M.nloc_max));
+    const size_t rs = (size_t)M.Nb * PA;
+    const float *f = (const float *)M.f;
+    const uint32_t row_bytes = (uint32_t)(PA * sizeof(float));
+    const int nwarp = TPV >> 5, lane = t & 31;
+    for (int k = t; k < nloc; k += TPV) {
+        const float vx = (float)M.vx[k % nvi], vy = (float)M.vy[jv0 + k / nvi], wv = (float)M.w[(size_t)v0 + k];
+        const float wx = wv * vx, wy = wv * vy;
+        float4 *d = reinterpret_cast<float4 *>(coef + (size_t)k * MOMF2_COEF);
+        const float c2 = vx * vx + vy * vy, wxx = wx * vx, wyy = wy * vy, wxy = wx * vy;
+        d[0] = make_float4(wv, wv, wx, wx);
+        d[1] = make_float4(wy, wy, c2, c2);
+        d[2] = make_float4(wxx, wxx, wyy, wyy);
+        d[3] = make_float4(wxy, wxy, 0.f, 0.f);
+    }
+    if (t == 0) {
+        for (int k = 0; k < MOM_NST; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], nwarp);
+        }
+        fence_async_shared();
+    }
+    __syncthreads();
+    auto issue = [&](int n) {
+        const int k = n % MOM_NST;
+        const int cnt = min(VPS, nloc - n * VPS);
+        mbar_arrive_expect_tx(&full[k], 2 * row_bytes * cnt);
+        for (int u = 0; u < cnt; u++) {
+            const float *src = f + (size_t)(v0 + n * VPS + u) * 2 * rs + (size_t)(b - 1) * PA;
+            float *dst = stage + ((size_t)k * VPS + u) * 2 * PA;
+            bulk_g2s(dst, src, row_bytes, &full[k]);
+            bulk_g2s(dst + PA, src + rs, row_bytes, &full[k]);
+        }
+    };
+    int issued = 0;   // slots issued (thread 0)
+    if (t == 0)
+        for (; issued < MOM_NST - 1 && issued < nslot; issued++) issue(issued);
+    // plain sums over blocks of 8 velocities, Kahan sums of the blocks
+    float2 blk[NM], ks[NM], kc[NM];
+#pragma unroll
+    for (int q = 0; q < NM; q++) blk[q] = ks[q] = kc[q] = make_float2(0.f, 0.f);
+    bool ok = true;
+    for (int n = 0; n < nslot; n++) {
+        const int k = n % MOM_NST;
+        if (t == 0 && ok && n + MOM_NST - 1 < nslot) {
+            if (n >= 1 && !mbar_wait_bounded(&empty[(n - 1) % MOM_NST], (uint32_t)(((n - 1) / MOM_NST) & 1), M.spin))
+                ok = false;
+            else
+                issue(issued++);
+        }
+        if (ok && !mbar_wait_bounded(&full[k], (uint32_t)((n / MOM_NST) & 1), M.spin)) ok = false;
+        if (act && ok) {
+            const int cnt = min(VPS, nloc - n * VPS);
+            const float *gs = stage + (size_t)k * VPS * 2 * PA + (a0 - 1);
+#pragma unroll
+            for (int u = 0; u < VPS; u++) {
+                if (u < cnt) {
+                    const float4 *cw = reinterpret_cast<const float4 *>(coef + (size_t)(n * VPS + u) * MOMF2_COEF);
+                    const float4 c0 = cw[0], c1 = cw[1];
+                    const float2 wv = make_float2(c0.x, c0.y), wx = make_float2(c0.z, c0.w);
+                    const float2 wy = make_float2(c1.x, c1.y), c2 = make_float2(c1.z, c1.w);
+                    const float2 g = *reinterpret_cast<const float2 *>(gs + (size_t)u * 2 * PA);
+                    const float2 h = *reinterpret_cast<const float2 *>(gs + (size_t)u * 2 * PA + PA);
+                    const float2 b4 = m2_fma(c2, g, h);                     // H + c^2 G
+                    blk[0] = m2_fma(wv, g, blk[0]);
+                    blk[1] = m2_fma(wx, g, blk[1]);
+                    blk[2] = m2_fma(wy, g, blk[2]);
+                    blk[3] = m2_fma(wv, b4, blk[3]);
+                    if constexpr (NM > 4) {
+                        const float4 c2v = cw[2], c3v = cw[3];
+                        blk[4] = m2_fma(make_float2(c2v.x, c2v.y), g, blk[4]);
+                        blk[5] = m2_fma(make_float2(c2v.z, c2v.w), g, blk[5]);
+                        blk[6] = m2_fma(make_float2(c3v.x, c3v.y), g, blk[6]);
+                        blk[7] = m2_fma(wx, b4, blk[7]);
+                        blk[8] = m2_fma(wy, b4, blk[8]);
+                        blk[9] = m2_fma(wv, h, blk[9]);
+                    }
+                }
+            }
+            if ((n % FLUSH) == FLUSH - 1 || n == nslot - 1) {
+#pragma unroll
+                for (int q = 0; q < NM; q++) {
+                    const float2 y = m2_sub(blk[q], kc[q]);
+                    const float2 s2 = m2_add(ks[q], y);
+                    kc[q] = m2_sub(m2_sub(s2, ks[q]), y);
+                    ks[q] = s2;
+                    blk[q] = make_float2(0.f, 0.f);
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[k]);
+    }
+    if (__syncthreads_or(!ok)) {
+        if (t == 0) {
+            atomicExch(M.err, HYB_ERR_TIMEOUT);
+            for (int n = issued > MOM_NST ? issued - MOM_NST : 0; n < issued; n++)
+                mbar_wait_bounded(&full[n % MOM_NST], (uint32_t)((n / MOM_NST) & 1), M.spin);
+        }
+        return;
+    }
+    if (!act) return;
+    const size_t ncell = (size_t)M.Nb * PA;
+    const size_t cell0 = (size_t)(b - 1) * PA + (a0 - 1);    // even: the two cells' pairs are one 16-byte store
+#pragma unroll
+    for (int q = 0; q < NM; q++)
+        *reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(M.part) + ((size_t)slice * NM + q) * ncell + cell0) =
+            make_float4(ks[q].x, -kc[q].x, ks[q].y, -kc[q].y);
+}
+
+template <int NM>
+__global__ void __launch_bounds__(256, 3) k_moments_f2(MomArgs M) {
+    moments_body_f2<NM>(M, blockIdx.x, blockIdx.y);
+}
+
 // NARROW: CTAs of at most 256 threads, three per SM (80 registers); FP32
 // rows of up to 512 cells take it, wider rows and FP64 keep 512 threads
 template <typename real, int MC, int NM, bool NARROW>
@@ -885,6 +1043,20 @@ static MomArgs mom_args(hyb_ctx *ctx, const void *f, size_t *smem, int *mc) {
 
 template <int NM>
 static int launch_mom_pass(hyb_ctx *ctx, const MomArgs &M, int mc, size_t smem) {
+    if constexpr (NM == 10 || NM == 4) {
+        // FP32 rows of up to 512 cells at two cells per thread: the packed pass
+        const size_t s2 = mom_f2_smem_bytes(ctx->PA, M.nloc_max);
+        if (ctx->precision != HYB_PREC_FP64 && mc == 2 && ctx->PA / 2 <= 256 && s2 <= (size_t)227 * 1024) {
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_moments_f2<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+                attr = true;
+            }
+            k_moments_f2<NM><<<dim3(ctx->Nb, M.vs), ctx->PA / 2, s2, ctx->stream>>>(M);
+            ctx->launches++;
+            return check_err(ctx, "k_moments_f2");
+        }
+    }
     if (smem > (size_t)227 * 1024) {
         ctx->last_error = "moments: velocity slice too large for shared memory";
         return HYB_ERR_UNSUPPORTED;

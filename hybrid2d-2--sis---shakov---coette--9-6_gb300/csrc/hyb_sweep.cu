@@ -20,7 +20,13 @@ void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb) {
     int c = ctx->sw_cpt > 0 ? ctx->sw_cpt : ctx->cpt;
     if (ctx->cpt % c != 0 || ctx->PA / c > 256) c = ctx->cpt;
     int tpv = ctx->PA / c;
-    int v = ctx->sw_vpb > 0 ? ctx->sw_vpb : 256 / tpv;
+    // the specialised FP32 NND sweep runs best in CTAs of 128 threads (one
+    // velocity per CTA at PA = 512: 1.67 against 1.84 ms on the 128x512 x 64^2
+    // Couette case); the others default to 256
+    const bool nnd4 = c == 4 && !ctx->sw_generic && ctx->precision != HYB_PREC_FP64 && ctx->uniform &&
+                      ctx->prm.sweep_order == HYB_SWEEP_REFERENCE && ctx->prm.scheme == HYB_SCHEME_NND &&
+                      ctx->Na % 4 == 0 && ctx->PA % HYB_EQP_BLK == 0;
+    int v = ctx->sw_vpb > 0 ? ctx->sw_vpb : (nnd4 ? 128 : 256) / tpv;
     if (v < 1) v = 1;
     while (v > 1 && tpv * v > 256) v--;
     *cpt = c;

@@ -28,7 +28,9 @@
 //   cell and the upwind face value f(k) + h sigma(k), h = +-0.5 by the sign of
 //   the face speed; the face takes the value of its upwind cell.  FMINMD is
 //   symmetric, so these are the reference's values (the sign of a zero slope
-//   aside, which cannot change a sum).
+//   aside, which cannot change a sum).  FMINMD itself is the median of its
+//   arguments and 0 (four min/max operations).
+// * Arithmetic on neighbouring cells runs as packed FP32 pairs.
 // * Periodicity of each axis and the axis roles are template parameters.
 #pragma once
 #include "hyb_sweep.cuh"
@@ -36,6 +38,24 @@
 namespace hyb {
 
 constexpr int NND_PAD = 4;   // floats of pad before and after a staged row
+
+// Packed FP32 pairs (FADD2 / FMUL2 / FFMA2 of sm_100 and later): the same
+// IEEE round-to-nearest results as the scalar operations, two lanes per
+// instruction.  The sweep pairs neighbouring cells (2p, 2p+1) of a thread.
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 pk(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 pk(const float *a, int p) { return make_float2(a[2 * p], a[2 * p + 1]); }
+__device__ __forceinline__ void upk(float2 x, float *a, int p) { a[2 * p] = x.x; a[2 * p + 1] = x.y; }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b as b * (-1) + a: one rounding, the value of the subtraction
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// FMINMD (Functions.f90:10-25) as the median of x, y and 0: the
+// smaller-magnitude argument when both have the same sign, else 0 -- the
+// reference's value, from four FP32 min/max operations
+__device__ __forceinline__ float mmed(float x, float y) { return fmaxf(fminf(x, y), fminf(fmaxf(x, y), 0.f)); }
+__device__ __forceinline__ float2 mm2(float2 x, float2 y) { return make_float2(mmed(x.x, y.x), mmed(x.y, y.y)); }
 
 template <bool PERA, bool PERB, bool SJ>
 __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
@@ -148,7 +168,10 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
             ld4(x3 + r * RS + pa0, c);
             float *F = r ? FH : FG;
 #pragma unroll
-            for (int k = 0; k < 4; k++) F[k] = sB * (m[k] + 0.5f * fminmd(c[k] - m[k], m[k] - a[k]));
+            for (int p = 0; p < 2; p++) {
+                const float2 mp = pk(m, p);
+                upk(mul2(pk(sB), fma2(pk(0.5f), mm2(sub2(pk(c, p), mp), sub2(mp, pk(a, p))), mp)), F, p);
+            }
         }
     };
     // march-face flux through face q next to a wall of the march axis
@@ -204,6 +227,10 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
     }
     const bool need_scan = __syncthreads_or(vok && upA) != 0;
 
+    // two rows per trip: the row parity of the double buffers is then fixed
+    // in each copy of the body, and the carried state changes registers
+    // without moves in between
+#pragma unroll 2
     for (int b = 1; b <= Nb; b++) {
         // each thread waits on the row's mbarrier itself (that wait makes the
         // bulk copy visible); a timed-out wait is acted on at the row's one
@@ -236,7 +263,7 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
 #pragma unroll
                 for (int k = 0; k < 7; k++) D[k] = w[k + 1] - w[k];
 #pragma unroll
-                for (int k = 1; k < 7; k++) val[k] = w[k] + hA * fminmd(D[k], D[k - 1]);
+                for (int k = 1; k < 7; k++) val[k] = w[k] + hA * mmed(D[k], D[k - 1]);
 #pragma unroll
                 for (int m = 0; m <= CPT; m++) F[m] = sA * (upA ? val[m + 1] : val[m + 2]);
             }
@@ -278,30 +305,43 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
             for (int k = 0; k < CPT; k++) {
                 fo0[k] = m0[k];
                 fo1[k] = m1[k];
-                float divG, divH;
+            }
+            // cells in pairs (2p, 2p+1)
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+                const float2 fa0G = pk(FA_G[2 * p], FA_G[2 * p + 1]), fa1G = pk(FA_G[2 * p + 1], FA_G[2 * p + 2]);
+                const float2 fa0H = pk(FA_H[2 * p], FA_H[2 * p + 1]), fa1H = pk(FA_H[2 * p + 1], FA_H[2 * p + 2]);
+                float2 divG, divH;
                 if (SJ) {
-                    divG = (FBh_G[k] - FBl_G[k]) + FA_G[k + 1] - FA_G[k];
-                    divH = (FBh_H[k] - FBl_H[k]) + FA_H[k + 1] - FA_H[k];
+                    divG = sub2(add2(sub2(pk(FBh_G, p), pk(FBl_G, p)), fa1G), fa0G);
+                    divH = sub2(add2(sub2(pk(FBh_H, p), pk(FBl_H, p)), fa1H), fa0H);
                 } else {
-                    divG = (FA_G[k + 1] - FA_G[k]) + FBh_G[k] - FBl_G[k];
-                    divH = (FA_H[k + 1] - FA_H[k]) + FBh_H[k] - FBl_H[k];
+                    divG = sub2(add2(sub2(fa1G, fa0G), pk(FBh_G, p)), pk(FBl_G, p));
+                    divH = sub2(add2(sub2(fa1H, fa0H), pk(FBh_H, p)), pk(FBl_H, p));
                 }
                 // Shakhov equilibrium (GKUA_Residual.f90:441-458)
-                const float viu = vx - e_u[k], vjv = vy - e_v[k];
-                const float vij2 = (viu * viu + vjv * vjv) * e_it[k];
-                const float fvx = e_qx[k] * viu + e_qy[k] * vjv;
-                const float gdv = e_crt[k] * sweep_exp<float>(-vij2);
-                const float geq = gdv * (1.f + fvx * (2.f * vij2 - 4.f));
-                const float heq = (e_ht[k] * gdv) * (1.f + fvx * (2.f * vij2 - 2.f));
-                rG[k] = -divG * ivol + e_cf[k] * (geq - wG[k + 2]);
-                rH[k] = -divH * ivol + e_cf[k] * (heq - wH[k + 2]);
+                const float2 viu = sub2(pk(vx), pk(e_u, p)), vjv = sub2(pk(vy), pk(e_v, p));
+                const float2 vij2 = mul2(fma2(viu, viu, mul2(vjv, vjv)), pk(e_it, p));
+                const float2 fvx = fma2(pk(e_qx, p), viu, mul2(pk(e_qy, p), vjv));
+                const float2 gdv = mul2(pk(e_crt, p), pk(sweep_exp<float>(-vij2.x), sweep_exp<float>(-vij2.y)));
+                const float2 geq = mul2(gdv, fma2(fvx, fma2(pk(2.f), vij2, pk(-4.f)), pk(1.f)));
+                const float2 heq = mul2(mul2(pk(e_ht, p), gdv), fma2(fvx, fma2(pk(2.f), vij2, pk(-2.f)), pk(1.f)));
+                const float2 ecf = pk(e_cf, p);
+                const float2 r2G = fma2(divG, pk(-ivol), mul2(ecf, sub2(geq, pk(wG + 2, p))));
+                const float2 r2H = fma2(divH, pk(-ivol), mul2(ecf, sub2(heq, pk(wH + 2, p))));
+                upk(r2G, rG, p);
+                upk(r2H, rH, p);
                 // LU-SGS forward element (GKUA_Residual.f90:39-57)
-                const float alfa = abase + vol * e_cf[k];
-                ia[k] = sweep_rcp<float>(alfa);
-                pc[k] = pA * ia[k];
-                cG[k] = (vol * rG[k] + pB * dG[k]) * ia[k];
-                cH[k] = (vol * rH[k] + pB * dH[k]) * ia[k];
-                // thread-local composition of the affine maps
+                const float2 alfa = fma2(pk(vol), ecf, pk(abase));
+                const float2 ia2 = pk(sweep_rcp<float>(alfa.x), sweep_rcp<float>(alfa.y));
+                upk(ia2, ia, p);
+                upk(mul2(pk(pA), ia2), pc, p);
+                upk(mul2(fma2(pk(vol), r2G, mul2(pk(pB), pk(dG, p))), ia2), cG, p);
+                upk(mul2(fma2(pk(vol), r2H, mul2(pk(pB), pk(dH, p))), ia2), cH, p);
+            }
+            // thread-local composition of the affine maps
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
                 CGt = cG[k] + pc[k] * CGt;
                 CHt = cH[k] + pc[k] * CHt;
                 P = pc[k] * P;
@@ -379,14 +419,18 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
                 const bool has_next = (pa0 + CPT < Na);
                 const float lastG = has_next ? dlp[t + 1] : 0.f, lastH = has_next ? dlp[TPV + t + 1] : 0.f;
                 float uG[CPT], uH[CPT];
+                const float nxG[CPT] = {dG[1], dG[2], dG[3], lastG}, nxH[CPT] = {dH[1], dH[2], dH[3], lastH};
 #pragma unroll
-                for (int k = 0; k < CPT; k++) {
-                    const float nxG = (k + 1 < CPT) ? dG[k + 1] : lastG;
-                    const float nxH = (k + 1 < CPT) ? dH[k + 1] : lastH;
-                    const float fg = msc * (fo0[k] + (dG[k] + (cA * nxG + cB * nG[k]) * iap[k]));
-                    const float fh = msc * (fo1[k] + (dH[k] + (cA * nxH + cB * nH[k]) * iap[k]));
-                    uG[k] = fg < fl ? fl : fg;
-                    uH[k] = fh < fl ? fl : fh;
+                for (int p = 0; p < 2; p++) {
+                    const float2 ip = pk(iap, p);
+                    const float2 g2 = mul2(pk(msc), add2(pk(fo0, p), fma2(fma2(pk(cA), pk(nxG, p), mul2(pk(cB), pk(nG, p))),
+                                                                          ip, pk(dG, p))));
+                    const float2 h2 = mul2(pk(msc), add2(pk(fo1, p), fma2(fma2(pk(cA), pk(nxH, p), mul2(pk(cB), pk(nH, p))),
+                                                                          ip, pk(dH, p))));
+                    uG[2 * p] = g2.x < fl ? fl : g2.x;
+                    uG[2 * p + 1] = g2.y < fl ? fl : g2.y;
+                    uH[2 * p] = h2.x < fl ? fl : h2.x;
+                    uH[2 * p + 1] = h2.y < fl ? fl : h2.y;
                 }
                 st4(fst, uG);
                 st4(fst + rstride, uH);
