@@ -1,5 +1,5 @@
 """mlp_oracle.py -- CPU restatement of the learned-closure MLP (forward, loss,
-backward) used to check the GPU kernels' gradients.
+backward, Adam step) used to check the GPU kernels' gradients and updates.
 
 TEST INFRASTRUCTURE ONLY: only tests/, __graft_entry__.smoke() and bench.py's
 CPU baseline may import it; the product never does.
@@ -96,6 +96,20 @@ def loss_and_grad(w, x, y_true, norm, quantize=True):
     g["b1"] = dz1.sum(0)
     g["W1"] = q(dz1).T @ c["xn"]
     return loss, pack(g)
+
+
+def adam_step(w, m1, m2, g, t, lr):
+    """One Adam step in FP32, as k_mlp_adam (csrc/hyb_mlp.cu) takes it:
+    beta1 0.9, beta2 0.999, eps 1e-8, bias corrections 1 - beta^t of the
+    step count t (1 for the first step).  Returns the new (w, m1, m2)."""
+    f = np.float32
+    w, m1, m2, g = (np.asarray(a, dtype=np.float32) for a in (w, m1, m2, g))
+    c1 = f(1.0) - f(0.9) ** f(t)
+    c2 = f(1.0) - f(0.999) ** f(t)
+    a = f(0.9) * m1 + f(0.1) * g
+    b = f(0.999) * m2 + f(0.001) * g * g
+    w = w - f(lr) * (a / c1) / (np.sqrt(b / c2) + f(1e-8))
+    return w.astype(np.float32), a, b
 
 
 def glorot(seed):

@@ -65,6 +65,34 @@ def test_forward_matches_cpu_restatement(pkg):
     assert np.abs(yg - yo).max() < 1e-3 * np.abs(yo).max()
 
 
+def test_adam_steps_match_cpu_restatement(pkg):
+    """Three Adam steps of one full batch each: the GPU's FP32 master weights
+    after every step against the restatement's update from the same
+    gradient (the network's own, read back with hyb_mlp_grad; the training
+    step reduces the same tiles in the same order).  The bias corrections
+    and first and second moments carry over the steps."""
+    rng = np.random.default_rng(21)
+    net, w = _net(13)
+    norm = _norm(rng)
+    net.set_norm(*norm)
+    n, lr = 3000, 1e-3
+    x = (rng.standard_normal((n, 8)) * norm[1] + norm[0]).astype(np.float32)
+    y = rng.standard_normal((n, 4)).astype(np.float32)
+    net.set_data(x, y)
+    wc = w.astype(np.float32)
+    m1 = np.zeros_like(wc)
+    m2 = np.zeros_like(wc)
+    for t in (1, 2, 3):
+        _, g = net.grad(x, y)
+        net.train_epoch(np.arange(n), batch=n, lr=lr)
+        wc, m1, m2 = M.adam_step(wc, m1, m2, g, t, lr)
+        wg = net.params()
+        # FP32 rounding of the update (about lr) and of the weight itself
+        tol = 1e-5 * lr + 2.0 * np.spacing(np.abs(wc))
+        assert np.all(np.abs(wg - wc) <= tol), (t, np.abs(wg - wc).max())
+        assert np.abs(wg - w).max() > 0.5 * lr          # the weights did move
+
+
 def test_training_lowers_loss_and_is_deterministic(pkg):
     rng = np.random.default_rng(5)
     x = rng.uniform(-1, 1, (40000, 8)).astype(np.float32)
