@@ -449,7 +449,7 @@ int hyb_autotune(hyb_ctx *ctx, int reps, int *cpt_out, int *vpb_out) {
     const int cands_c[3] = {4, 2, 1}, cands_v[4] = {1, 2, 4, 8};
     for (int ci = 0; ci < 3; ci++) {
         const int c = cands_c[ci];
-        if (ctx->cpt % c != 0 || ctx->PA / c > 256) continue;
+        if (!hyb::sweep_cpt_ok(ctx, c)) continue;
         for (int vi = 0; vi < 4; vi++) {
             const int v = cands_v[vi];
             if ((ctx->PA / c) * v > 256) continue;

@@ -164,6 +164,8 @@ __host__ __device__ inline size_t hyb_eqp_elems(size_t ncell) {
 
 // launch helpers implemented in the .cu files
 namespace hyb {
+bool sweep_nnd_ok(const hyb_ctx *ctx, int cpt);
+bool sweep_cpt_ok(const hyb_ctx *ctx, int cpt);
 int launch_wall(hyb_ctx *ctx);
 int launch_sweep(hyb_ctx *ctx, int store_rhs);
 int sweep_prepare(hyb_ctx *ctx);

@@ -16,17 +16,31 @@ size_t sweep_group_bytes_f64(int PA, int tpv);
 // and velocity groups per CTA (vpb, CTAs of at most 256 threads).  The
 // autotuner sets ctx->sw_cpt / sw_vpb by timing; HYB_SWEEP_SHAPE="cpt,vpb,0"
 // overrides them at context creation.
+size_t sweep_nnd_group_bytes_f32(int PA, int tpv);
+
+// the specialised FP32 NND sweep (hyb_sweep_nnd.cuh) covers this context at
+// c cells per thread: FP32, uniform mesh, reference order, NND, 4 cells per
+// thread on the layout's 128-cell chunks
+bool sweep_nnd_ok(const hyb_ctx *ctx, int c) {
+    if (ctx->sw_generic || ctx->precision == HYB_PREC_FP64 || !ctx->uniform ||
+        ctx->prm.sweep_order != HYB_SWEEP_REFERENCE || ctx->prm.scheme != HYB_SCHEME_NND)
+        return false;
+    return c == 4 && ctx->cpt == 4 && ctx->Na % 4 == 0 && ctx->PA % HYB_EQP_BLK == 0;
+}
+
+// cells per thread c admissible for the context's sweep
+bool sweep_cpt_ok(const hyb_ctx *ctx, int c) {
+    return (c == 1 || c == 2 || c == 4) && ctx->cpt % c == 0 && ctx->PA / c <= 256;
+}
+
 void sweep_shape(const hyb_ctx *ctx, int *cpt, int *vpb) {
     int c = ctx->sw_cpt > 0 ? ctx->sw_cpt : ctx->cpt;
-    if (ctx->cpt % c != 0 || ctx->PA / c > 256) c = ctx->cpt;
+    if (!sweep_cpt_ok(ctx, c)) c = ctx->cpt;
     int tpv = ctx->PA / c;
     // the specialised FP32 NND sweep runs best in CTAs of 128 threads (one
     // velocity per CTA at PA = 512: 1.67 against 1.84 ms on the 128x512 x 64^2
     // Couette case); the others default to 256
-    const bool nnd4 = c == 4 && !ctx->sw_generic && ctx->precision != HYB_PREC_FP64 && ctx->uniform &&
-                      ctx->prm.sweep_order == HYB_SWEEP_REFERENCE && ctx->prm.scheme == HYB_SCHEME_NND &&
-                      ctx->Na % 4 == 0 && ctx->PA % HYB_EQP_BLK == 0;
-    int v = ctx->sw_vpb > 0 ? ctx->sw_vpb : (nnd4 ? 128 : 256) / tpv;
+    int v = ctx->sw_vpb > 0 ? ctx->sw_vpb : (sweep_nnd_ok(ctx, c) ? 128 : 256) / tpv;
     if (v < 1) v = 1;
     while (v > 1 && tpv * v > 256) v--;
     *cpt = c;
@@ -38,7 +52,8 @@ size_t sweep_smem_bytes(const hyb_ctx *ctx) {
     sweep_shape(ctx, &cpt, &vpb);
     int tpv = ctx->PA / cpt;
     size_t g = ctx->precision == HYB_PREC_FP64 ? sweep_group_bytes_f64(ctx->PA, tpv)
-                                               : sweep_group_bytes_f32(ctx->PA, tpv);
+               : sweep_nnd_ok(ctx, cpt)         ? sweep_nnd_group_bytes_f32(ctx->PA, tpv)
+                                                : sweep_group_bytes_f32(ctx->PA, tpv);
     return g * vpb;
 }
 

@@ -42,16 +42,12 @@ namespace hyb {
 
 constexpr int RING = 8;   // staged rows per velocity
 
-// shared memory of one velocity group; staged rows are sized with 16 bytes
-// of pad at each end, which the specialised FP32 sweep (hyb_sweep_nnd.cuh)
-// fills with wrapped halo cells
 template <typename real>
 __host__ __device__ inline size_t sweep_group_bytes(int PA, int TPV) {
     size_t nw = (size_t)TPV / 32;
-    size_t rs = (size_t)PA + 2 * 16 / sizeof(real);
     size_t b = 128;                                    // RING+2 mbarriers
-    b += (size_t)RING * 2 * rs * sizeof(real);         // staged rows
-    b += (size_t)2 * 2 * rs * sizeof(real);            // rows Nb+1, Nb+2 (periodic)
+    b += (size_t)RING * 2 * PA * sizeof(real);         // staged rows
+    b += (size_t)2 * 2 * PA * sizeof(real);            // rows Nb+1, Nb+2 (periodic)
     b += (size_t)2 * 2 * TPV * sizeof(real);           // first-cell dF per thread
     b += (size_t)2 * nw * 3 * sizeof(real);            // warp aggregates
     return (b + 127) / 128 * 128;

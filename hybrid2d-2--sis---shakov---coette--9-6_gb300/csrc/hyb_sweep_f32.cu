@@ -4,9 +4,10 @@
 
 namespace hyb {
 int sweep_launch_f32(hyb_ctx *ctx, const KinArgs<float> &A, int cpt, int vpb, bool launch) {
-    if (!ctx->sw_generic && sweep_nnd4_applies(ctx, A, cpt)) return sweep_nnd4_dispatch(ctx, A, vpb, launch);
+    if (sweep_nnd_ok(ctx, cpt)) return sweep_nnd_dispatch(ctx, A, vpb, launch);
     return sweep_launch_real<float>(ctx, A, cpt, vpb, launch);
 }
+size_t sweep_nnd_group_bytes_f32(int PA, int tpv) { return nnd_group_bytes(PA, tpv); }
 size_t sweep_group_bytes_f32(int PA, int tpv) { return sweep_group_bytes<float>(PA, tpv); }
 int sweep_batch_f32(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int cpt, int vpb, bool uni,
                    int scheme, cudaStream_t s) {

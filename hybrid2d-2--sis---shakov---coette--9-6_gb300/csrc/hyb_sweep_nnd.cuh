@@ -39,6 +39,18 @@ namespace hyb {
 
 constexpr int NND_PAD = 4;   // floats of pad before and after a staged row
 
+// shared memory of one velocity group: the layout of sweep_body's with
+// padded staged rows
+__host__ __device__ inline size_t nnd_group_bytes(int PA, int TPV) {
+    const size_t nw = (size_t)TPV / 32, rs = (size_t)PA + 2 * NND_PAD;
+    size_t b = 128;                                    // RING+2 mbarriers
+    b += (size_t)RING * 2 * rs * sizeof(float);        // staged rows
+    b += (size_t)2 * 2 * rs * sizeof(float);           // rows Nb+1, Nb+2 (periodic)
+    b += (size_t)2 * 2 * TPV * sizeof(float);          // first-cell dF per thread
+    b += (size_t)2 * nw * 3 * sizeof(float);           // warp aggregates
+    return (b + 127) / 128 * 128;
+}
+
 // Packed FP32 pairs (FADD2 / FMUL2 / FFMA2 of sm_100 and later): the same
 // IEEE round-to-nearest results as the scalar operations, two lanes per
 // instruction.  The sweep pairs neighbouring cells (2p, 2p+1) of a thread.
@@ -57,9 +69,9 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 __device__ __forceinline__ float mmed(float x, float y) { return fmaxf(fminf(x, y), fminf(fmaxf(x, y), 0.f)); }
 __device__ __forceinline__ float2 mm2(float2 x, float2 y) { return make_float2(mmed(x.x, y.x), mmed(x.y, y.y)); }
 
-template <bool PERA, bool PERB, bool SJ>
-__device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
-    constexpr int CPT = 4;
+template <int CPT, bool PERA, bool PERB, bool SJ>
+__device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
+    static_assert(CPT == 4 || CPT == 8, "4 or 8 cells per thread");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int PA = A.PA, Na = A.Na, Nb = A.Nb;
     const int TPV = PA / CPT;
@@ -72,7 +84,7 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
     const bool act = vok && pa0 < Na;            // chunks are all-in or all-out
     const bool producer = (t == 0) && vok;
 
-    unsigned char *base = smem_raw + (size_t)g * sweep_group_bytes<float>(PA, TPV);
+    unsigned char *base = smem_raw + (size_t)g * nnd_group_bytes(PA, TPV);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base);
     float *ring = reinterpret_cast<float *>(base + 128);
     float *wrap = ring + (size_t)RING * 2 * RS;
@@ -156,19 +168,28 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
         o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w;
     };
     auto st4 = [](float *p, const float *o) { *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]); };
+    // the CPT consecutive values at p (16-byte aligned)
+    auto ldc = [&](const float *p, float *o) {
+#pragma unroll
+        for (int h = 0; h < CPT / 4; h++) ld4(p + 4 * h, o + 4 * h);
+    };
+    auto stc = [&](float *p, const float *o) {
+#pragma unroll
+        for (int h = 0; h < CPT / 4; h++) st4(p + 4 * h, o + 4 * h);
+    };
     // march-face flux at the thread's cells from the upwind stencil rows
     // x1, x2, x3 (GKUA_Residual.f90:155-185 with the mirrored inputs of a
     // negative speed)
     auto march_flux = [&](const float *x1, const float *x2, const float *x3, float *FG, float *FH) {
 #pragma unroll
         for (int r = 0; r < 2; r++) {
-            float a[4], m[4], c[4];
-            ld4(x1 + r * RS + pa0, a);
-            ld4(x2 + r * RS + pa0, m);
-            ld4(x3 + r * RS + pa0, c);
+            float a[CPT], m[CPT], c[CPT];
+            ldc(x1 + r * RS + pa0, a);
+            ldc(x2 + r * RS + pa0, m);
+            ldc(x3 + r * RS + pa0, c);
             float *F = r ? FH : FG;
 #pragma unroll
-            for (int p = 0; p < 2; p++) {
+            for (int p = 0; p < CPT / 2; p++) {
                 const float2 mp = pk(m, p);
                 upk(mul2(pk(sB), fma2(pk(0.5f), mm2(sub2(pk(c, p), mp), sub2(mp, pk(a, p))), mp)), F, p);
             }
@@ -181,7 +202,7 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
         for (int r = 0; r < 2; r++) {
             float *F = r ? FH : FG;
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
+            for (int k = 0; k < CPT; k++) {
                 const int o = r * RS + pa0 + k;
                 if (q == 1) F[k] = sB * A.fw_blo[((size_t)v * 2 + r) * PA + pa0 + k];
                 else if (q == Nb + 1) F[k] = sB * A.fw_bhi[((size_t)v * 2 + r) * PA + pa0 + k];
@@ -208,9 +229,10 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
     // block, so a row is PA / 128 whole blocks (8 * PA values)
     const float *epr = A.eqp + hyb_eqp_at((size_t)pa0, 0);
     const size_t ep_row = (size_t)8 * PA;
-    // line `lane` of the warp's block in the next row (the block starts
-    // 4 * lane values before this thread's parameters)
-    const size_t ep_pf = ep_row + (size_t)28 * lane;
+    // the next row's lines of the warp's blocks, CPT / 4 per lane: thread j
+    // of a block (j = (pa0 % 128) / CPT) starts CPT * j values into it and
+    // takes its lines j * CPT / 4 .. (j + 1) * CPT / 4 - 1 (32 values each)
+    const size_t ep_pf = ep_row + (size_t)7 * CPT * ((pa0 & (HYB_EQP_BLK - 1)) / CPT);
     float *fst = A.f + vrow0 + pa0;                      // row 1 of the update
     float *rst = A.rhs ? A.rhs + vrow0 + pa0 : nullptr;  // row 1 of the RHS store
 
@@ -241,29 +263,29 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
         float P = 1.f, CGt = 0.f, CHt = 0.f;
         if (act) {
             const float *rm = rowp(b - 1), *r0 = rowp(b), *rp = rowp(b + 1), *rq = rowp(b + 2);
-            // window f(a0-2 .. a0+5) of both components
-            float wG[8], wH[8];
+            // window f(a0-2 .. a0+CPT+1) of both components
+            float wG[CPT + 4], wH[CPT + 4];
             {
                 const float2 lg = *reinterpret_cast<const float2 *>(r0 + pa0 - 2);
-                const float2 hg = *reinterpret_cast<const float2 *>(r0 + pa0 + 4);
+                const float2 hg = *reinterpret_cast<const float2 *>(r0 + pa0 + CPT);
                 const float2 lh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 - 2);
-                const float2 hh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 + 4);
-                wG[0] = lg.x; wG[1] = lg.y; wG[6] = hg.x; wG[7] = hg.y;
-                wH[0] = lh.x; wH[1] = lh.y; wH[6] = hh.x; wH[7] = hh.y;
-                ld4(r0 + pa0, wG + 2);
-                ld4(r0 + RS + pa0, wH + 2);
+                const float2 hh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 + CPT);
+                wG[0] = lg.x; wG[1] = lg.y; wG[CPT + 2] = hg.x; wG[CPT + 3] = hg.y;
+                wH[0] = lh.x; wH[1] = lh.y; wH[CPT + 2] = hh.x; wH[CPT + 3] = hh.y;
+                ldc(r0 + pa0, wG + 2);
+                ldc(r0 + RS + pa0, wH + 2);
             }
-            // scan-face fluxes through faces a0 .. a0+4 (window cells m+1 | m+2)
+            // scan-face fluxes through faces a0 .. a0+CPT (window cells m+1 | m+2)
             float FA_G[CPT + 1], FA_H[CPT + 1];
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const float *w = r ? wH : wG;
                 float *F = r ? FA_H : FA_G;
-                float D[7], val[7];
+                float D[CPT + 3], val[CPT + 3];
 #pragma unroll
-                for (int k = 0; k < 7; k++) D[k] = w[k + 1] - w[k];
+                for (int k = 0; k < CPT + 3; k++) D[k] = w[k + 1] - w[k];
 #pragma unroll
-                for (int k = 1; k < 7; k++) val[k] = w[k] + hA * mmed(D[k], D[k - 1]);
+                for (int k = 1; k < CPT + 3; k++) val[k] = w[k] + hA * mmed(D[k], D[k - 1]);
 #pragma unroll
                 for (int m = 0; m <= CPT; m++) F[m] = sA * (upA ? val[m + 1] : val[m + 2]);
             }
@@ -277,26 +299,29 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
                     FA_H[1] = flux_wlo<HYB_SCHEME_NND>(sA, wH[2], wH[3], wH[4]);
                 }
                 if (pa0 + CPT == Na) {
-                    FA_G[3] = flux_whi<HYB_SCHEME_NND>(sA, wG[5], wG[4], wG[3]);
-                    FA_H[3] = flux_whi<HYB_SCHEME_NND>(sA, wH[5], wH[4], wH[3]);
-                    FA_G[4] = sA * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[4] = sA * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[CPT - 1] = flux_whi<HYB_SCHEME_NND>(sA, wG[CPT + 1], wG[CPT], wG[CPT - 1]);
+                    FA_H[CPT - 1] = flux_whi<HYB_SCHEME_NND>(sA, wH[CPT + 1], wH[CPT], wH[CPT - 1]);
+                    FA_G[CPT] = sA * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
+                    FA_H[CPT] = sA * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
                 }
             }
             float m0[CPT], m1[CPT];
-            ld4(rm + pa0, m0);
-            ld4(rm + RS + pa0, m1);
+            ldc(rm + pa0, m0);
+            ldc(rm + RS + pa0, m1);
             // Shakhov parameters of the thread's cells
             float e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT];
-            ld4(epr + 0 * HYB_EQP_BLK, e_crt);
-            ld4(epr + 1 * HYB_EQP_BLK, e_u);
-            ld4(epr + 2 * HYB_EQP_BLK, e_v);
-            ld4(epr + 3 * HYB_EQP_BLK, e_it);
-            ld4(epr + 4 * HYB_EQP_BLK, e_ht);
-            ld4(epr + 5 * HYB_EQP_BLK, e_qx);
-            ld4(epr + 6 * HYB_EQP_BLK, e_qy);
-            ld4(epr + 7 * HYB_EQP_BLK, e_cf);
-            if (b < Nb) asm volatile("prefetch.global.L1 [%0];" ::"l"(epr + ep_pf));
+            ldc(epr + 0 * HYB_EQP_BLK, e_crt);
+            ldc(epr + 1 * HYB_EQP_BLK, e_u);
+            ldc(epr + 2 * HYB_EQP_BLK, e_v);
+            ldc(epr + 3 * HYB_EQP_BLK, e_it);
+            ldc(epr + 4 * HYB_EQP_BLK, e_ht);
+            ldc(epr + 5 * HYB_EQP_BLK, e_qx);
+            ldc(epr + 6 * HYB_EQP_BLK, e_qy);
+            ldc(epr + 7 * HYB_EQP_BLK, e_cf);
+            if (b < Nb) {
+#pragma unroll
+                for (int i = 0; i < CPT / 4; i++) asm volatile("prefetch.global.L1 [%0];" ::"l"(epr + ep_pf + 32 * i));
+            }
             // march faces b+1
             if (PERB || (b >= 2 && b <= Nb - 2)) march_flux(upB ? rm : rq, upB ? r0 : rp, upB ? rp : r0, FBh_G, FBh_H);
             else march_wall(b + 1, FBh_G, FBh_H);
@@ -308,7 +333,7 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
             }
             // cells in pairs (2p, 2p+1)
 #pragma unroll
-            for (int p = 0; p < 2; p++) {
+            for (int p = 0; p < CPT / 2; p++) {
                 const float2 fa0G = pk(FA_G[2 * p], FA_G[2 * p + 1]), fa1G = pk(FA_G[2 * p + 1], FA_G[2 * p + 2]);
                 const float2 fa0H = pk(FA_H[2 * p], FA_H[2 * p + 1]), fa1H = pk(FA_H[2 * p + 1], FA_H[2 * p + 2]);
                 float2 divG, divH;
@@ -347,8 +372,8 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
                 P = pc[k] * P;
             }
             if (rst) {
-                st4(rst, rG);
-                st4(rst + rstride, rH);
+                stc(rst, rG);
+                stc(rst + rstride, rH);
             }
         } else {
 #pragma unroll
@@ -418,10 +443,14 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
                 const float *dlp = dlf + (size_t)((b - 1) & 1) * 2 * TPV;
                 const bool has_next = (pa0 + CPT < Na);
                 const float lastG = has_next ? dlp[t + 1] : 0.f, lastH = has_next ? dlp[TPV + t + 1] : 0.f;
-                float uG[CPT], uH[CPT];
-                const float nxG[CPT] = {dG[1], dG[2], dG[3], lastG}, nxH[CPT] = {dH[1], dH[2], dH[3], lastH};
+                float uG[CPT], uH[CPT], nxG[CPT], nxH[CPT];
 #pragma unroll
-                for (int p = 0; p < 2; p++) {
+                for (int k = 0; k < CPT; k++) {
+                    nxG[k] = k + 1 < CPT ? dG[k + 1] : lastG;
+                    nxH[k] = k + 1 < CPT ? dH[k + 1] : lastH;
+                }
+#pragma unroll
+                for (int p = 0; p < CPT / 2; p++) {
                     const float2 ip = pk(iap, p);
                     const float2 g2 = mul2(pk(msc), add2(pk(fo0, p), fma2(fma2(pk(cA), pk(nxG, p), mul2(pk(cB), pk(nG, p))),
                                                                           ip, pk(dG, p))));
@@ -432,8 +461,8 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
                     uH[2 * p] = h2.x < fl ? fl : h2.x;
                     uH[2 * p + 1] = h2.y < fl ? fl : h2.y;
                 }
-                st4(fst, uG);
-                st4(fst + rstride, uH);
+                stc(fst, uG);
+                stc(fst + rstride, uH);
             }
             fst += PA;
         }
@@ -452,8 +481,8 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
         const bool has_next = (pa0 + CPT < Na);
         const float *o0 = rowp(Nb);
         float f0[CPT], f1[CPT], uG[CPT], uH[CPT];
-        ld4(o0 + pa0, f0);
-        ld4(o0 + RS + pa0, f1);
+        ldc(o0 + pa0, f0);
+        ldc(o0 + RS + pa0, f1);
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
             const float nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : 0.f);
@@ -463,58 +492,61 @@ __device__ __forceinline__ void sweep_nnd4(const KinArgs<float> &A, int vblk) {
             uG[k] = fg < fl ? fl : fg;
             uH[k] = fh < fl ? fl : fh;
         }
-        st4(fst, uG);
-        st4(fst + rstride, uH);
+        stc(fst, uG);
+        stc(fst + rstride, uH);
     }
     // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
     // for above, so no copy is in flight when the CTA exits
 }
 
-template <bool PERA, bool PERB, bool SJ>
-__global__ void __launch_bounds__(256, 2) k_sweep_nnd4(KinArgs<float> A) {
-    sweep_nnd4<PERA, PERB, SJ>(A, blockIdx.x);
+// 4 cells per thread, CTAs of up to 256 threads, 128 registers.  8 cells
+// per thread compiles (the body is written for either) but measured slower
+// on the 128x512 x 64^2 Couette case, 1.86 against 1.60 ms: twice the
+// per-cell state leaves 10 warps per SM.  Only 4 is instantiated.
+template <int CPT, bool PERA, bool PERB, bool SJ>
+__global__ void __launch_bounds__(256, 2) k_sweep_nnd(KinArgs<float> A) {
+    sweep_nnd<CPT, PERA, PERB, SJ>(A, blockIdx.x);
 }
 
-template <bool PERA, bool PERB, bool SJ>
-int sweep_nnd4_launch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
-    const int tpv = ctx->PA / 4;
-    const size_t smem = sweep_group_bytes<float>(ctx->PA, tpv) * vpb;
+template <int CPT, bool PERA, bool PERB, bool SJ>
+int sweep_nnd_launch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
+    const int tpv = ctx->PA / CPT;
+    const size_t smem = nnd_group_bytes(ctx->PA, tpv) * vpb;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_sweep_nnd4<PERA, PERB, SJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_sweep_nnd<CPT, PERA, PERB, SJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr = true;
     }
     if (!launch) return HYB_OK;
     dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
-    k_sweep_nnd4<PERA, PERB, SJ><<<grd, blk, smem, ctx->stream>>>(A);
+    k_sweep_nnd<CPT, PERA, PERB, SJ><<<grd, blk, smem, ctx->stream>>>(A);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
-        ctx->last_error = std::string("k_sweep_nnd4: ") + cudaGetErrorString(e);
+        ctx->last_error = std::string("k_sweep_nnd: ") + cudaGetErrorString(e);
         return HYB_ERR_CUDA;
     }
     return HYB_OK;
 }
 
-// the specialised sweep covers FP32, uniform meshes, the reference order, NND
-// and 4 cells per thread; returns false when the context is outside that
-inline bool sweep_nnd4_applies(const hyb_ctx *ctx, const KinArgs<float> &A, int cpt) {
-    return cpt == 4 && ctx->uniform && ctx->prm.sweep_order == HYB_SWEEP_REFERENCE && A.scheme == HYB_SCHEME_NND &&
-           A.Na % 4 == 0 && A.PA % HYB_EQP_BLK == 0;
-}
-
-inline int sweep_nnd4_dispatch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
+template <int CPT>
+inline int sweep_nnd_dispatch_cpt(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
     const bool pa = A.bca_lo == AX_PERIODIC, pb = A.bcb_lo == AX_PERIODIC, sj = A.scan_is_j != 0;
     if (pa) {
-        if (pb) return sj ? sweep_nnd4_launch<true, true, true>(ctx, A, vpb, launch)
-                          : sweep_nnd4_launch<true, true, false>(ctx, A, vpb, launch);
-        return sj ? sweep_nnd4_launch<true, false, true>(ctx, A, vpb, launch)
-                  : sweep_nnd4_launch<true, false, false>(ctx, A, vpb, launch);
+        if (pb) return sj ? sweep_nnd_launch<CPT, true, true, true>(ctx, A, vpb, launch)
+                          : sweep_nnd_launch<CPT, true, true, false>(ctx, A, vpb, launch);
+        return sj ? sweep_nnd_launch<CPT, true, false, true>(ctx, A, vpb, launch)
+                  : sweep_nnd_launch<CPT, true, false, false>(ctx, A, vpb, launch);
     }
-    if (pb) return sj ? sweep_nnd4_launch<false, true, true>(ctx, A, vpb, launch)
-                      : sweep_nnd4_launch<false, true, false>(ctx, A, vpb, launch);
-    return sj ? sweep_nnd4_launch<false, false, true>(ctx, A, vpb, launch)
-              : sweep_nnd4_launch<false, false, false>(ctx, A, vpb, launch);
+    if (pb) return sj ? sweep_nnd_launch<CPT, false, true, true>(ctx, A, vpb, launch)
+                      : sweep_nnd_launch<CPT, false, true, false>(ctx, A, vpb, launch);
+    return sj ? sweep_nnd_launch<CPT, false, false, true>(ctx, A, vpb, launch)
+              : sweep_nnd_launch<CPT, false, false, false>(ctx, A, vpb, launch);
+}
+
+// the specialised sweep (sweep_nnd_ok(ctx, 4) holds)
+inline int sweep_nnd_dispatch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
+    return sweep_nnd_dispatch_cpt<4>(ctx, A, vpb, launch);
 }
 
 }  // namespace hyb

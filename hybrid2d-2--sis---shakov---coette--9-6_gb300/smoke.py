@@ -35,6 +35,22 @@ def run():
     g.close()
     if not (abs(rm["max_rms"] - ro["max_rms"]) < 1e-3 * ro["max_rms"]):
         raise AssertionError("mixed-precision residual far from the FP64 oracle")
+    # a 128-cell scan axis: the specialised FP32 sweep (k_sweep_nnd4) and the
+    # packed FP32 moment pass (k_moments_f2), as on the large workloads
+    c = cases.couette_small(name="couette-4x128-nv8-kn0.1", ncy=128, nvx=8, nvy=8, dt=0.05)
+    g = abi.Solver(c, precision=1)
+    g.init_maxwellian()
+    rm = g.step(2)
+    o = O.Oracle(c, threads=0)
+    o.init_maxwellian()
+    ro = o.step(2)
+    fg = g.download_f().reshape(c.nv, c.ny + 7, c.nx + 7, 2)[:, 4:4 + c.ny - 1, 4:4 + c.nx - 1]
+    fo = o.frd().reshape(c.nv, c.ny + 7, c.nx + 7, 2)[:, 4:4 + c.ny - 1, 4:4 + c.nx - 1]
+    g.close()
+    err = float(np.abs(fg - fo).max() / np.abs(fo).max())
+    print(f"smoke: {c.name} mixed 2 steps on cuda:0: max rel f err {err:.2e} (FP32 distribution)")
+    if not (err < 5e-5 and abs(rm["max_rms"] - ro["max_rms"]) < 1e-3 * ro["max_rms"]):
+        raise AssertionError(f"mixed-precision GPU result far from the FP64 oracle: f {err:.3e}")
 
 
 if __name__ == "__main__":

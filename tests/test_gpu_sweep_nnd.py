@@ -1,4 +1,4 @@
-"""The specialised FP32 sweep (k_sweep_nnd4: uniform mesh, reference order,
+"""The specialised FP32 sweep (k_sweep_nnd: uniform mesh, reference order,
 NND, four scan cells per thread) on every combination of periodic and wall
 scan and march axes, in both axis roles.
 
@@ -30,15 +30,15 @@ def mods(pkg):
     return abi, cases, T
 
 
-def _case(cases, T, pera, perb, sj, **kw):
-    """A 128-cell scan axis (4 cells per thread) of the given boundary kinds;
-    the scan axis is y when sj, else x."""
+def _case(cases, T, pera, perb, sj, na=128, **kw):
+    """A scan axis of na cells (4 cells per thread) of the given boundary
+    kinds; the scan axis is y when sj, else x."""
     P, W = T.HYB_BC_PERIODIC, T.HYB_BC_WALL
     ka, kb = (P if pera else W), (P if perb else W)
     if sj:
-        d = dict(ncx=12, ncy=128, bcs=(kb, ka, kb, ka))
+        d = dict(ncx=12, ncy=na, bcs=(kb, ka, kb, ka))
     else:
-        d = dict(ncx=128, ncy=12, bcs=(ka, kb, ka, kb))
+        d = dict(ncx=na, ncy=12, bcs=(ka, kb, ka, kb))
     d.update(nvx=8, nvy=8, dt=0.05, precision=T.HYB_PREC_MIXED)
     d.update(kw)
     return cases.couette_small(**d)
@@ -49,10 +49,11 @@ def _perturbed(f, seed):
     return f * (1.0 + 0.2 * (rng.random(f.shape) - 0.5))
 
 
+@pytest.mark.parametrize("na", [128, 256])
 @pytest.mark.parametrize("pera,perb,sj", list(itertools.product([False, True], repeat=3)))
-def test_nnd4_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, sj):
+def test_nnd_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, sj, na):
     abi, cases, T = mods
-    c = _case(cases, T, pera, perb, sj)
+    c = _case(cases, T, pera, perb, sj, na=na)
     g = abi.Solver(c, precision=T.HYB_PREC_MIXED)
     g.init_maxwellian()
     g.upload_f(_perturbed(g.download_f(), 11))
@@ -78,7 +79,7 @@ def test_nnd4_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, s
         assert _rel(Sg[..., k], So[..., k]) < MIXED_TOL or np.abs(Sg[..., k] - So[..., k]).max() < MIXED_TOL, k
 
 
-def test_nnd4_rhs_only_pass_matches_generic_kernel(mods, monkeypatch):
+def test_nnd_rhs_only_pass_matches_generic_kernel(mods, monkeypatch):
     """The RHS-only pass of the synthetic solve (f left unchanged) and the
     RHS store of the last iteration run through the same kernel."""
     abi, cases, T = mods
