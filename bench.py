@@ -35,9 +35,9 @@ from hyb_gb300 import abi, cases  # noqa: E402
 
 METRIC = "cell-velocity updates/s (plain kinetic iteration)"
 # what the mixed path computes in which type
-PREC_MIXED = ("fp32 f, fluxes, equilibrium and sweeps; moments: fp32 products summed in fp32 over blocks of 8 "
-              "velocities, the blocks Kahan-compensated in fp32, velocity slices folded in float-float, the "
-              "primitive conversion and residual in fp64")
+PREC_MIXED = ("fp32 f, fluxes, equilibrium and sweeps; moments: fp32 products summed in fp32 over blocks of 16 "
+              "velocities (8 on rows the packed pass does not take), the blocks Kahan-compensated in fp32, "
+              "velocity slices folded in float-float, the primitive conversion and residual in fp64")
 UNIT = "cell*velocity updates/s"
 
 
@@ -190,6 +190,36 @@ def dist_barrier(world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+class PinnedArray:
+    """A float64 host array in page-locked memory (cudaHostAlloc through the
+    CUDA runtime the library already loaded): the end-to-end leg reads the
+    step's results into it, as a host that keeps its output fields pinned."""
+
+    def __init__(self, n):
+        import ctypes as C
+        self.rt = None
+        for name in ("libcudart.so.13", "libcudart.so"):
+            try:
+                self.rt = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if self.rt is None:
+            raise RuntimeError("CUDA runtime library not found")
+        self.rt.cudaHostAlloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint]
+        self.rt.cudaFreeHost.argtypes = [C.c_void_p]
+        self.p = C.c_void_p()
+        if self.rt.cudaHostAlloc(C.byref(self.p), n * 8, 0) != 0:
+            raise RuntimeError("cudaHostAlloc failed")
+        self.a = np.ctypeslib.as_array((C.c_double * n).from_address(self.p.value))
+
+    def free(self):
+        if self.p:
+            self.a = None
+            self.rt.cudaFreeHost(self.p)
+            self.p = None
 
 
 def dist_max(world, x):
@@ -374,8 +404,8 @@ def run_gb300(args, world, rank, local):
             traffic = t.get("bytes_per_launch")
     # ---- end to end through the C ABI with host buffers ------------------------
     u, v, t = case.walls()
-    S_host = np.zeros(11 * (case.nx + 7) * (case.ny + 7))
-    cf_host = np.zeros((case.nx + 3) * (case.ny + 3))
+    S_pin, cf_pin = PinnedArray(11 * (case.nx + 7) * (case.ny + 7)), PinnedArray((case.nx + 3) * (case.ny + 3))
+    S_host, cf_host = S_pin.a, cf_pin.a
     h2d = sum(3 * 8 * len(u[f]) for f in (1, 3))
     d2h = S_host.nbytes + cf_host.nbytes + 9 * 8
     dist_barrier(world)
@@ -388,6 +418,9 @@ def run_gb300(args, world, rank, local):
                                  cf_host.ctypes.data_as(abi.C.POINTER(abi.C.c_double)))
     e2e_s = dist_max(world, time.perf_counter() - t0)
     e2e = world * units / e2e_s
+    S_host = cf_host = None
+    S_pin.free()
+    cf_pin.free()
     s.close()
     # ---- the same workload through the FP64 path ------------------------------
     fp64 = None
@@ -426,7 +459,9 @@ def run_gb300(args, world, rank, local):
                    "sweep_shape": {"cells_per_thread": shape[0], "velocities_per_cta": shape[1]},
                    "l2": "inputs larger than L2 (f is %.2f GB)" % (case.cells * case.nv * 2 * rs / 1e9)},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "calls": "hyb_set_walls x2 + hyb_step(1, residual) + hyb_download_moments per step"},
+                "calls": "hyb_set_walls x2 + hyb_step(1, residual) + hyb_download_moments per step",
+                "host_buffers": "moments and CF read into page-locked host arrays; wall data staged by the "
+                                "library through its page-locked buffer"},
         "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "alg_bytes_per_cell_velocity": b_alg,

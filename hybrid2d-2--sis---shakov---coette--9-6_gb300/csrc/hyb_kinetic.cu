@@ -462,8 +462,9 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
 
 // ---- FP32 moment pass, two cells per thread, packed pairs -------------------
 // The DETFP moments (NM = 10) or moments 1-4 of a stored RHS (NM = 4) of FP32
-// distributions.  Same ring, slices, block sums and Kahan sums as
-// moments_body; the arithmetic differs in form only:
+// distributions.  Same ring and slices as moments_body, plain FP32 sums over
+// blocks of 16 velocities (8 there) added into Kahan sums; the arithmetic
+// differs in form only:
 // * the weight of each moment per velocity (w, w vx, w vy, vx^2 + vy^2,
 //   w vx^2, w vy^2, w vx vy) is formed once per CTA and stored twice over, so
 //   that a packed FP32 pair reads it from shared memory as a register pair;
@@ -473,7 +474,8 @@ __device__ __forceinline__ void moments_body(const MomArgs &M, int bidx, int sli
 // The Kahan terms stay in registers: at 80 registers (three CTAs per SM) a
 // few of them spill around the block flushes, which measured faster than
 // keeping the compensations in shared memory (0.54 against 0.75 ms on the
-// 128x512 x 64^2 Couette case).
+// 128x512 x 64^2 Couette case); flushing every 16 velocities instead of 8
+// halves that spill traffic (0.544 -> 0.518 ms).
 constexpr int MOMF2_COEF = 16;   // floats per velocity in the weight table
 
 __host__ __device__ inline size_t mom_f2_coef_bytes(int nloc_max) {
@@ -491,7 +493,7 @@ template <int NM>
 __device__ __forceinline__ void moments_body_f2(const MomArgs &M, int bidx, int slice) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int VPS = MomVps<float>::v;
-    constexpr int FLUSH = 8 / VPS;                  // slots per block of 8 velocities
+    constexpr int FLUSH = 16 / VPS;                  // slots per block of 16 velocities
     const int PA = M.PA, t = threadIdx.x, TPV = blockDim.x;
     const int b = bidx + 1;
     const int a0 = t * 2 + 1;
@@ -540,7 +542,7 @@ __device__ __forceinline__ void moments_body_f2(const MomArgs &M, int bidx, int 
     int issued = 0;   // slots issued (thread 0)
     if (t == 0)
         for (; issued < MOM_NST - 1 && issued < nslot; issued++) issue(issued);
-    // plain sums over blocks of 8 velocities, Kahan sums of the blocks
+    // plain sums over blocks of 16 velocities, Kahan sums of the blocks
     float2 blk[NM], ks[NM], kc[NM];
 #pragma unroll
     for (int q = 0; q < NM; q++) blk[q] = ks[q] = kc[q] = make_float2(0.f, 0.f);
