@@ -79,6 +79,33 @@ def test_nnd_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, sj
         assert _rel(Sg[..., k], So[..., k]) < MIXED_TOL or np.abs(Sg[..., k] - So[..., k]).max() < MIXED_TOL, k
 
 
+@pytest.mark.parametrize("pera,perb", [(False, True), (True, False)])
+def test_nnd_widest_rows_match_generic_kernel_and_oracle(mods, monkeypatch, pera, perb):
+    """A 1024-cell scan axis: 256 threads and 8 warps per velocity, so the
+    cross-warp carry of the scan runs over up to 7 warp aggregates."""
+    abi, cases, T = mods
+    c = _case(cases, T, pera, perb, True, na=1024, nvx=4, nvy=4)
+    c.ncx = 6
+    g = abi.Solver(c, precision=T.HYB_PREC_MIXED)
+    g.init_maxwellian()
+    g.upload_f(_perturbed(g.download_f(), 5))
+    f0 = g.download_f()
+    monkeypatch.setenv("HYB_SWEEP_GENERIC", "1")
+    h = abi.Solver(c, precision=T.HYB_PREC_MIXED)
+    monkeypatch.delenv("HYB_SWEEP_GENERIC")
+    h.upload_f(f0)
+    o = O.Oracle(c, threads=0)
+    o.upload_f(f0)
+    for _ in range(2):
+        g.step(1)
+        h.step(1)
+        o.step(1)
+    fg, fh = g.download_f(), h.download_f()
+    assert np.abs(fg - fh).max() <= TWIN_TOL * np.abs(fh).max()
+    fi, fo = _interior_f(c, fg), _interior_f(c, o.frd())
+    assert _rel(fi, fo) < MIXED_TOL, _rel(fi, fo)
+
+
 def test_nnd_rhs_only_pass_matches_generic_kernel(mods, monkeypatch):
     """The RHS-only pass of the synthetic solve (f left unchanged) and the
     RHS store of the last iteration run through the same kernel."""
