@@ -69,6 +69,25 @@ template <typename real> __device__ __forceinline__ real fminmd(real x, real y) 
     const real t = copysign(real(1), x) * y;
     return copysign(fmax(real(0), fmin(fabs(x), t)), x);
 }
+// FP64: the same value from integer operations on the IEEE bit patterns,
+// which keeps the limiter off the FP64 pipe (2 lanes per clock per SM on
+// GB300).  Equal sign bits and a smaller magnitude field select x, else y;
+// different sign bits give 0.  A zero argument gives a zero either way.
+template <> __device__ __forceinline__ double fminmd<double>(double x, double y) {
+    const long long ix = __double_as_longlong(x), iy = __double_as_longlong(y);
+    const long long mask = 0x7fffffffffffffffLL;
+    const double m = (ix & mask) < (iy & mask) ? x : y;
+    return (ix ^ iy) >= 0 ? m : 0.0;
+}
+
+// max(v, fl) for the floor of the update, fl > 0 (GKUA_Residual.f90:104-109:
+// values below fl become fl).  FP64 compares the bit patterns as signed
+// 64-bit integers, which order every double below a positive fl (negative
+// values and -0 included) below it, off the FP64 pipe.
+template <typename real> __device__ __forceinline__ real floor_at(real v, real fl) { return v < fl ? fl : v; }
+template <> __device__ __forceinline__ double floor_at<double>(double v, double fl) {
+    return __double_as_longlong(v) < __double_as_longlong(fl) ? fl : v;
+}
 
 template <typename real> __device__ __forceinline__ real dexp(real x);
 template <> __device__ __forceinline__ float dexp<float>(float x) { return expf(x); }

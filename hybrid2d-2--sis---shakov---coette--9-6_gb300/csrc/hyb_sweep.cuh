@@ -567,8 +567,8 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
                 const real cb = -negp(sBl[k]);
                 real fg = msc * (fo0[k] + (dG[k] + (ca * nxG + cb * nG[k]) * iap[k]));
                 real fh = msc * (fo1[k] + (dH[k] + (ca * nxH + cb * nH[k]) * iap[k]));
-                uG[k] = fg < fl ? fl : fg;
-                uH[k] = fh < fl ? fl : fh;
+                uG[k] = floor_at(fg, fl);
+                uH[k] = floor_at(fh, fl);
             }
             const size_t c1 = (size_t)(prow(b - 1) - 1) * PA;
             stc(A.f + vrow0 + c1, uG);
@@ -600,8 +600,8 @@ __device__ __forceinline__ void sweep_body(const KinArgs<real> &A, int vblk) {
             const real ca = -negp(sAhp[k]);
             real fg = msc * (f0[k] + (dG[k] + (ca * nxG) * iap[k]));
             real fh = msc * (f1[k] + (dH[k] + (ca * nxH) * iap[k]));
-            uG[k] = fg < fl ? fl : fg;
-            uH[k] = fh < fl ? fl : fh;
+            uG[k] = floor_at(fg, fl);
+            uH[k] = floor_at(fh, fl);
         }
         const size_t c1 = (size_t)(prow(Nb) - 1) * PA;
         stc(A.f + vrow0 + c1, uG);
