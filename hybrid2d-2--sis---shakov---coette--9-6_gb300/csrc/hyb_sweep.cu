@@ -19,11 +19,10 @@ size_t sweep_group_bytes_f64(int PA, int tpv);
 size_t sweep_nnd_group_bytes_f32(int PA, int tpv);
 
 // the specialised FP32 NND sweep (hyb_sweep_nnd.cuh) covers this context at
-// c cells per thread: FP32, uniform mesh, reference order, NND, 4 cells per
+// c cells per thread: FP32, uniform mesh, either order, NND, 4 cells per
 // thread on the layout's 128-cell chunks
 bool sweep_nnd_ok(const hyb_ctx *ctx, int c) {
-    if (ctx->sw_generic || ctx->precision == HYB_PREC_FP64 || !ctx->uniform ||
-        ctx->prm.sweep_order != HYB_SWEEP_REFERENCE || ctx->prm.scheme != HYB_SCHEME_NND)
+    if (ctx->sw_generic || ctx->precision == HYB_PREC_FP64 || !ctx->uniform || ctx->prm.scheme != HYB_SCHEME_NND)
         return false;
     return c == 4 && ctx->cpt == 4 && ctx->Na % 4 == 0 && ctx->PA % HYB_EQP_BLK == 0;
 }

@@ -1,6 +1,7 @@
 // hyb_sweep_nnd.cuh -- the fused kinetic step (GKUA_Residual.f90:4-469) for
 // its most common form: FP32 distributions, a uniform Cartesian mesh, the
-// reference order, the NND scheme and 4 scan cells per thread.  The work
+// NND scheme and 4 scan cells per thread, in the reference order or the
+// upwind order (HYB_SWEEP_UPWIND; the mirrored frames of sweep_body).  The work
 // decomposition, the affine scan and the backward step are those of
 // sweep_body (hyb_sweep.cuh); what differs is how a row is read and how the
 // face values are formed, so that a thread spends its instructions on the
@@ -31,7 +32,12 @@
 //   aside, which cannot change a sum).  FMINMD itself is the median of its
 //   arguments and 0 (four min/max operations).
 // * Arithmetic on neighbouring cells runs as packed FP32 pairs.
-// * Periodicity of each axis and the axis roles are template parameters.
+// * Periodicity of each axis, the axis roles and the order are template
+//   parameters.  In the upwind order a velocity whose scan (march) face speed
+//   is negative works in the frame mirrored along that axis: logical cell k
+//   of a thread's chunk is physical cell pp0 + CPT-1-k, logical row b is
+//   physical row Nb+1-b, and the wall slots of the two ends swap.  Loads and
+//   stores reverse the chunk; the row pointers step backwards.
 #pragma once
 #include "hyb_sweep.cuh"
 
@@ -69,7 +75,7 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 __device__ __forceinline__ float mmed(float x, float y) { return fmaxf(fminf(x, y), fminf(fmaxf(x, y), 0.f)); }
 __device__ __forceinline__ float2 mm2(float2 x, float2 y) { return make_float2(mmed(x.x, y.x), mmed(x.y, y.y)); }
 
-template <int CPT, bool PERA, bool PERB, bool SJ>
+template <int CPT, bool PERA, bool PERB, bool SJ, bool UPW>
 __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
     static_assert(CPT == 4 || CPT == 8, "4 or 8 cells per thread");
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -99,11 +105,20 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
     // ---- velocity and face speeds (uniform mesh) --------------------------------
     const int iv = vok ? v % A.nvi : 0, jv = vok ? v / A.nvi : 0;
     const float vx = vok ? (float)A.vx[iv] : 0.f, vy = vok ? (float)A.vy[jv] : 0.f;
-    const float sA = vx * A.gA1[0] + vy * A.gA2[0];
-    const float sB = vx * A.gB1[0] + vy * A.gB2[0];
+    float sA = vx * A.gA1[0] + vy * A.gA2[0];
+    float sB = vx * A.gB1[0] + vy * A.gB2[0];
     const float vol = A.vol[0];
     const float ivol = 1.f / vol;
     const float abase = vol / A.dt + (posp(sA) - negp(sA) + posp(sB) - negp(sB));
+    // mirrored scan / march axis of this velocity (upwind order only)
+    const bool ra = UPW && sA < 0.f, rb = UPW && sB < 0.f;
+    if (ra) sA = -sA;
+    if (rb) sB = -sB;
+    // first physical cell of the thread's chunk; physical row of logical row b
+    const int pp0 = !act ? 0 : ra ? Na - pa0 - CPT : pa0;
+    auto prow = [&](int b) -> int { return rb ? Nb + 1 - b : b; };
+    const float *fw_alo = ra ? A.fw_ahi : A.fw_alo, *fw_ahi = ra ? A.fw_alo : A.fw_ahi;
+    const float *fw_blo = rb ? A.fw_bhi : A.fw_blo, *fw_bhi = rb ? A.fw_blo : A.fw_bhi;
     const bool upA = sA > 0.f, upB = sB > 0.f;
     const float hA = upA ? 0.5f : -0.5f;
     const float pA = posp(sA), pB = posp(sB);
@@ -111,8 +126,8 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
 
     // ---- staged rows ---------------------------------------------------------
     auto phys_row = [&](int bp) -> int {
-        if (bp >= 1 && bp <= Nb) return bp;
-        if (PERB && bp <= 0) return bp + Nb;
+        if (bp >= 1 && bp <= Nb) return prow(bp);
+        if (PERB && bp <= 0) return prow(bp + Nb);
         return 0;
     };
     // f row pr (1..Nb) into a staged row whose cell 0 is at dst
@@ -145,7 +160,7 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
     if (producer) {
         for (int bp = -1; bp <= RING - 3; bp++) issue_row(bp);
         if (PERB)
-            for (int w = 0; w < 2; w++) copy_row(wrap + (size_t)w * 2 * RS + NND_PAD, w + 1, &bars[RING + w]);
+            for (int w = 0; w < 2; w++) copy_row(wrap + (size_t)w * 2 * RS + NND_PAD, prow(w + 1), &bars[RING + w]);
     }
     // cell 0 of the G row of logical row bp (H is RS further)
     auto rowp = [&](int bp) -> const float * {
@@ -173,9 +188,29 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
 #pragma unroll
         for (int h = 0; h < CPT / 4; h++) ld4(p + 4 * h, o + 4 * h);
     };
-    auto stc = [&](float *p, const float *o) {
+    // the thread's chunk starting at p (its first physical cell) in logical
+    // order, and back
+    auto ldl = [&](const float *p, float *o) {
+        if (!ra) {
+            ldc(p, o);
+        } else {
+            float q[CPT];
+            ldc(p, q);
 #pragma unroll
-        for (int h = 0; h < CPT / 4; h++) st4(p + 4 * h, o + 4 * h);
+            for (int k = 0; k < CPT; k++) o[k] = q[CPT - 1 - k];
+        }
+    };
+    auto stl = [&](float *p, const float *o) {
+        if (!ra) {
+#pragma unroll
+            for (int h = 0; h < CPT / 4; h++) st4(p + 4 * h, o + 4 * h);
+        } else {
+            float q[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) q[k] = o[CPT - 1 - k];
+#pragma unroll
+            for (int h = 0; h < CPT / 4; h++) st4(p + 4 * h, q + 4 * h);
+        }
     };
     // march-face flux at the thread's cells from the upwind stencil rows
     // x1, x2, x3 (GKUA_Residual.f90:155-185 with the mirrored inputs of a
@@ -184,9 +219,9 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             float a[CPT], m[CPT], c[CPT];
-            ldc(x1 + r * RS + pa0, a);
-            ldc(x2 + r * RS + pa0, m);
-            ldc(x3 + r * RS + pa0, c);
+            ldl(x1 + r * RS + pp0, a);
+            ldl(x2 + r * RS + pp0, m);
+            ldl(x3 + r * RS + pp0, c);
             float *F = r ? FH : FG;
 #pragma unroll
             for (int p = 0; p < CPT / 2; p++) {
@@ -203,9 +238,10 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
             float *F = r ? FH : FG;
 #pragma unroll
             for (int k = 0; k < CPT; k++) {
-                const int o = r * RS + pa0 + k;
-                if (q == 1) F[k] = sB * A.fw_blo[((size_t)v * 2 + r) * PA + pa0 + k];
-                else if (q == Nb + 1) F[k] = sB * A.fw_bhi[((size_t)v * 2 + r) * PA + pa0 + k];
+                const int pc = pp0 + (ra ? CPT - 1 - k : k);      // physical cell of logical cell k
+                const int o = r * RS + pc;
+                if (q == 1) F[k] = sB * fw_blo[((size_t)v * 2 + r) * PA + pc];
+                else if (q == Nb + 1) F[k] = sB * fw_bhi[((size_t)v * 2 + r) * PA + pc];
                 else if (q == 2) F[k] = flux_wlo<HYB_SCHEME_NND>(sB, rowp(1)[o], rowp(2)[o], rowp(3)[o]);
                 else if (q == Nb) F[k] = flux_whi<HYB_SCHEME_NND>(sB, rowp(Nb)[o], rowp(Nb - 1)[o], rowp(Nb - 2)[o]);
                 else F[k] = flux_std<HYB_SCHEME_NND>(sB, rowp(q - 2)[o], rowp(q - 1)[o], rowp(q)[o], rowp(q + 1)[o]);
@@ -225,16 +261,16 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
     }
     const float fl = Consts<float>::floor_();
     const float msc = A.mscale ? (float)*A.mscale : 1.f;
-    // this thread's parameters in row 1: PA is a multiple of the 128-cell
-    // block, so a row is PA / 128 whole blocks (8 * PA values)
-    const float *epr = A.eqp + hyb_eqp_at((size_t)pa0, 0);
-    const size_t ep_row = (size_t)8 * PA;
-    // the next row's lines of the warp's blocks, CPT / 4 per lane: thread j
-    // of a block (j = (pa0 % 128) / CPT) starts CPT * j values into it and
-    // takes its lines j * CPT / 4 .. (j + 1) * CPT / 4 - 1 (32 values each)
-    const size_t ep_pf = ep_row + (size_t)7 * CPT * ((pa0 & (HYB_EQP_BLK - 1)) / CPT);
-    float *fst = A.f + vrow0 + pa0;                      // row 1 of the update
-    float *rst = A.rhs ? A.rhs + vrow0 + pa0 : nullptr;  // row 1 of the RHS store
+    // this thread's parameters in logical row 1: PA is a multiple of the
+    // 128-cell block, so a row is PA / 128 whole blocks (8 * PA values)
+    const float *epr = A.eqp + hyb_eqp_at((size_t)(prow(1) - 1) * PA + pp0, 0);
+    const ptrdiff_t ep_row = rb ? -(ptrdiff_t)8 * PA : (ptrdiff_t)8 * PA;
+    // the next row's parameter lines: the 8 chunks of a 32-cell group take
+    // one parameter's 128-byte line each
+    const ptrdiff_t ep_pf = ep_row + (ptrdiff_t)((pp0 >> 2) & 7) * HYB_EQP_BLK;
+    const ptrdiff_t row_step = rb ? -(ptrdiff_t)PA : (ptrdiff_t)PA;
+    float *fst = A.f + vrow0 + (size_t)(prow(1) - 1) * PA + pp0;                      // logical row 1
+    float *rst = A.rhs ? A.rhs + vrow0 + (size_t)(prow(1) - 1) * PA + pp0 : nullptr;
 
     for (int bp = -1; bp <= 2; bp++) wait_row(bp);
     // the copies of rows 1, 2 for rows Nb+1, Nb+2 read f rows that the
@@ -266,14 +302,21 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
             // window f(a0-2 .. a0+CPT+1) of both components
             float wG[CPT + 4], wH[CPT + 4];
             {
-                const float2 lg = *reinterpret_cast<const float2 *>(r0 + pa0 - 2);
-                const float2 hg = *reinterpret_cast<const float2 *>(r0 + pa0 + CPT);
-                const float2 lh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 - 2);
-                const float2 hh = *reinterpret_cast<const float2 *>(r0 + RS + pa0 + CPT);
-                wG[0] = lg.x; wG[1] = lg.y; wG[CPT + 2] = hg.x; wG[CPT + 3] = hg.y;
-                wH[0] = lh.x; wH[1] = lh.y; wH[CPT + 2] = hh.x; wH[CPT + 3] = hh.y;
-                ldc(r0 + pa0, wG + 2);
-                ldc(r0 + RS + pa0, wH + 2);
+                // physical window pp0-2 .. pp0+CPT+1, reversed in a mirrored frame
+                const float2 lg = *reinterpret_cast<const float2 *>(r0 + pp0 - 2);
+                const float2 hg = *reinterpret_cast<const float2 *>(r0 + pp0 + CPT);
+                const float2 lh = *reinterpret_cast<const float2 *>(r0 + RS + pp0 - 2);
+                const float2 hh = *reinterpret_cast<const float2 *>(r0 + RS + pp0 + CPT);
+                float pG[CPT + 4], pH[CPT + 4];
+                pG[0] = lg.x; pG[1] = lg.y; pG[CPT + 2] = hg.x; pG[CPT + 3] = hg.y;
+                pH[0] = lh.x; pH[1] = lh.y; pH[CPT + 2] = hh.x; pH[CPT + 3] = hh.y;
+                ldc(r0 + pp0, pG + 2);
+                ldc(r0 + RS + pp0, pH + 2);
+#pragma unroll
+                for (int i = 0; i < CPT + 4; i++) {
+                    wG[i] = ra ? pG[CPT + 3 - i] : pG[i];
+                    wH[i] = ra ? pH[CPT + 3 - i] : pH[i];
+                }
             }
             // scan-face fluxes through faces a0 .. a0+CPT (window cells m+1 | m+2)
             float FA_G[CPT + 1], FA_H[CPT + 1];
@@ -293,35 +336,32 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
                 // faces 1, 2 and Na, Na+1 next to the walls of the scan axis
                 // (GKUA_Residual.f90:196-257)
                 if (pa0 == 0) {
-                    FA_G[0] = sA * A.fw_alo[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[0] = sA * A.fw_alo[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[0] = sA * fw_alo[((size_t)v * 2 + 0) * Nb + (prow(b) - 1)];
+                    FA_H[0] = sA * fw_alo[((size_t)v * 2 + 1) * Nb + (prow(b) - 1)];
                     FA_G[1] = flux_wlo<HYB_SCHEME_NND>(sA, wG[2], wG[3], wG[4]);
                     FA_H[1] = flux_wlo<HYB_SCHEME_NND>(sA, wH[2], wH[3], wH[4]);
                 }
                 if (pa0 + CPT == Na) {
                     FA_G[CPT - 1] = flux_whi<HYB_SCHEME_NND>(sA, wG[CPT + 1], wG[CPT], wG[CPT - 1]);
                     FA_H[CPT - 1] = flux_whi<HYB_SCHEME_NND>(sA, wH[CPT + 1], wH[CPT], wH[CPT - 1]);
-                    FA_G[CPT] = sA * A.fw_ahi[((size_t)v * 2 + 0) * Nb + (b - 1)];
-                    FA_H[CPT] = sA * A.fw_ahi[((size_t)v * 2 + 1) * Nb + (b - 1)];
+                    FA_G[CPT] = sA * fw_ahi[((size_t)v * 2 + 0) * Nb + (prow(b) - 1)];
+                    FA_H[CPT] = sA * fw_ahi[((size_t)v * 2 + 1) * Nb + (prow(b) - 1)];
                 }
             }
             float m0[CPT], m1[CPT];
-            ldc(rm + pa0, m0);
-            ldc(rm + RS + pa0, m1);
+            ldl(rm + pp0, m0);
+            ldl(rm + RS + pp0, m1);
             // Shakhov parameters of the thread's cells
             float e_crt[CPT], e_u[CPT], e_v[CPT], e_it[CPT], e_ht[CPT], e_qx[CPT], e_qy[CPT], e_cf[CPT];
-            ldc(epr + 0 * HYB_EQP_BLK, e_crt);
-            ldc(epr + 1 * HYB_EQP_BLK, e_u);
-            ldc(epr + 2 * HYB_EQP_BLK, e_v);
-            ldc(epr + 3 * HYB_EQP_BLK, e_it);
-            ldc(epr + 4 * HYB_EQP_BLK, e_ht);
-            ldc(epr + 5 * HYB_EQP_BLK, e_qx);
-            ldc(epr + 6 * HYB_EQP_BLK, e_qy);
-            ldc(epr + 7 * HYB_EQP_BLK, e_cf);
-            if (b < Nb) {
-#pragma unroll
-                for (int i = 0; i < CPT / 4; i++) asm volatile("prefetch.global.L1 [%0];" ::"l"(epr + ep_pf + 32 * i));
-            }
+            ldl(epr + 0 * HYB_EQP_BLK, e_crt);
+            ldl(epr + 1 * HYB_EQP_BLK, e_u);
+            ldl(epr + 2 * HYB_EQP_BLK, e_v);
+            ldl(epr + 3 * HYB_EQP_BLK, e_it);
+            ldl(epr + 4 * HYB_EQP_BLK, e_ht);
+            ldl(epr + 5 * HYB_EQP_BLK, e_qx);
+            ldl(epr + 6 * HYB_EQP_BLK, e_qy);
+            ldl(epr + 7 * HYB_EQP_BLK, e_cf);
+            if (b < Nb) asm volatile("prefetch.global.L1 [%0];" ::"l"(epr + ep_pf));
             // march faces b+1
             if (PERB || (b >= 2 && b <= Nb - 2)) march_flux(upB ? rm : rq, upB ? r0 : rp, upB ? rp : r0, FBh_G, FBh_H);
             else march_wall(b + 1, FBh_G, FBh_H);
@@ -372,8 +412,8 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
                 P = pc[k] * P;
             }
             if (rst) {
-                stc(rst, rG);
-                stc(rst + rstride, rH);
+                stl(rst, rG);
+                stl(rst + rstride, rH);
             }
         } else {
 #pragma unroll
@@ -381,7 +421,7 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
             P = 0.f;
         }
         epr += ep_row;
-        if (rst) rst += PA;
+        if (rst) rst += row_step;
         float Pe = 1.f, Ge = 0.f, He = 0.f;
         float *aggb = agg + (size_t)(b & 1) * nw * 3;
         if (need_scan) {
@@ -461,10 +501,10 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
                     uH[2 * p] = h2.x < fl ? fl : h2.x;
                     uH[2 * p + 1] = h2.y < fl ? fl : h2.y;
                 }
-                stc(fst, uG);
-                stc(fst + rstride, uH);
+                stl(fst, uG);
+                stl(fst + rstride, uH);
             }
-            fst += PA;
+            fst += row_step;
         }
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
@@ -481,8 +521,8 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
         const bool has_next = (pa0 + CPT < Na);
         const float *o0 = rowp(Nb);
         float f0[CPT], f1[CPT], uG[CPT], uH[CPT];
-        ldc(o0 + pa0, f0);
-        ldc(o0 + RS + pa0, f1);
+        ldl(o0 + pp0, f0);
+        ldl(o0 + RS + pp0, f1);
 #pragma unroll
         for (int k = 0; k < CPT; k++) {
             const float nxG = (k + 1 < CPT) ? dG[k + 1] : (has_next ? dlp[t + 1] : 0.f);
@@ -492,8 +532,8 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
             uG[k] = fg < fl ? fl : fg;
             uH[k] = fh < fl ? fl : fh;
         }
-        stc(fst, uG);
-        stc(fst + rstride, uH);
+        stl(fst, uG);
+        stl(fst + rstride, uH);
     }
     // every bulk copy issued (rows 1..Nb and the wrap rows) has been waited
     // for above, so no copy is in flight when the CTA exits
@@ -503,23 +543,24 @@ __device__ __forceinline__ void sweep_nnd(const KinArgs<float> &A, int vblk) {
 // per thread compiles (the body is written for either) but measured slower
 // on the 128x512 x 64^2 Couette case, 1.86 against 1.60 ms: twice the
 // per-cell state leaves 10 warps per SM.  Only 4 is instantiated.
-template <int CPT, bool PERA, bool PERB, bool SJ>
+template <int CPT, bool PERA, bool PERB, bool SJ, bool UPW>
 __global__ void __launch_bounds__(256, 2) k_sweep_nnd(KinArgs<float> A) {
-    sweep_nnd<CPT, PERA, PERB, SJ>(A, blockIdx.x);
+    sweep_nnd<CPT, PERA, PERB, SJ, UPW>(A, blockIdx.x);
 }
 
-template <int CPT, bool PERA, bool PERB, bool SJ>
+template <int CPT, bool PERA, bool PERB, bool SJ, bool UPW>
 int sweep_nnd_launch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
     const int tpv = ctx->PA / CPT;
     const size_t smem = nnd_group_bytes(ctx->PA, tpv) * vpb;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_sweep_nnd<CPT, PERA, PERB, SJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_sweep_nnd<CPT, PERA, PERB, SJ, UPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024);
         attr = true;
     }
     if (!launch) return HYB_OK;
     dim3 blk(tpv, vpb), grd((ctx->nv + vpb - 1) / vpb);
-    k_sweep_nnd<CPT, PERA, PERB, SJ><<<grd, blk, smem, ctx->stream>>>(A);
+    k_sweep_nnd<CPT, PERA, PERB, SJ, UPW><<<grd, blk, smem, ctx->stream>>>(A);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -529,24 +570,25 @@ int sweep_nnd_launch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch
     return HYB_OK;
 }
 
-template <int CPT>
+template <int CPT, bool UPW>
 inline int sweep_nnd_dispatch_cpt(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
     const bool pa = A.bca_lo == AX_PERIODIC, pb = A.bcb_lo == AX_PERIODIC, sj = A.scan_is_j != 0;
     if (pa) {
-        if (pb) return sj ? sweep_nnd_launch<CPT, true, true, true>(ctx, A, vpb, launch)
-                          : sweep_nnd_launch<CPT, true, true, false>(ctx, A, vpb, launch);
-        return sj ? sweep_nnd_launch<CPT, true, false, true>(ctx, A, vpb, launch)
-                  : sweep_nnd_launch<CPT, true, false, false>(ctx, A, vpb, launch);
+        if (pb) return sj ? sweep_nnd_launch<CPT, true, true, true, UPW>(ctx, A, vpb, launch)
+                          : sweep_nnd_launch<CPT, true, true, false, UPW>(ctx, A, vpb, launch);
+        return sj ? sweep_nnd_launch<CPT, true, false, true, UPW>(ctx, A, vpb, launch)
+                  : sweep_nnd_launch<CPT, true, false, false, UPW>(ctx, A, vpb, launch);
     }
-    if (pb) return sj ? sweep_nnd_launch<CPT, false, true, true>(ctx, A, vpb, launch)
-                      : sweep_nnd_launch<CPT, false, true, false>(ctx, A, vpb, launch);
-    return sj ? sweep_nnd_launch<CPT, false, false, true>(ctx, A, vpb, launch)
-              : sweep_nnd_launch<CPT, false, false, false>(ctx, A, vpb, launch);
+    if (pb) return sj ? sweep_nnd_launch<CPT, false, true, true, UPW>(ctx, A, vpb, launch)
+                      : sweep_nnd_launch<CPT, false, true, false, UPW>(ctx, A, vpb, launch);
+    return sj ? sweep_nnd_launch<CPT, false, false, true, UPW>(ctx, A, vpb, launch)
+              : sweep_nnd_launch<CPT, false, false, false, UPW>(ctx, A, vpb, launch);
 }
 
-// the specialised sweep (sweep_nnd_ok(ctx, 4) holds)
+// the specialised sweep (sweep_nnd_ok(ctx, 4) holds), in the context's order
 inline int sweep_nnd_dispatch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
-    return sweep_nnd_dispatch_cpt<4>(ctx, A, vpb, launch);
+    return ctx->prm.sweep_order == HYB_SWEEP_UPWIND ? sweep_nnd_dispatch_cpt<4, true>(ctx, A, vpb, launch)
+                                                    : sweep_nnd_dispatch_cpt<4, false>(ctx, A, vpb, launch);
 }
 
 }  // namespace hyb

@@ -49,11 +49,14 @@ def _perturbed(f, seed):
     return f * (1.0 + 0.2 * (rng.random(f.shape) - 0.5))
 
 
-@pytest.mark.parametrize("na", [128, 256])
+@pytest.mark.parametrize("order,na", [(0, 128), (0, 256), (1, 128)])
 @pytest.mark.parametrize("pera,perb,sj", list(itertools.product([False, True], repeat=3)))
-def test_nnd_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, sj, na):
+def test_nnd_matches_generic_kernel_and_oracle(mods, monkeypatch, pera, perb, sj, order, na):
+    """order 1: the upwind order (mirrored frames per velocity) at dt 1e6 with
+    the mass pin, as the fast-converging runs use it."""
     abi, cases, T = mods
-    c = _case(cases, T, pera, perb, sj, na=na)
+    kw = dict(sweep_order=1, mass_pin=1, dt=1.0e6) if order else {}
+    c = _case(cases, T, pera, perb, sj, na=na, **kw)
     g = abi.Solver(c, precision=T.HYB_PREC_MIXED)
     g.init_maxwellian()
     g.upload_f(_perturbed(g.download_f(), 11))
