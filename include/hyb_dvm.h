@@ -419,11 +419,12 @@ int hyb_mlp_launch_count(const hyb_mlp *m, long long *count);
  * (its predicted non-NSF t_xy, t_yy, q_x, q_y on the j-faces, in place of
  * the kinetic HoT, weighted by a local-Kn gate that ramps from 0 at
  * Kn/rho = 0.02 to 1 at 0.05: below that the NSF closure is the better
- * model and the network's error exceeds the HoT) are iterated from the kinetic state towards a steady
- * state on the band, then the moments and f are corrected to that state as
- * in the synthetic solve.  The kinetic GSIS iteration that follows converges
- * to the kinetic solution whatever the network's error, and its residual
- * judges it.  hyb_closure_samples writes the network's inputs x[n][8] and
+ * model and the network's error exceeds the HoT) are iterated from the
+ * kinetic state towards a steady state on the band, then the moments and f
+ * are corrected to that state as in the synthetic solve.  The kinetic GSIS
+ * iteration that follows converges to the kinetic solution whatever the
+ * network's error, and its residual measures that error.
+ * hyb_closure_samples writes the network's inputs x[n][8] and
  * targets y[n][4] (the Convert_NS HoT t_xy, t_yy, q_x, q_y) of every j-face,
  * n = (nx-1)*ny, face (i, j) at (j-1)*(nx-1) + i-1, for the current kinetic
  * state: training data from the solver's own runs.  With x or y NULL it
