@@ -10,13 +10,14 @@
 // * Staged rows carry 16 bytes of pad on each side.  On a periodic scan axis
 //   the producer copies the two wrapped halo cells of each end into the pads
 //   (cp.async.bulk of the 16-byte blocks at the other end), so a thread reads
-//   its window f(a0-2 .. a0+5) at fixed offsets from its own chunk: one
-//   16-byte and two 8-byte shared loads per component.
+//   its window f(a0-2 .. a0+CPT+1) at fixed offsets from its own chunk: one
+//   16-byte and two 8-byte shared loads per component at 4 cells.
 // * The Shakhov parameters of the thread's cells are read at fixed offsets
 //   from one pointer into the blocked layout (hyb_eqp_at; a warp's 128 cells
-//   are one block, each parameter a contiguous 512-byte span), which advances
-//   one row per step; each lane prefetches one 128-byte line of its warp's
-//   block of the next row into L1.
+//   are one block, each parameter a contiguous 512-byte span), which moves
+//   one row per step; the 8 chunks of each 32-cell group prefetch one
+//   parameter's 128-byte line each of the next row into L1 (without it the
+//   sweep is a fifth slower).
 // * March faces: the three rows of the upwind stencil are chosen per row by
 //   pointer (rows b-1, b, b+1 for a positive face speed, b+2, b+1, b for a
 //   negative one), so one limiter formula serves both directions with no
