@@ -367,6 +367,26 @@ def time_to_residual(tol=1e-8, large=True):
     return res
 
 
+def time_to_residual_sine():
+    """The 512x512 sine case (48^2 on [-5, 5], Kn 0.005, T_w = 1 + 0.1 sin(2 pi x),
+    plates +-0.3), mixed precision, upwind order at dt 1e6 with the mass pin:
+    the plain iteration for 1000 iterations, the synthetic solve with and
+    without the learned warm start for 150 outer iterations each (about the
+    same wall time); 1e-8 is out of reach in minutes, so these report the
+    residual each reaches and the cost of an iteration."""
+    from hyb_gb300 import hyb_types as T
+    M = T.HYB_PREC_MIXED
+    gl2 = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0, inner_rtol=1e-8,
+               relax_pct=70)
+    out = {}
+    for name, g, learned, cap, chunk in (("plain_mixed", None, False, 1000, 50), ("gsis_mixed", gl2, False, 150, 10),
+                                         ("gsis_mixed_learned", dict(gl2, mlp_warm_after=20, mlp_warm_inner=400),
+                                          True, 150, 10)):
+        c = cases.couette_sine(dt=1.0e6, sweep_order=1, mass_pin=1, precision=M)
+        out[name], _ = _ttr_run(name, c, M, g, False, learned, tol=1e-8, max_iters=cap, chunk=chunk)
+    return {"workload": "couette-512x512-nv48-kn0.005-sine, upwind order dt 1e6, mass pin", "runs": out}
+
+
 def run_gb300(args, world, rank, local):
     case = make_case(args.config)
     s = abi.Solver(case, device=local)
@@ -483,6 +503,8 @@ def run_gb300(args, world, rank, local):
         line["fp64"] = fp64
     if not args.no_ttr and rank == 0:
         line["time_to_residual"] = time_to_residual(large=not args.no_ttr_large)
+    if args.ttr_sine and rank == 0:
+        line["time_to_residual_sine"] = time_to_residual_sine()
     if not args.no_cpu:
         orc = cpu_oracle(case, os.cpu_count() or 1)
         orc[1].step(1)
@@ -592,6 +614,8 @@ def main():
     ap.add_argument("--no-ttr", action="store_true", help="skip the time-to-residual runs")
     ap.add_argument("--no-ttr-large", action="store_true", help="time to residual on the small channel only")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 throughput of the same workload")
+    ap.add_argument("--ttr-sine", action="store_true",
+                    help="add the bounded residual runs of the 512x512 sine case (about 20 s)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:
