@@ -99,6 +99,7 @@ void drop_graphs(hyb_batch *b) {
 struct Group {
     std::vector<int> members;            // instance indices
     int PA = 0, cpt = 0, vpb = 0, uni = 0, mc = 0, tpv = 0;
+    int nsig = 0;                        // sweep_nnd_signature of the members (0: generic sweep)
     size_t wall_smem = 0, mom_smem = 0;
     // offsets into the table (bytes) and launch sizes
     size_t o_wall, o_wwork, o_kin, o_kwork, o_mom, o_mwork, o_fwork, o_sg, o_swork, o_scount;
@@ -135,10 +136,11 @@ bool make_groups(hyb_batch *b, std::vector<Group> &gs) {
         if (hyb::sweep_smem_bytes(c) > (size_t)227 * 1024 - 1024) return false;
         int cpt, vpb;
         hyb::sweep_shape(c, &cpt, &vpb);
+        const int sig = c->precision == HYB_PREC_FP64 ? 0 : hyb::sweep_nnd_signature(c, cpt);
         Group *g = nullptr;
         for (Group &q : gs)
             if (q.PA == c->PA && q.cpt == cpt && q.vpb == vpb && q.uni == (c->uniform != 0) &&
-                b->inst[q.members[0]]->cpt == c->cpt)
+                b->inst[q.members[0]]->cpt == c->cpt && q.nsig == sig)
                 g = &q;
         if (!g) {
             gs.emplace_back();
@@ -147,6 +149,7 @@ bool make_groups(hyb_batch *b, std::vector<Group> &gs) {
             g->cpt = cpt;
             g->vpb = vpb;
             g->uni = c->uniform != 0;
+            g->nsig = sig;
         }
         g->members.push_back((int)k);
     }
@@ -290,8 +293,10 @@ int group_launches(hyb_batch *b, const Plan &P, const Group &g, unsigned char *t
         rc = prec == HYB_PREC_FP64
                  ? hyb::sweep_batch_f64((const hyb::KinArgs<double> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
                                         g.uni, HYB_SCHEME_NND, s)
-                 : hyb::sweep_batch_f32((const hyb::KinArgs<float> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
-                                        g.uni, HYB_SCHEME_NND, s);
+             : g.nsig ? hyb::sweep_nnd_batch_f32((const hyb::KinArgs<float> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.vpb,
+                                                 g.nsig, s)
+                      : hyb::sweep_batch_f32((const hyb::KinArgs<float> *)(t + g.o_kin), kw, g.n_kin, g.PA, g.cpt, g.vpb,
+                                             g.uni, HYB_SCHEME_NND, s);
     }
     const int4 *mw = (const int4 *)(t + g.o_mwork), *fw = (const int4 *)(t + g.o_fwork);
     if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 10, t + g.o_mom, mw, g.n_mom, g.mom_smem, s);
@@ -315,7 +320,8 @@ int group_prepare(hyb_batch *b, const Group &g) {
     if (!rc)
         rc = prec == HYB_PREC_FP64
                  ? hyb::sweep_batch_f64(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main)
-                 : hyb::sweep_batch_f32(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main);
+             : g.nsig ? hyb::sweep_nnd_batch_f32(nullptr, nullptr, 0, g.PA, g.vpb, g.nsig, b->main)
+                      : hyb::sweep_batch_f32(nullptr, nullptr, 0, g.PA, g.cpt, g.vpb, g.uni, HYB_SCHEME_NND, b->main);
     if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 10, nullptr, nullptr, 0, g.mom_smem, b->main);
     if (!rc) rc = hyb::moments_part_batch_launch(prec, g.mc, g.tpv, 4, nullptr, nullptr, 0, g.mom_smem, b->main);
     return rc;

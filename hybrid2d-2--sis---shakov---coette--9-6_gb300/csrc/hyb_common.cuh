@@ -166,6 +166,9 @@ __host__ __device__ inline size_t hyb_eqp_elems(size_t ncell) {
 namespace hyb {
 bool sweep_nnd_ok(const hyb_ctx *ctx, int cpt);
 bool sweep_cpt_ok(const hyb_ctx *ctx, int cpt);
+int sweep_nnd_signature(const hyb_ctx *ctx, int cpt);
+int sweep_nnd_batch_f32(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int vpb, int sig,
+                        cudaStream_t s);
 int launch_wall(hyb_ctx *ctx);
 int launch_sweep(hyb_ctx *ctx, int store_rhs);
 int sweep_prepare(hyb_ctx *ctx);

@@ -27,6 +27,16 @@ bool sweep_nnd_ok(const hyb_ctx *ctx, int c) {
     return c == 4 && ctx->cpt == 4 && ctx->Na % 4 == 0 && ctx->PA % HYB_EQP_BLK == 0;
 }
 
+// 0 when the context's sweep at c cells per thread is the generic one; else
+// 8 | periodic scan axis | periodic march axis << 1 | scan axis = j << 2, the
+// template signature of the specialised kernel (reference order)
+int sweep_nnd_signature(const hyb_ctx *ctx, int c) {
+    if (!sweep_nnd_ok(ctx, c) || ctx->prm.sweep_order != HYB_SWEEP_REFERENCE) return 0;
+    const int fa_lo = ctx->scan_is_j ? 2 : 1, fb_lo = ctx->scan_is_j ? 1 : 2;
+    const int pa = ctx->bc[fa_lo - 1] == HYB_BC_PERIODIC, pb = ctx->bc[fb_lo - 1] == HYB_BC_PERIODIC;
+    return 8 | pa | (pb << 1) | ((ctx->scan_is_j != 0) << 2);
+}
+
 // cells per thread c admissible for the context's sweep
 bool sweep_cpt_ok(const hyb_ctx *ctx, int c) {
     return (c == 1 || c == 2 || c == 4) && ctx->cpt % c == 0 && ctx->PA / c <= 256;

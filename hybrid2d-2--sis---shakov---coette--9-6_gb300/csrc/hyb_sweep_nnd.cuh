@@ -586,6 +586,50 @@ inline int sweep_nnd_dispatch_cpt(hyb_ctx *ctx, const KinArgs<float> &A, int vpb
               : sweep_nnd_launch<CPT, false, false, false, UPW>(ctx, A, vpb, launch);
 }
 
+// many contexts of one launch shape and one kernel signature in one launch:
+// CTA i sweeps velocity block work[i].y of context work[i].x (reference order;
+// batches do not take the upwind order)
+template <bool PERA, bool PERB, bool SJ>
+__global__ void __launch_bounds__(256, 2) k_sweep_nnd_batch(const KinArgs<float> *__restrict__ args,
+                                                            const int2 *__restrict__ work) {
+    __shared__ KinArgs<float> As;
+    const int2 w = work[blockIdx.x];
+    if (threadIdx.x == 0 && threadIdx.y == 0) As = args[w.x];
+    __syncthreads();
+    sweep_nnd<4, PERA, PERB, SJ, false>(As, w.y);
+}
+
+template <bool PERA, bool PERB, bool SJ>
+int sweep_nnd_batch_one(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int vpb, cudaStream_t s) {
+    const int tpv = PA / 4;
+    const size_t smem = nnd_group_bytes(PA, tpv) * vpb;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sweep_nnd_batch<PERA, PERB, SJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024 - 1024);
+        attr = true;
+    }
+    if (nwork <= 0) return HYB_OK;   // attributes only (before a capture)
+    k_sweep_nnd_batch<PERA, PERB, SJ><<<nwork, dim3(tpv, vpb), smem, s>>>(args, work);
+    return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+}
+
+// sig: sweep_nnd_signature (bit 0 periodic scan axis, bit 1 periodic march
+// axis, bit 2 scan axis = j)
+inline int sweep_nnd_batch(const KinArgs<float> *args, const int2 *work, int nwork, int PA, int vpb, int sig,
+                           cudaStream_t s) {
+    switch (sig & 7) {
+        case 0: return sweep_nnd_batch_one<false, false, false>(args, work, nwork, PA, vpb, s);
+        case 1: return sweep_nnd_batch_one<true, false, false>(args, work, nwork, PA, vpb, s);
+        case 2: return sweep_nnd_batch_one<false, true, false>(args, work, nwork, PA, vpb, s);
+        case 3: return sweep_nnd_batch_one<true, true, false>(args, work, nwork, PA, vpb, s);
+        case 4: return sweep_nnd_batch_one<false, false, true>(args, work, nwork, PA, vpb, s);
+        case 5: return sweep_nnd_batch_one<true, false, true>(args, work, nwork, PA, vpb, s);
+        case 6: return sweep_nnd_batch_one<false, true, true>(args, work, nwork, PA, vpb, s);
+        default: return sweep_nnd_batch_one<true, true, true>(args, work, nwork, PA, vpb, s);
+    }
+}
+
 // the specialised sweep (sweep_nnd_ok(ctx, 4) holds), in the context's order
 inline int sweep_nnd_dispatch(hyb_ctx *ctx, const KinArgs<float> &A, int vpb, bool launch) {
     return ctx->prm.sweep_order == HYB_SWEEP_UPWIND ? sweep_nnd_dispatch_cpt<4, true>(ctx, A, vpb, launch)
