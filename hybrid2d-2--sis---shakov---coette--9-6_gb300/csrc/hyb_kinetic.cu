@@ -620,6 +620,21 @@ __global__ void __launch_bounds__(256, 3) k_moments_f2(MomArgs M) {
     moments_body_f2<NM>(M, blockIdx.x, blockIdx.y);
 }
 
+// many contexts in one launch: CTA i takes march row work[i].y and velocity
+// slice work[i].z of context work[i].x
+template <int NM>
+__global__ void __launch_bounds__(256, 3) k_moments_f2_batch(const MomArgs *__restrict__ args,
+                                                            const int4 *__restrict__ work) {
+    __shared__ MomArgs Ms;
+    const int4 w = work[blockIdx.x];
+    if (threadIdx.x == 0) Ms = args[w.x];
+    __syncthreads();
+    moments_body_f2<NM>(Ms, w.y, w.z);
+}
+
+// the packed FP32 pass takes FP32 rows of up to 512 cells at two cells per thread
+static bool mom_f2_ok(int precision, int mc, int tpv) { return precision != HYB_PREC_FP64 && mc == 2 && tpv <= 256; }
+
 // NARROW: CTAs of at most 256 threads, three per SM (80 registers); FP32
 // rows of up to 512 cells take it, wider rows and FP64 keep 512 threads
 template <typename real, int MC, int NM, bool NARROW>
@@ -1252,6 +1267,8 @@ size_t mom_arg_bytes() { return sizeof(MomArgs); }
 int mom_arg_fill(hyb_ctx *ctx, const void *f, void *dst, int *mc, int *tpv, size_t *smem, int *vs, int *lpc,
                  int *nfin) {
     MomArgs M = mom_args(ctx, f ? f : ctx->d_f, smem, mc);
+    if (mom_f2_ok(ctx->precision, *mc, ctx->PA / *mc))   // the batched packed pass's shared memory
+        *smem = mom_f2_smem_bytes(ctx->PA, M.nloc_max);
     if (*smem > (size_t)227 * 1024 - 1024) return HYB_ERR_UNSUPPORTED;   // the batched kernel's limit
     memcpy(dst, &M, sizeof(M));
     *tpv = ctx->PA / *mc;
@@ -1287,6 +1304,16 @@ static int mom_part_batch_one(const MomArgs *args, const int4 *work, int nwork, 
 template <int NM>
 static int mom_part_batch_nm(int precision, int mc, int tpv, const MomArgs *a, const int4 *work, int nwork,
                              size_t smem, cudaStream_t s) {
+    if (mom_f2_ok(precision, mc, tpv)) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_moments_f2_batch<NM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 1024);
+            attr = true;
+        }
+        if (nwork <= 0) return HYB_OK;   // attributes only (before a capture)
+        k_moments_f2_batch<NM><<<nwork, tpv, smem, s>>>(a, work);
+        return cudaGetLastError() == cudaSuccess ? HYB_OK : HYB_ERR_CUDA;
+    }
     if (precision == HYB_PREC_FP64)
         return mc == 2 ? mom_part_batch_one<double, 2, NM>(a, work, nwork, tpv, smem, s)
                        : mom_part_batch_one<double, 1, NM>(a, work, nwork, tpv, smem, s);
