@@ -230,6 +230,7 @@ class Solver:
         gp.correct_f = kw.get("correct_f", 0)
         gp.wall_band = kw.get("wall_band", 0)
         gp.relax_pct = kw.get("relax_pct", 0)
+        gp.line_mean = kw.get("line_mean", 0)
         self._ck(self.L.hyb_gsis_configure(self.h, C.byref(gp)), "gsis_configure")
 
     def gsis_last_inner(self):

@@ -71,6 +71,9 @@ struct NsDev {
     double *wface;                                           // wall-face kinetic rho, u, v, T [4][4][mx]
     double *sk;                                              // band moments before the correction [6][nc]
     double *lin;                                             // line-solver scratch [16][nc]
+    int line_mean;                                           // the line-averaged correction (ns_solver 2)
+    float *lmean;                                            // its rows A, B, C [16], d [4], x [4] and the
+                                                             // sequential scratch G [16], g [4], per cell
     double *d, *uu, *vv, *T, *p, *cc, *amu;
     double *fluxi, *fluxj, *ti_out, *qi_out, *tj_out, *qj_out;
     const double *vol, *si, *sj, *ni1, *ni2, *nj1, *nj2;   // (nx,ny)
@@ -963,18 +966,32 @@ __device__ __forceinline__ void mm4(const float *X, const float *Y, float *Z) { 
 // and c = -C_k B_{k+s}^-1, A' = a A_{k-s}, C' = c C_{k+s},
 // B' = B_k + a C_{k-s} + c A_{k+s}, d' = d_k + a d_{k-s} + c d_{k+s}; after
 // ceil(log2 n) steps every row is decoupled and dU_k = B_k^-1 d_k.
+// MEAN: the line-averaged system of line_mean instead of a mesh line (one
+// CTA; rows from D.lmean, the solution x back into D.lmean).
 constexpr int PCR_MAX = 512;
+// floats per cell of D.lmean: A, B, C [16], d [4], x [4] (offset 52),
+// G [16] (56), g [4] (72) of the sequential elimination
+constexpr int LMEAN_ROW = 80;
+template <bool MEAN>
 __global__ void __launch_bounds__(PCR_MAX, 1) k_ns_lines_pcr(NsDev D, int col) {
     if (D.ctrl->done) return;
     const LineGeo G = line_geo(D);
-    const int ln = line_of(G, col, blockIdx.x);
+    const int ln = MEAN ? 0 : line_of(G, col, blockIdx.x);
     if (ln < 0) return;
     const int n = G.k1 - G.k0 + 1, k = threadIdx.x;
     extern __shared__ float pcr_sm[];
     float *sA = pcr_sm, *sB = sA + 16 * n, *sC = sB + 16 * n, *sD = sC + 16 * n, *sI = sD + 4 * n;
     float A[16], B[16], C[16], d[4];
     if (k < n) {
-        line_row(D, G, ln, G.k0 + k, A, B, C, d);
+        if (MEAN) {
+            const float *row = D.lmean + (size_t)k * LMEAN_ROW;
+#pragma unroll
+            for (int q = 0; q < 16; q++) { A[q] = row[q]; B[q] = row[16 + q]; C[q] = row[32 + q]; }
+#pragma unroll
+            for (int q = 0; q < 4; q++) d[q] = row[48 + q];
+        } else {
+            line_row(D, G, ln, G.k0 + k, A, B, C, d);
+        }
 #pragma unroll
         for (int q = 0; q < 16; q++) { sA[k * 16 + q] = A[q]; sB[k * 16 + q] = B[q]; sC[k * 16 + q] = C[q]; }
 #pragma unroll
@@ -1055,9 +1072,168 @@ __global__ void __launch_bounds__(PCR_MAX, 1) k_ns_lines_pcr(NsDev D, int col) {
             float t = 0.f;
 #pragma unroll
             for (int m = 0; m < 4; m++) t += Bi[r * 4 + m] * d[m];
-            D.dU[(size_t)r * D.nc + c] = (double)t;
+            if (MEAN) D.lmean[(size_t)k * LMEAN_ROW + 52 + r] = t;
+            else D.dU[(size_t)r * D.nc + c] = (double)t;
         }
     }
+}
+
+// ---- the line-averaged correction (line_mean, no counterpart in the
+// reference) -------------------------------------------------------------------
+// With dU_(l,k) = x_k on every line l, the line system becomes one block-
+// tridiagonal system along the line axis whose blocks are the means over the
+// lines of A, of B minus the two cross-axis neighbour blocks, of C, and whose
+// right side is the mean of Res: the Galerkin coarse operator of the
+// prolongation that copies x to every line and the restriction that
+// averages.  Before the colour passes of an inner iteration it is assembled
+// (k_ns_lmean_rows), solved (k_ns_lines_pcr<true>, or k_ns_lmean_seq for
+// lines above PCR_MAX cells) and copied to every line (k_ns_lmean_fill).  On
+// a problem invariant along the periodic axis that is the exact solution of
+// the line system; line Gauss-Seidel alone builds that mode up over
+// O((cells across / line length)^2) passes.
+
+// the sum of the two cross-axis neighbour blocks of cell (ln, k), those
+// line_row applies to the neighbouring lines' dU
+__device__ void cross_blocks(const NsDev &D, const LineGeo &G, int ln, int k, float *X) {
+    const bool aj = G.along_j;
+    const int i = aj ? ln : k, j = aj ? k : ln;
+    const size_t nc = D.nc;
+    const float g = (float)D.gamma;
+#pragma unroll
+    for (int q = 0; q < 16; q++) X[q] = 0.f;
+    for (int side = 0; side < 2; side++) {
+        int q = side == 0 ? ln - 1 : ln + 1;
+        if (q < G.n0 || q > G.n1) {
+            if (!G.per) continue;
+            q = q < G.n0 ? G.n1 : G.n0;
+        }
+        const size_t cn = c2(D, aj ? q : i, aj ? j : q);
+        float Un[4], J[16];
+#pragma unroll
+        for (int m = 0; m < 4; m++) Un[m] = (float)D.U[(size_t)m * nc + cn];
+        const float m1 = (float)(aj ? D.ni1[mi(D, i, j)] : D.nj1[mi(D, i, j)]);
+        const float m2 = (float)(aj ? D.ni2[mi(D, i, j)] : D.nj2[mi(D, i, j)]);
+        const float dg = (float)(0.5 * (aj ? D.Lci[cn] : D.Lcj[cn]) + (aj ? D.Lvi[cn] : D.Lvj[cn]));
+        const float sf = (float)(side == 0 ? (aj ? D.si[mi(D, i, j)] : D.sj[mi(D, i, j)])
+                                           : (aj ? D.si[mi(D, i + 1, j)] : D.sj[mi(D, i, j + 1)]));
+        const float sg = side == 0 ? 0.5f : -0.5f;
+        flux_jacf(Un, m1, m2, g, J);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) X[r * 4 + m] += sg * J[r * 4 + m] * sf + (r == m ? dg : 0.f);
+    }
+}
+
+// one CTA per cell k of the line axis sums over the lines; dU is 0 here
+// (k_ns_res reset it), so line_row's right side is Res
+constexpr int LMEAN_THREADS = 128;
+__global__ void __launch_bounds__(LMEAN_THREADS) k_ns_lmean_rows(NsDev D) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int k = G.k0 + blockIdx.x;
+    if (k > G.k1) return;
+    float acc[52];
+#pragma unroll
+    for (int q = 0; q < 52; q++) acc[q] = 0.f;
+    for (int ln = G.n0 + (int)threadIdx.x; ln <= G.n1; ln += LMEAN_THREADS) {
+        float A[16], B[16], C[16], d[4], X[16];
+        line_row(D, G, ln, k, A, B, C, d);
+        cross_blocks(D, G, ln, k, X);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            acc[q] += A[q];
+            acc[16 + q] += B[q] - X[q];
+            acc[32 + q] += C[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[48 + q] += d[q];
+    }
+    __shared__ float red[LMEAN_THREADS / 32][52];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 52; q++) {
+        float v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 52) {
+        float t = 0.f;
+#pragma unroll
+        for (int ww = 0; ww < LMEAN_THREADS / 32; ww++) t += red[ww][threadIdx.x];
+        D.lmean[(size_t)blockIdx.x * LMEAN_ROW + threadIdx.x] = t / (float)(G.n1 - G.n0 + 1);
+    }
+}
+
+// the line-averaged system above PCR_MAX cells: block-tridiagonal
+// elimination by one thread (A x_{k-1} + B x_k + C x_{k+1} = d,
+// x_{k-1} = g_{k-1} + G_{k-1} x_k)
+__global__ void k_ns_lmean_seq(NsDev D) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int n = G.k1 - G.k0 + 1;
+    for (int k = 0; k < n; k++) {
+        float *row = D.lmean + (size_t)k * LMEAN_ROW;
+        float A[16], M[16], r[4], Bm[20];
+#pragma unroll
+        for (int q = 0; q < 16; q++) { A[q] = row[q]; M[q] = row[16 + q]; }
+#pragma unroll
+        for (int q = 0; q < 4; q++) r[q] = row[48 + q];
+        if (k > 0) {
+            const float *pr = row - LMEAN_ROW;
+            float T[16];
+            mm4(A, pr + 56, T);
+#pragma unroll
+            for (int q = 0; q < 16; q++) M[q] += T[q];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int m = 0; m < 4; m++) r[a] -= A[a * 4 + m] * pr[72 + m];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) Bm[a * 5 + q] = -row[32 + a * 4 + q];
+            Bm[a * 5 + 4] = r[a];
+        }
+        solve4f<5>(M, Bm);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) row[56 + a * 4 + q] = Bm[a * 5 + q];
+            row[72 + a] = Bm[a * 5 + 4];
+        }
+    }
+    float nxt[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k = n - 1; k >= 0; k--) {
+        float *row = D.lmean + (size_t)k * LMEAN_ROW;
+        float x[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            float t = row[72 + a];
+#pragma unroll
+            for (int q = 0; q < 4; q++) t += row[56 + a * 4 + q] * nxt[q];
+            x[a] = t;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) { row[52 + a] = x[a]; nxt[a] = x[a]; }
+    }
+}
+
+// dU of every band cell from the solution of its position on the line axis
+__global__ void k_ns_lmean_fill(NsDev D) {
+    if (D.ctrl->done) return;
+    const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= bw * bh) return;
+    const int i = D.ilo + t % bw, j = D.jlo + t / bw;
+    const LineGeo G = line_geo(D);
+    const float *x = D.lmean + (size_t)((G.along_j ? j : i) - G.k0) * LMEAN_ROW + 52;
+    const size_t c = c2(D, i, j);
+#pragma unroll
+    for (int m = 0; m < 4; m++) D.dU[(size_t)m * D.nc + c] = (double)x[m];
 }
 
 // lines longer than PCR_MAX cells: block-tridiagonal elimination, one
@@ -1587,11 +1763,13 @@ static void ns_band(const hyb_ctx *ctx, NsDev &D) {
     if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = e; D.jhi = D.ny - e; }
     D.wall_band = ctx->gsis.wall_band != 0;
     D.relax = ctx->gsis.relax_pct > 0 ? ctx->gsis.relax_pct / 100.0 : 1.0;
+    D.line_mean = ctx->gsis.line_mean != 0;
 }
 
 int ns_create(hyb_ctx *ctx) {
     if (ctx->gsis.ns_solver < 0 || ctx->gsis.ns_solver > 2 || ctx->gsis.relax_pct < 0 ||
-        ctx->gsis.relax_pct > 100)
+        ctx->gsis.relax_pct > 100 || ctx->gsis.line_mean < 0 || ctx->gsis.line_mean > 1 ||
+        (ctx->gsis.line_mean && ctx->gsis.ns_solver != 2))
         return HYB_ERR_INVALID;
     if (ctx->ns) {   // reconfigured: re-capture with the new parameters
         NsState *st = (NsState *)ctx->ns;
@@ -1625,6 +1803,7 @@ int ns_create(hyb_ctx *ctx) {
     // see the pointer carve below; the wall-face states follow the last array
     const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6;
     const size_t nwf = (size_t)16 * (D.nx > D.ny ? D.nx : D.ny);
+    const size_t nlm = (size_t)LMEAN_ROW / 2 * (D.nx > D.ny ? D.nx : D.ny);   // doubles
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
     if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
@@ -1639,14 +1818,14 @@ int ns_create(hyb_ctx *ctx) {
         return HYB_ERR_NOMEM;
     }
     cudaMemsetAsync(st->rk, 0, 4 * ncell * sizeof(double), ctx->stream);
-    if (cudaMalloc((void **)&st->buf, ((size_t)ncomp * nc + nwf) * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc((void **)&st->buf, ((size_t)ncomp * nc + nwf + nlm) * sizeof(double)) != cudaSuccess) {
         cudaFree(st->rk);
         cudaFree(ctx->d_rhs_gsis);
         ctx->d_rhs_gsis = nullptr;
         delete st;
         return HYB_ERR_NOMEM;
     }
-    cudaMemsetAsync(st->buf, 0, ((size_t)ncomp * nc + nwf) * sizeof(double), ctx->stream);
+    cudaMemsetAsync(st->buf, 0, ((size_t)ncomp * nc + nwf + nlm) * sizeof(double), ctx->stream);
     double *h = st->buf;
     D.U = h; h += 4 * nc; D.src = h; h += 4 * nc; D.U2 = h; h += 4 * nc; D.dU = h; h += 4 * nc; D.Res = h; h += 4 * nc;
     D.dt = h; h += nc; D.Lci = h; h += nc; D.Lcj = h; h += nc; D.Lvi = h; h += nc; D.Lvj = h; h += nc;
@@ -1657,6 +1836,7 @@ int ns_create(hyb_ctx *ctx) {
     D.lin = h; h += 16 * nc;
     D.sk = h; h += 6 * nc;
     D.wface = h; h += nwf;  // [4 faces][rho u v T][max(nx, ny)]
+    D.lmean = reinterpret_cast<float *>(h); h += nlm;   // [max(nx, ny)][LMEAN_ROW] floats
     const size_t nm = (size_t)ctx->nx * ctx->ny;
     if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
         cudaFree(st->buf);
@@ -1725,7 +1905,9 @@ int ns_create(hyb_ctx *ctx) {
     st->have_graph = false;
     // the line solver's reduction holds a line of up to PCR_MAX cells in
     // shared memory (set before any capture)
-    cudaFuncSetAttribute(k_ns_lines_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_ns_lines_pcr<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(68 * PCR_MAX * sizeof(float)));
+    cudaFuncSetAttribute(k_ns_lines_pcr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(68 * PCR_MAX * sizeof(float)));
     {
         // enough blocks for one cell per thread, within what is co-resident
@@ -1771,12 +1953,20 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
         const bool aj = !D.pery;
         const int nl = aj ? D.ihi - D.ilo + 1 : D.jhi - D.jlo + 1, nk = aj ? D.jhi - D.jlo + 1 : D.ihi - D.ilo + 1;
         const bool per = aj ? D.perx != 0 : D.pery != 0;
+        if (D.line_mean && per) {
+            k_ns_lmean_rows<<<nk, LMEAN_THREADS, 0, s>>>(D);
+            if (nk <= PCR_MAX)
+                k_ns_lines_pcr<true><<<1, PCR_MAX, (size_t)68 * nk * sizeof(float), s>>>(D, 0);
+            else
+                k_ns_lmean_seq<<<1, 1, 0, s>>>(D);
+            k_ns_lmean_fill<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
+        }
         const int order[4] = {0, 1, 2, 0};
         for (int ph = 0; ph < 4; ph++) {
             const int col = order[ph], cnt = lines_of_colour(nl, per, col);
             if (cnt == 0) continue;
             if (nk <= PCR_MAX)
-                k_ns_lines_pcr<<<cnt, PCR_MAX, (size_t)68 * nk * sizeof(float), s>>>(D, col);
+                k_ns_lines_pcr<false><<<cnt, PCR_MAX, (size_t)68 * nk * sizeof(float), s>>>(D, col);
             else
                 k_ns_lines_seq<<<(cnt + 31) / 32, 32, 0, s>>>(D, col);
         }
@@ -1801,7 +1991,7 @@ static int inner_launches(const hyb_ctx *ctx, const NsDev &D) {
         const int nl = aj ? D.ihi - D.ilo + 1 : D.jhi - D.jlo + 1;
         const bool per = aj ? D.perx != 0 : D.pery != 0;
         lines = 2 * (lines_of_colour(nl, per, 0) > 0) + (lines_of_colour(nl, per, 1) > 0) +
-                (lines_of_colour(nl, per, 2) > 0);
+                (lines_of_colour(nl, per, 2) > 0) + (D.line_mean && per ? 3 : 0);
     }
     const int solver = ctx->gsis.ns_solver == 2 ? lines : (ctx->gsis.ns_solver == 1 ? 2 : 4);
     return 6 + solver + (D.mlp_on ? 2 : 0) + (D.wall_band ? 1 : 0);

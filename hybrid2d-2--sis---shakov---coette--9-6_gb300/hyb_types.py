@@ -83,7 +83,7 @@ class HybGsisParams(C.Structure):
         ("flux", C.c_int), ("ns_scheme", C.c_int), ("mlp_warm_after", C.c_int),
         ("ns_solver", C.c_int), ("correct_f", C.c_int), ("no_mass_projection", C.c_int),
         ("lusgs_planes", C.c_int), ("mlp_warm_inner", C.c_int), ("mlp_warm_rtol", C.c_double),
-        ("wall_band", C.c_int), ("relax_pct", C.c_int),
+        ("wall_band", C.c_int), ("relax_pct", C.c_int), ("line_mean", C.c_int),
     ]
 
 

@@ -49,7 +49,7 @@ module hyb_dvm
      integer(c_int) :: flux, ns_scheme, mlp_warm_after, ns_solver
      integer(c_int) :: correct_f, no_mass_projection, lusgs_planes, mlp_warm_inner
      real(c_double) :: mlp_warm_rtol
-     integer(c_int) :: wall_band, relax_pct
+     integer(c_int) :: wall_band, relax_pct, line_mean
   end type hyb_gsis_params
 
   interface

@@ -188,6 +188,12 @@ typedef struct hyb_gsis_params {
                                kinetic state held outside it              */
     int    relax_pct;       /* the correction is applied as U_k + r (U - U_k),
                                r = relax_pct / 100 (0: r = 1, the reference)  */
+    int    line_mean;       /* ns_solver 2 with a periodic axis across the
+                               lines: 1 also solves, in each inner iteration
+                               and before the line passes, the system of the
+                               correction that is constant across the
+                               periodic axis (the line system averaged over
+                               the lines); no counterpart in the reference  */
 } hyb_gsis_params;
 
 typedef struct hyb_ctx hyb_ctx;

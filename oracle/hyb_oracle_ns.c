@@ -35,6 +35,10 @@
  *     black, backward sweep black then red, dU reset to 0 at each inner
  *     iteration.  lusgs_planes = 1 in hyb_gsis_params selects the
  *     reference's anti-diagonal order instead.
+ *   - ns_solver 2 solves the same matrix exactly along every wall-normal
+ *     line (ns_lines); line_mean adds the coarse solve of the line-averaged
+ *     system before the line passes (ns_line_mean).  Neither has a
+ *     counterpart in the reference.
  */
 #include "hyb_oracle_impl.h"
 
@@ -734,6 +738,124 @@ static void cross_terms(orc *o, int i, int j, int along_j, int per, int lo, int 
     }
 }
 
+/* one neighbour block of the line system of cell (i, j): the block of the
+ * cell at (ia, ja) across the face with normal (n1f, n2f) and area sf, with
+ * the spectral radii of cell cr; sg = +0.5 for the lower neighbour
+ * (0.5 (A s + Lc) + Lv), -0.5 for the upper one (-0.5 (A s - Lc) + Lv) */
+static void nb_block(orc *o, size_t cn, size_t cr, int lc_i, double n1f, double n2f, double sf, double sg,
+                     double *B)
+{
+    struct orc_ns *ns = o->ns;
+    double Un[4], A[16];
+    get4(ns, ns->U, cn, Un);
+    flux_jacobian(Un, n1f, n2f, o->prm.gamma, A);
+    const double lc = lc_i ? ns->Lci[cr] : ns->Lcj[cr], lv = lc_i ? ns->Lvi[cr] : ns->Lvj[cr];
+    for (int q = 0; q < 16; q++) B[q] = sg * A[q] * sf;
+    for (int q = 0; q < 4; q++) B[q * 4 + q] += 0.5 * lc + lv;
+}
+
+/* the mode constant across the periodic axis (line_mean, no counterpart in
+ * the reference).  With dU_(l,k) = e_k on every line l the line system
+ * becomes one block-tridiagonal system along the line axis whose blocks are
+ * the means over the lines of (diagonal - the two cross-axis neighbour
+ * blocks), of the lower and of the upper neighbour blocks, and whose right
+ * side is the mean of Res: the Galerkin coarse operator of the prolongation
+ * that copies e to every line and the restriction that averages.  It is
+ * solved exactly and dU is set to e on every line before the red-black line
+ * passes.  On a problem that is invariant along the periodic axis this is
+ * the exact solution of the line system; line Gauss-Seidel alone takes
+ * O((cells across / line length)^2) passes to build that mode up. */
+static void ns_line_mean(orc *o, int along_j, int n0, int n1, int k0, int k1, double *G, double *gv)
+{
+    struct orc_ns *ns = o->ns;
+    const int nl = n1 - n0 + 1;
+    const double inl = 1.0 / nl;
+    for (int k = k0; k <= k1; k++) {
+        double D[16], Lo[16], Up[16], r[4], B[16];
+        for (int q = 0; q < 16; q++) D[q] = Lo[q] = Up[q] = 0.0;
+        for (int m = 0; m < 4; m++) r[m] = 0.0;
+        const int wlo = o->gsis.wall_band && k == k0 && o->bc[along_j ? 1 : 0] == HYB_BC_WALL;
+        const int whi = o->gsis.wall_band && k == k1 && o->bc[along_j ? 3 : 2] == HYB_BC_WALL;
+        for (int ln = n0; ln <= n1; ln++) {
+            const int i = along_j ? ln : k, j = along_j ? k : ln;
+            const size_t c = C2(o, i, j);
+            const double alfa = o->vol[MI(o, i, j)] / ns->dt[c] + ns->Lci[c] + ns->Lcj[c] +
+                                2.0 * (ns->Lvi[c] + ns->Lvj[c]);
+            for (int q = 0; q < 4; q++) D[q * 4 + q] += alfa;
+            for (int m = 0; m < 4; m++) r[m] += A4(ns->Res, m, c);
+            /* cross-axis neighbours (periodic): lower line p-1, upper line p+1 */
+            {
+                const int lo = ln > n0 ? ln - 1 : n1, hi = ln < n1 ? ln + 1 : n0;
+                const size_t clo = along_j ? C2(o, lo, j) : C2(o, i, lo), chi = along_j ? C2(o, hi, j) : C2(o, i, hi);
+                const double n1f = along_j ? o->ni1[MI(o, i, j)] : o->nj1[MI(o, i, j)];
+                const double n2f = along_j ? o->ni2[MI(o, i, j)] : o->nj2[MI(o, i, j)];
+                const double slo = along_j ? o->si[MI(o, i, j)] : o->sj[MI(o, i, j)];
+                const double shi = along_j ? o->si[MI(o, i + 1, j)] : o->sj[MI(o, i, j + 1)];
+                nb_block(o, clo, clo, along_j, n1f, n2f, slo, 0.5, B);
+                for (int q = 0; q < 16; q++) D[q] -= B[q];
+                nb_block(o, chi, chi, along_j, n1f, n2f, shi, -0.5, B);
+                for (int q = 0; q < 16; q++) D[q] -= B[q];
+            }
+            const double n1f = along_j ? o->nj1[MI(o, i, j)] : o->ni1[MI(o, i, j)];
+            const double n2f = along_j ? o->nj2[MI(o, i, j)] : o->ni2[MI(o, i, j)];
+            if (k > k0 || wlo) {
+                const size_t cn = along_j ? C2(o, i, j - 1) : C2(o, i - 1, j);
+                const double sf = along_j ? o->sj[MI(o, i, j)] : o->si[MI(o, i, j)];
+                nb_block(o, cn, wlo ? c : cn, !along_j, n1f, n2f, sf, 0.5, B);
+                double *T = wlo ? D : Lo;
+                for (int q = 0; q < 16; q++) T[q] += B[q];
+            }
+            if (k < k1 || whi) {
+                const size_t cn = along_j ? C2(o, i, j + 1) : C2(o, i + 1, j);
+                const double sf = along_j ? o->sj[MI(o, i, j + 1)] : o->si[MI(o, i + 1, j)];
+                nb_block(o, cn, whi ? c : cn, !along_j, n1f, n2f, sf, -0.5, B);
+                double *T = whi ? D : Up;
+                for (int q = 0; q < 16; q++) T[q] += B[q];
+            }
+        }
+        double M[16], Bm[20];
+        for (int q = 0; q < 16; q++) M[q] = D[q] * inl;
+        for (int m = 0; m < 4; m++) {
+            Bm[m * 5 + 4] = r[m] * inl;
+            for (int q = 0; q < 4; q++) Bm[m * 5 + q] = Up[m * 4 + q] * inl;
+        }
+        if (k > k0) {   /* M -= L G_{k-1}; r += L g_{k-1} */
+            const double *Gp = G + (size_t)(k - 1 - k0) * 16, *gp = gv + (size_t)(k - 1 - k0) * 4;
+            for (int a = 0; a < 4; a++) {
+                for (int q = 0; q < 4; q++) {
+                    double t = 0.0;
+                    for (int m = 0; m < 4; m++) t += Lo[a * 4 + m] * inl * Gp[m * 4 + q];
+                    M[a * 4 + q] -= t;
+                }
+                double t = 0.0;
+                for (int m = 0; m < 4; m++) t += Lo[a * 4 + m] * inl * gp[m];
+                Bm[a * 5 + 4] += t;
+            }
+        }
+        solve4(M, Bm, 5);
+        double *Gk = G + (size_t)(k - k0) * 16, *gk = gv + (size_t)(k - k0) * 4;
+        for (int a = 0; a < 4; a++) {
+            for (int q = 0; q < 4; q++) Gk[a * 4 + q] = Bm[a * 5 + q];
+            gk[a] = Bm[a * 5 + 4];
+        }
+    }
+    double nxt[4] = {0, 0, 0, 0};
+    for (int k = k1; k >= k0; k--) {
+        const double *Gk = G + (size_t)(k - k0) * 16, *gk = gv + (size_t)(k - k0) * 4;
+        double d[4];
+        for (int a = 0; a < 4; a++) {
+            double t = gk[a];
+            for (int q = 0; q < 4; q++) t += Gk[a * 4 + q] * nxt[q];
+            d[a] = t;
+        }
+        for (int ln = n0; ln <= n1; ln++) {
+            const int i = along_j ? ln : k, j = along_j ? k : ln;
+            for (int a = 0; a < 4; a++) A4(ns->dU, a, C2(o, i, j)) = d[a];
+        }
+        for (int a = 0; a < 4; a++) nxt[a] = d[a];
+    }
+}
+
 static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
 {
     struct orc_ns *ns = o->ns;
@@ -746,6 +868,7 @@ static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
     double *G = malloc((size_t)nk * 16 * sizeof(double)), *gv = malloc((size_t)nk * 4 * sizeof(double));
     if (!G || !gv) { free(G); free(gv); return HYB_ERR_NOMEM; }
     memset(ns->dU, 0, 4 * ns->nc * sizeof(double));
+    if (o->gsis.line_mean && per) ns_line_mean(o, along_j, n0, n1, k0, k1, G, gv);
     /* red-black line Gauss-Seidel: colour 0 (even offsets from n0), 1 (odd),
      * 2 (the last line of an odd periodic count, which meets line n0 across
      * the seam), then colour 0 again; a line takes the current dU of its

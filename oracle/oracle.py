@@ -15,9 +15,14 @@ LIB_PATH = os.path.join(HERE, "_build", "libhyb_oracle.so")
 _lib = None
 
 
+def _sources():
+    own = [os.path.join(HERE, n) for n in os.listdir(HERE) if n.endswith((".c", ".h")) or n == "Makefile"]
+    return own + [os.path.join(os.path.dirname(HERE), "include", "hyb_dvm.h")]
+
+
 def build(force=False):
     if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "hyb_oracle.c")):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(p) for p in _sources() if os.path.exists(p)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -178,6 +183,7 @@ class Oracle:
         gp.correct_f = kw.get("correct_f", 0)
         gp.wall_band = kw.get("wall_band", 0)
         gp.relax_pct = kw.get("relax_pct", 0)
+        gp.line_mean = kw.get("line_mean", 0)
         rc = self.L.orc_gsis_configure(self.h, C.byref(gp))
         if rc != 0:
             raise RuntimeError(f"orc_gsis_configure failed: {rc}")

@@ -74,3 +74,32 @@ def test_bench_batch_cases_keep_the_kinetic_cfl(cm):
     assert len(cl) == 256 and all(c.precision == 1 for c in cl)
     ratios = {round(c.dt * c.ncy / c.ly, 12) for c in cl}
     assert ratios == {0.64}
+
+
+def test_bench_time_to_residual_report_shape(cm, monkeypatch):
+    """time_to_residual's bookkeeping (field errors against the FP64 runs,
+    the wall-time ratios of the large case) on stand-in runs: no GPU, no
+    solver; every run the bench makes returns a fixed record."""
+    import numpy as np
+    import bench
+    calls = []
+
+    def fake(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
+             wall_s=None):
+        calls.append((name, case.name, prec, promote, learned, max_iters))
+        S = np.full((case.ncy - 1, case.ncx - 1, 4), 1.0 + 1e-9 * len(calls))
+        return {"seconds": 10.0 if "fp64" in name and "to_fp64" not in name else 4.0, "iterations": 100,
+                "residual": 5e-9, "reached": True}, S
+
+    monkeypatch.setattr(bench, "_ttr_run", fake)
+    out = bench.time_to_residual(large=True)
+    lg = out["large"]["runs"]
+    assert set(lg) == {"gsis_fp64_line_mean", "gsis_mixed_line_mean_to_fp64",
+                       "gsis_mixed_learned_line_mean_to_fp64", "gsis_mixed_without_line_mean", "plain_mixed"}
+    for name in ("gsis_mixed_line_mean_to_fp64", "gsis_mixed_learned_line_mean_to_fp64"):
+        assert lg[name]["wall_time_ratio_fp64_over_this"] == 2.5
+        assert set(lg[name]["field_rel_err_vs_fp64"]) == {"rho", "u", "v", "T"}
+    assert all(r["field_rel_err_vs_fp64"] is not None for r in out["runs"].values())
+    # the large case's runs are the 128x512 workload; the learned one loads the closure
+    large = [c for c in calls if c[1].startswith("couette-128x512")]
+    assert len(large) == 5 and sum(c[4] for c in large) == 1

@@ -125,3 +125,73 @@ def test_line_solver_gsis_converges_to_the_oracle_fixed_point(cases_mod):
     for k in range(10):
         d = np.abs(Sg[..., k] - So[..., k]).max()
         assert d <= 1e-10 * max(np.abs(So[..., k]).max(), 1e-2), (k, d)
+
+
+def _line_mean_case(cases_mod, kind, **kw):
+    """Wall-normal lines with a periodic axis across them: lines along j
+    (the channel), lines along i (walls on the x faces), and lines of 519
+    cells, above the 512 cells a CTA reduces (the sequential paths)."""
+    from hyb_gb300 import hyb_types as T
+    P, W = T.HYB_BC_PERIODIC, T.HYB_BC_WALL
+    if kind == "along_j":
+        return cases_mod.couette_small(ncx=24, ncy=32, nvx=16, nvy=16, **kw)
+    if kind == "along_i":
+        return cases_mod.couette_small(ncx=32, ncy=24, nvx=16, nvy=16, bcs=(W, P, W, P), t_top=1.2, **kw)
+    return cases_mod.couette_small(ncx=6, ncy=520, nvx=16, nvy=16, **kw)
+
+
+@pytest.mark.parametrize("kind", ["along_j", "along_i", "long"])
+def test_line_mean_matches_oracle(cases_mod, kind):
+    """line_mean: before the colour passes of each inner iteration, the
+    line system averaged over the lines is solved and copied to every line;
+    GPU (FP32 elimination, FP64 residual and update) against the oracle's
+    FP64 restatement after three outer iterations."""
+    c = _line_mean_case(cases_mod, kind, dt=1.0e6, sweep_order=1, mass_pin=1)
+    g, o = _pair(c, 0, wall_band=1, correct_f=1, ns_solver=2, line_mean=1, cfl=100.0, **FIXED)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    assert g.gsis_skipped() == o.gsis_skipped() == 0
+    _cmp_state(c, g, o, 1e-5)
+
+
+def test_line_mean_needs_the_line_solver(cases_mod):
+    from hyb_gb300 import abi, hyb_types as T
+    c = _line_mean_case(cases_mod, "along_j", dt=0.02)
+    s = abi.Solver(c, precision=0)
+    with pytest.raises(abi.HybError) as e:
+        s.gsis(ns_solver=0, line_mean=1, **FIXED)
+    assert e.value.rc == T.HYB_ERR_INVALID
+    s.close()
+
+
+def test_line_mean_converges_to_the_oracle_fixed_point(cases_mod):
+    """Kn 0.01 channel with 16 cells across the periodic axis (16 x 128,
+    48^2 velocities on [-6, 6], plates +-0.5, walls 1 / 1.2), upwind order
+    at dt 1e6, mass pin, band to the walls, line solver with line_mean:
+    residual 1e-8 within 100 outer iterations (the oracle: 70), and after
+    160 the converged moments equal the oracle's run of the same iteration
+    to 1e-10.  (Meshes of 32 or 64 cells along the wall normal stall near
+    4e-5 / 1.5e-7 with or without line_mean, in the oracle as on the GPU.)"""
+    c = cases_mod.Case(name="kn0.01-16x128", ncx=16, ncy=128, nvx=48, nvy=48, vmax=6.0, kn=0.01, uw=0.5,
+                       t_top=1.2, dt=1.0e6, sweep_order=1, mass_pin=1)
+    gk = dict(wall_band=1, correct_f=1, ns_solver=2, line_mean=1, cfl=300.0, max_inner=20, inner_tol=0.0,
+              inner_rtol=1e-4)
+    g, o = _pair(c, 0, **gk)
+    it, it8 = 0, None
+    while it < 160:
+        rg = g.step(10)
+        ro = o.step(10)
+        it += 10
+        if it8 is None and rg["max_rms"] < 1e-8:
+            it8 = it
+    assert it8 is not None and it8 <= 100, (it8, rg)
+    assert rg["max_rms"] < 1e-9 and ro["max_rms"] < 1e-9, (rg, ro)
+    sg, _ = g.moments()
+    so = o.s_gkua()
+    n = (c.ny + 7, c.nx + 7, 11)
+    Sg = sg.reshape(n)[4:4 + c.ny - 1, 4:4 + c.nx - 1, :10]
+    So = so.reshape(n)[4:4 + c.ny - 1, 4:4 + c.nx - 1, :10]
+    for k in range(10):
+        d = np.abs(Sg[..., k] - So[..., k]).max()
+        assert d <= 1e-10 * max(np.abs(So[..., k]).max(), 1e-2), (k, d)

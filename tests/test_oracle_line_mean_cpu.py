@@ -1,0 +1,53 @@
+"""CPU checks of the line-averaged correction of the synthetic solve
+(line_mean, oracle/hyb_oracle_ns.c ns_line_mean), which the GPU kernels
+k_ns_lmean_rows / k_ns_lines_pcr<true> / k_ns_lmean_seq / k_ns_lmean_fill are
+tested against.
+
+Line Gauss-Seidel across the periodic axis builds up the correction that is
+constant along that axis over O((cells across / line length)^2) passes; the
+coarse solve of the line system averaged over the lines gives it in one.  On
+a Kn 0.01 channel with 32 cells across and 48 along the wall normal (33^2
+velocities on [-6, 6], plates +-0.5, walls 1 / 1.2, upwind order at dt 1e6,
+mass pin, band to the walls, line solver of 20 inner iterations at CFL 300),
+40 outer iterations take the residual to 1.9e-6 with it and 5.3e-3 without.
+"""
+import pytest
+
+from oracle import oracle as O
+
+
+def _run(cases, line_mean, nit):
+    c = cases.Case(name="kn0.01-32x48", ncx=32, ncy=48, nvx=33, nvy=33, vmax=6.0, kn=0.01, uw=0.5, t_top=1.2,
+                   dt=1.0e6, sweep_order=1, mass_pin=1)
+    o = O.Oracle(c, threads=0)
+    o.init_maxwellian()
+    o.convert_ns()
+    o.gsis(wall_band=1, correct_f=1, ns_solver=2, line_mean=line_mean, cfl=300.0, max_inner=20, inner_tol=0.0,
+           inner_rtol=1e-4)
+    r = o.step(nit)
+    assert o.gsis_skipped() == 0
+    return r["max_rms"]
+
+
+def test_line_mean_accelerates_the_synthetic_solve(pkg):
+    from hyb_gb300 import cases
+    with_lm, without = _run(cases, 1, 40), _run(cases, 0, 40)
+    assert with_lm < 1e-5, with_lm
+    assert with_lm < 1e-2 * without, (with_lm, without)
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_line_mean_is_ignored_without_the_line_solver_in_the_oracle(pkg, solver):
+    """The oracle takes line_mean only in the line solver (the library
+    rejects it elsewhere): with LU-SGS or ADI the runs are bit-identical."""
+    from hyb_gb300 import cases
+    c = cases.couette_small(ncx=8, ncy=16, nvx=17, nvy=17, dt=0.02)
+    out = []
+    for lm in (0, 1):
+        o = O.Oracle(c, threads=0)
+        o.init_maxwellian()
+        o.convert_ns()
+        o.gsis(ns_solver=solver, line_mean=lm, max_inner=8, inner_tol=0.0, inner_rtol=0.0, cfl=20.0)
+        o.step(2)
+        out.append(o.frd())
+    assert (out[0] == out[1]).all()
