@@ -103,3 +103,21 @@ def test_bench_time_to_residual_report_shape(cm, monkeypatch):
     # the large case's runs are the 128x512 workload; the learned one loads the closure
     large = [c for c in calls if c[1].startswith("couette-128x512")]
     assert len(large) == 5 and sum(c[4] for c in large) == 1
+
+
+def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
+    import numpy as np
+    import bench
+    calls = []
+
+    def fake(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
+             wall_s=None):
+        calls.append((name, case.name, (gsis or {}).get("line_mean", 0), learned, max_iters))
+        return {"seconds": 1.0, "iterations": max_iters, "residual": 1e-3, "reached": False}, np.zeros(1)
+
+    monkeypatch.setattr(bench, "_ttr_run", fake)
+    out = bench.time_to_residual_sine()
+    assert set(out["runs"]) == {"plain_mixed", "gsis_mixed_line_mean", "gsis_mixed_learned_line_mean",
+                                "gsis_mixed_without_line_mean"}
+    assert all(c[1].startswith("couette-512x512") for c in calls)
+    assert [c[2] for c in calls] == [0, 1, 1, 0] and [c[3] for c in calls] == [False, False, True, False]
