@@ -391,20 +391,22 @@ def time_to_residual_sine():
     """The 512x512 sine case (48^2 on [-5, 5], Kn 0.005, T_w = 1 + 0.1 sin(2 pi x),
     plates +-0.3), mixed precision, upwind order at dt 1e6 with the mass pin:
     the plain iteration for 1000 iterations; the synthetic solve with the
-    line-averaged correction, with and without the learned warm start, for
-    400 outer iterations each; the synthetic solve without the correction for
-    150.  1e-8 is out of reach in minutes here, so these report the residual
+    line-averaged correction and its first two harmonics, with and without
+    the learned warm start, and with the constant mode only, for 400 outer
+    iterations each; the synthetic solve without the correction for 150.  1e-8 is out of reach in minutes here, so these report the residual
     each reaches and the cost of an iteration."""
     from hyb_gb300 import hyb_types as T
     M = T.HYB_PREC_MIXED
     gl2 = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0, inner_rtol=1e-8,
                relax_pct=70)
     glm = dict(gl2, line_mean=1)
+    glh = dict(gl2, line_mean=3)
     out = {}
     for name, g, learned, cap, chunk in (("plain_mixed", None, False, 1000, 50),
-                                         ("gsis_mixed_line_mean", glm, False, 400, 10),
-                                         ("gsis_mixed_learned_line_mean", dict(glm, mlp_warm_after=20,
+                                         ("gsis_mixed_harmonics", glh, False, 400, 10),
+                                         ("gsis_mixed_learned_harmonics", dict(glh, mlp_warm_after=20,
                                                                                mlp_warm_inner=400), True, 400, 10),
+                                         ("gsis_mixed_line_mean", glm, False, 400, 10),
                                          ("gsis_mixed_without_line_mean", gl2, False, 150, 10)):
         c = cases.couette_sine(dt=1.0e6, sweep_order=1, mass_pin=1, precision=M)
         out[name], _ = _ttr_run(name, c, M, g, False, learned, tol=1e-8, max_iters=cap, chunk=chunk)

@@ -71,9 +71,13 @@ struct NsDev {
     double *wface;                                           // wall-face kinetic rho, u, v, T [4][4][mx]
     double *sk;                                              // band moments before the correction [6][nc]
     double *lin;                                             // line-solver scratch [16][nc]
-    int line_mean;                                           // the line-averaged correction (ns_solver 2)
+    int line_mean;                                           // the line-averaged correction (ns_solver 2):
+                                                             // 1 the constant mode, n > 1 also harmonics 1..n-1
     float *lmean;                                            // its rows A, B, C [16], d [4], x [4] and the
                                                              // sequential scratch G [16], g [4], per cell
+    float *lharm;                                            // harmonic rows: S, X [16], rhat [LHARM_MAX][8]
+    float *lhsol;                                            // harmonic solves [LHARM_MAX][cell]: G, g, x
+    int lstride;                                             // cells per region of lmean / lharm / lhsol
     double *d, *uu, *vv, *T, *p, *cc, *amu;
     double *fluxi, *fluxj, *ti_out, *qi_out, *tj_out, *qj_out;
     const double *vol, *si, *sj, *ni1, *ni2, *nj1, *nj2;   // (nx,ny)
@@ -972,6 +976,14 @@ constexpr int PCR_MAX = 512;
 // floats per cell of D.lmean: A, B, C [16], d [4], x [4] (offset 52),
 // G [16] (56), g [4] (72) of the sequential elimination
 constexpr int LMEAN_ROW = 80;
+// harmonics of line_mean above 1: per cell S = mean X_lo + mean X_hi and
+// X = mean X_lo - mean X_hi [16 each], then the Fourier coefficients of Res
+// for h = 1 .. LHARM_MAX [4 complex each]; per harmonic and cell the
+// complex elimination's G [16], g [4] and solution x [4]
+constexpr int LHARM_MAX = 3;
+constexpr int LHARM_ROW = 32 + 8 * LHARM_MAX;
+constexpr int LHSOL_ROW = 48;
+constexpr int LMEAN_FLOATS = LMEAN_ROW + LHARM_ROW + LHARM_MAX * LHSOL_ROW;   // per cell of the line axis
 template <bool MEAN>
 __global__ void __launch_bounds__(PCR_MAX, 1) k_ns_lines_pcr(NsDev D, int col) {
     if (D.ctrl->done) return;
@@ -1092,16 +1104,19 @@ __global__ void __launch_bounds__(PCR_MAX, 1) k_ns_lines_pcr(NsDev D, int col) {
 // the line system; line Gauss-Seidel alone builds that mode up over
 // O((cells across / line length)^2) passes.
 
-// the sum of the two cross-axis neighbour blocks of cell (ln, k), those
-// line_row applies to the neighbouring lines' dU
-__device__ void cross_blocks(const NsDev &D, const LineGeo &G, int ln, int k, float *X) {
+// the two cross-axis neighbour blocks of cell (ln, k), those line_row
+// applies to the neighbouring lines' dU: into XL (lower line) and XH (upper
+// line); XL == XH sums them
+__device__ void cross_blocks(const NsDev &D, const LineGeo &G, int ln, int k, float *XL, float *XH) {
     const bool aj = G.along_j;
     const int i = aj ? ln : k, j = aj ? k : ln;
     const size_t nc = D.nc;
     const float g = (float)D.gamma;
 #pragma unroll
-    for (int q = 0; q < 16; q++) X[q] = 0.f;
+    for (int q = 0; q < 16; q++) { XL[q] = 0.f; XH[q] = 0.f; }
+#pragma unroll
     for (int side = 0; side < 2; side++) {
+        float *X = side == 0 ? XL : XH;
         int q = side == 0 ? ln - 1 : ln + 1;
         if (q < G.n0 || q > G.n1) {
             if (!G.per) continue;
@@ -1139,7 +1154,7 @@ __global__ void __launch_bounds__(LMEAN_THREADS) k_ns_lmean_rows(NsDev D) {
     for (int ln = G.n0 + (int)threadIdx.x; ln <= G.n1; ln += LMEAN_THREADS) {
         float A[16], B[16], C[16], d[4], X[16];
         line_row(D, G, ln, k, A, B, C, d);
-        cross_blocks(D, G, ln, k, X);
+        cross_blocks(D, G, ln, k, X, X);
 #pragma unroll
         for (int q = 0; q < 16; q++) {
             acc[q] += A[q];
@@ -1222,7 +1237,238 @@ __global__ void k_ns_lmean_seq(NsDev D) {
     }
 }
 
+// ---- harmonics h = 1 .. line_mean - 1 across the periodic axis ----------------
+// dU_(l,k) += 2 Re(e^{i t_h (l - n0)} x_k), t_h = 2 pi h / nl, with the
+// line-mean coefficients: the averaged system's diagonal becomes
+// D_h = D_0 + (1 - cos t_h) S + i sin t_h X with S = mean X_lo + mean X_hi,
+// X = mean X_lo - mean X_hi and D_0 the constant mode's (B minus both cross
+// blocks); the along-line blocks stay the means and the right side is the
+// Fourier coefficient mean(e^{-i t_h (l - n0)} Res).  Exact for a harmonic
+// where the coefficients do not vary along the periodic axis.  The
+// antisymmetric part of the cross blocks couples cos to sin, so each
+// harmonic is one complex system.
+
+// harmonics solved: line_mean - 1, at most LHARM_MAX and below nl / 2
+__host__ __device__ inline int lharm_count(int line_mean, int nl) {
+    int h = line_mean - 1;
+    if (h > LHARM_MAX) h = LHARM_MAX;
+    if (h > (nl - 1) / 2) h = (nl - 1) / 2;
+    return h < 0 ? 0 : h;
+}
+// e^{i 2 pi m / nl} for the integer phase m (reduced mod nl first)
+__device__ __forceinline__ float2 unit_phase(long long m, int nl) {
+    const int r = (int)(m % nl);
+    float sn, cs;
+    sincospif(2.f * (float)r / (float)nl, &sn, &cs);
+    return make_float2(cs, sn);
+}
+
+// one CTA per cell of the line axis: S, X and the Fourier coefficients of Res
+__global__ void __launch_bounds__(LMEAN_THREADS) k_ns_lharm_rows(NsDev D) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int k = G.k0 + blockIdx.x;
+    if (k > G.k1) return;
+    const int nl = G.n1 - G.n0 + 1, H = lharm_count(D.line_mean, nl);
+    float acc[LHARM_ROW];
+#pragma unroll
+    for (int q = 0; q < LHARM_ROW; q++) acc[q] = 0.f;
+    for (int ln = G.n0 + (int)threadIdx.x; ln <= G.n1; ln += LMEAN_THREADS) {
+        float XL[16], XH[16];
+        cross_blocks(D, G, ln, k, XL, XH);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            acc[q] += XL[q] + XH[q];
+            acc[16 + q] += XL[q] - XH[q];
+        }
+        const int i = G.along_j ? ln : k, j = G.along_j ? k : ln;
+        const size_t c = c2(D, i, j);
+        float r[4];
+#pragma unroll
+        for (int m = 0; m < 4; m++) r[m] = (float)D.Res[(size_t)m * D.nc + c];
+#pragma unroll
+        for (int h = 1; h <= LHARM_MAX; h++) {
+            if (h > H) break;
+            const float2 e = unit_phase((long long)h * (ln - G.n0), nl);   // e^{+i t}; the coefficient takes e^{-i t}
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                acc[32 + (h - 1) * 8 + 2 * m] += e.x * r[m];
+                acc[32 + (h - 1) * 8 + 2 * m + 1] -= e.y * r[m];
+            }
+        }
+    }
+    __shared__ float red[LMEAN_THREADS / 32][LHARM_ROW];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < LHARM_ROW; q++) {
+        float v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < LHARM_ROW) {
+        float t = 0.f;
+#pragma unroll
+        for (int ww = 0; ww < LMEAN_THREADS / 32; ww++) t += red[ww][threadIdx.x];
+        D.lharm[(size_t)blockIdx.x * LHARM_ROW + threadIdx.x] = t / (float)nl;
+    }
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 crcpf(float2 a) {
+    const float d = 1.f / (a.x * a.x + a.y * a.y);
+    return make_float2(a.x * d, -a.y * d);
+}
+// X = M^-1 B for a complex 4x4 M and K complex columns (row-major),
+// partial pivoting on |re| + |im|, compile-time row indices; M destroyed
+template <int K>
+__device__ __forceinline__ void csolve4f(float2 *M, float2 *B) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int pr = c;
+        float best = fabsf(M[c * 4 + c].x) + fabsf(M[c * 4 + c].y);
+#pragma unroll
+        for (int r = c + 1; r < 4; r++) {
+            const float v = fabsf(M[r * 4 + c].x) + fabsf(M[r * 4 + c].y);
+            if (v > best) { best = v; pr = r; }
+        }
+#pragma unroll
+        for (int r = c + 1; r < 4; r++) {
+            if (r != pr) continue;
+#pragma unroll
+            for (int q = 0; q < 4; q++) { float2 t = M[c * 4 + q]; M[c * 4 + q] = M[r * 4 + q]; M[r * 4 + q] = t; }
+#pragma unroll
+            for (int q = 0; q < K; q++) { float2 t = B[c * K + q]; B[c * K + q] = B[r * K + q]; B[r * K + q] = t; }
+        }
+        const float2 ip = crcpf(M[c * 4 + c]);
+#pragma unroll
+        for (int r = c + 1; r < 4; r++) {
+            const float2 f = cmulf(M[r * 4 + c], ip);
+#pragma unroll
+            for (int q = c; q < 4; q++) {
+                const float2 t = cmulf(f, M[c * 4 + q]);
+                M[r * 4 + q].x -= t.x;
+                M[r * 4 + q].y -= t.y;
+            }
+#pragma unroll
+            for (int q = 0; q < K; q++) {
+                const float2 t = cmulf(f, B[c * K + q]);
+                B[r * K + q].x -= t.x;
+                B[r * K + q].y -= t.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 3; c >= 0; c--) {
+        const float2 ip = crcpf(M[c * 4 + c]);
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            float2 t = B[c * K + q];
+#pragma unroll
+            for (int r = c + 1; r < 4; r++) {
+                const float2 u = cmulf(M[c * 4 + r], B[r * K + q]);
+                t.x -= u.x;
+                t.y -= u.y;
+            }
+            B[c * K + q] = cmulf(t, ip);
+        }
+    }
+}
+
+// one thread per harmonic: complex block-tridiagonal elimination along the
+// line axis (A x_{k-1} + B_h x_k + C x_{k+1} = rhat_h, A, C the constant
+// mode's real rows; x_{k-1} = g_{k-1} + G_{k-1} x_k)
+__global__ void k_ns_lharm_seq(NsDev D) {
+    if (D.ctrl->done) return;
+    const LineGeo G = line_geo(D);
+    const int nl = G.n1 - G.n0 + 1, n = G.k1 - G.k0 + 1, H = lharm_count(D.line_mean, nl);
+    const int h = (int)threadIdx.x + 1;
+    if (h > H) return;
+    float sn, cs;
+    sincospif(2.f * (float)h / (float)nl, &sn, &cs);
+    const float ct = 1.f - cs;
+    float *sol = D.lhsol + (size_t)(h - 1) * D.lstride * LHSOL_ROW;
+    for (int k = 0; k < n; k++) {
+        const float *row = D.lmean + (size_t)k * LMEAN_ROW, *hr = D.lharm + (size_t)k * LHARM_ROW;
+        float *sk = sol + (size_t)k * LHSOL_ROW;
+        float2 M[16], Bm[20];
+#pragma unroll
+        for (int q = 0; q < 16; q++) M[q] = make_float2(row[16 + q] + ct * hr[q], sn * hr[16 + q]);
+        float2 r[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) r[a] = make_float2(hr[32 + (h - 1) * 8 + 2 * a], hr[32 + (h - 1) * 8 + 2 * a + 1]);
+        if (k > 0) {   // M += A G_{k-1}; r -= A g_{k-1} (A real)
+            const float *pk = sk - LHSOL_ROW;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float tx = 0.f, ty = 0.f;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        tx += row[a * 4 + m] * pk[2 * (m * 4 + q)];
+                        ty += row[a * 4 + m] * pk[2 * (m * 4 + q) + 1];
+                    }
+                    M[a * 4 + q].x += tx;
+                    M[a * 4 + q].y += ty;
+                }
+                float tx = 0.f, ty = 0.f;
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    tx += row[a * 4 + m] * pk[32 + 2 * m];
+                    ty += row[a * 4 + m] * pk[32 + 2 * m + 1];
+                }
+                r[a].x -= tx;
+                r[a].y -= ty;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) Bm[a * 5 + q] = make_float2(-row[32 + a * 4 + q], 0.f);
+            Bm[a * 5 + 4] = r[a];
+        }
+        csolve4f<5>(M, Bm);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                sk[2 * (a * 4 + q)] = Bm[a * 5 + q].x;
+                sk[2 * (a * 4 + q) + 1] = Bm[a * 5 + q].y;
+            }
+            sk[32 + 2 * a] = Bm[a * 5 + 4].x;
+            sk[32 + 2 * a + 1] = Bm[a * 5 + 4].y;
+        }
+    }
+    float2 nxt[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    for (int k = n - 1; k >= 0; k--) {
+        float *sk = sol + (size_t)k * LHSOL_ROW;
+        float2 x[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            float2 t = make_float2(sk[32 + 2 * a], sk[32 + 2 * a + 1]);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float2 u = cmulf(make_float2(sk[2 * (a * 4 + q)], sk[2 * (a * 4 + q) + 1]), nxt[q]);
+                t.x += u.x;
+                t.y += u.y;
+            }
+            x[a] = t;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            sk[40 + 2 * a] = x[a].x;
+            sk[40 + 2 * a + 1] = x[a].y;
+            nxt[a] = x[a];
+        }
+    }
+}
+
 // dU of every band cell from the solution of its position on the line axis
+// (and the harmonics' contributions at its line)
 __global__ void k_ns_lmean_fill(NsDev D) {
     if (D.ctrl->done) return;
     const int bw = D.ihi - D.ilo + 1, bh = D.jhi - D.jlo + 1;
@@ -1230,10 +1476,19 @@ __global__ void k_ns_lmean_fill(NsDev D) {
     if (t >= bw * bh) return;
     const int i = D.ilo + t % bw, j = D.jlo + t / bw;
     const LineGeo G = line_geo(D);
-    const float *x = D.lmean + (size_t)((G.along_j ? j : i) - G.k0) * LMEAN_ROW + 52;
+    const int k = (G.along_j ? j : i) - G.k0, ln = (G.along_j ? i : j) - G.n0;
+    const float *x = D.lmean + (size_t)k * LMEAN_ROW + 52;
+    float u[4] = {x[0], x[1], x[2], x[3]};
+    const int nl = G.n1 - G.n0 + 1, H = lharm_count(D.line_mean, nl);
+    for (int h = 1; h <= H; h++) {
+        const float *xh = D.lhsol + ((size_t)(h - 1) * D.lstride + k) * LHSOL_ROW + 40;
+        const float2 e = unit_phase((long long)h * ln, nl);
+#pragma unroll
+        for (int m = 0; m < 4; m++) u[m] += 2.f * (e.x * xh[2 * m] - e.y * xh[2 * m + 1]);
+    }
     const size_t c = c2(D, i, j);
 #pragma unroll
-    for (int m = 0; m < 4; m++) D.dU[(size_t)m * D.nc + c] = (double)x[m];
+    for (int m = 0; m < 4; m++) D.dU[(size_t)m * D.nc + c] = (double)u[m];
 }
 
 // lines longer than PCR_MAX cells: block-tridiagonal elimination, one
@@ -1763,12 +2018,12 @@ static void ns_band(const hyb_ctx *ctx, NsDev &D) {
     if (D.pery) { D.jlo = 1; D.jhi = D.ny - 1; } else { D.jlo = e; D.jhi = D.ny - e; }
     D.wall_band = ctx->gsis.wall_band != 0;
     D.relax = ctx->gsis.relax_pct > 0 ? ctx->gsis.relax_pct / 100.0 : 1.0;
-    D.line_mean = ctx->gsis.line_mean != 0;
+    D.line_mean = ctx->gsis.line_mean;
 }
 
 int ns_create(hyb_ctx *ctx) {
     if (ctx->gsis.ns_solver < 0 || ctx->gsis.ns_solver > 2 || ctx->gsis.relax_pct < 0 ||
-        ctx->gsis.relax_pct > 100 || ctx->gsis.line_mean < 0 || ctx->gsis.line_mean > 1 ||
+        ctx->gsis.relax_pct > 100 || ctx->gsis.line_mean < 0 || ctx->gsis.line_mean > 1 + LHARM_MAX ||
         (ctx->gsis.line_mean && ctx->gsis.ns_solver != 2))
         return HYB_ERR_INVALID;
     if (ctx->ns) {   // reconfigured: re-capture with the new parameters
@@ -1803,7 +2058,7 @@ int ns_create(hyb_ctx *ctx) {
     // see the pointer carve below; the wall-face states follow the last array
     const int ncomp = 4 * 5 + 1 * 5 + 7 + 4 + 4 + 4 + 2 + 4 + 2 + 16 + 6;
     const size_t nwf = (size_t)16 * (D.nx > D.ny ? D.nx : D.ny);
-    const size_t nlm = (size_t)LMEAN_ROW / 2 * (D.nx > D.ny ? D.nx : D.ny);   // doubles
+    const size_t nlm = (size_t)LMEAN_FLOATS / 2 * (D.nx > D.ny ? D.nx : D.ny);   // doubles
     const size_t ncell = (size_t)ctx->Nb * ctx->PA;
     const size_t fbytes = (size_t)ctx->nv * 2 * ncell * ctx->real_size;
     if (cudaMalloc(&ctx->d_rhs_gsis, fbytes) != cudaSuccess) {
@@ -1836,7 +2091,11 @@ int ns_create(hyb_ctx *ctx) {
     D.lin = h; h += 16 * nc;
     D.sk = h; h += 6 * nc;
     D.wface = h; h += nwf;  // [4 faces][rho u v T][max(nx, ny)]
-    D.lmean = reinterpret_cast<float *>(h); h += nlm;   // [max(nx, ny)][LMEAN_ROW] floats
+    D.lstride = D.nx > D.ny ? D.nx : D.ny;
+    D.lmean = reinterpret_cast<float *>(h);             // [lstride][LMEAN_ROW] floats
+    D.lharm = D.lmean + (size_t)D.lstride * LMEAN_ROW;  // [lstride][LHARM_ROW]
+    D.lhsol = D.lharm + (size_t)D.lstride * LHARM_ROW;  // [LHARM_MAX][lstride][LHSOL_ROW]
+    h += nlm;
     const size_t nm = (size_t)ctx->nx * ctx->ny;
     if (cudaMalloc((void **)&st->geo, 7 * nm * sizeof(double)) != cudaSuccess) {
         cudaFree(st->buf);
@@ -1959,6 +2218,10 @@ static void inner_iteration(hyb_ctx *ctx, const NsDev &D) {
                 k_ns_lines_pcr<true><<<1, PCR_MAX, (size_t)68 * nk * sizeof(float), s>>>(D, 0);
             else
                 k_ns_lmean_seq<<<1, 1, 0, s>>>(D);
+            if (lharm_count(D.line_mean, nl) > 0) {
+                k_ns_lharm_rows<<<nk, LMEAN_THREADS, 0, s>>>(D);
+                k_ns_lharm_seq<<<1, 32, 0, s>>>(D);
+            }
             k_ns_lmean_fill<<<(nband + bs - 1) / bs, bs, 0, s>>>(D);
         }
         const int order[4] = {0, 1, 2, 0};
@@ -1991,7 +2254,8 @@ static int inner_launches(const hyb_ctx *ctx, const NsDev &D) {
         const int nl = aj ? D.ihi - D.ilo + 1 : D.jhi - D.jlo + 1;
         const bool per = aj ? D.perx != 0 : D.pery != 0;
         lines = 2 * (lines_of_colour(nl, per, 0) > 0) + (lines_of_colour(nl, per, 1) > 0) +
-                (lines_of_colour(nl, per, 2) > 0) + (D.line_mean && per ? 3 : 0);
+                (lines_of_colour(nl, per, 2) > 0) + (D.line_mean && per ? 3 : 0) +
+                (D.line_mean && per && lharm_count(D.line_mean, nl) > 0 ? 2 : 0);
     }
     const int solver = ctx->gsis.ns_solver == 2 ? lines : (ctx->gsis.ns_solver == 1 ? 2 : 4);
     return 6 + solver + (D.mlp_on ? 2 : 0) + (D.wall_band ? 1 : 0);

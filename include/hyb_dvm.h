@@ -193,7 +193,11 @@ typedef struct hyb_gsis_params {
                                and before the line passes, the system of the
                                correction that is constant across the
                                periodic axis (the line system averaged over
-                               the lines); no counterpart in the reference  */
+                               the lines); n = 2..4 adds the harmonics
+                               1..n-1 across that axis, each one complex
+                               averaged system with the line-mean
+                               coefficients; no counterpart in the
+                               reference                                    */
 } hyb_gsis_params;
 
 typedef struct hyb_ctx hyb_ctx;

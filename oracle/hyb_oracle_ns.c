@@ -42,6 +42,7 @@
  */
 #include "hyb_oracle_impl.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -856,6 +857,169 @@ static void ns_line_mean(orc *o, int along_j, int n0, int n1, int k0, int k1, do
     }
 }
 
+/* the harmonics h = 1 .. line_mean - 1 across the periodic axis (line_mean
+ * above 1, no counterpart in the reference).  dU_(l,k) = 2 Re(e^{i t_h l}
+ * e_k), t_h = 2 pi h / nl, with the line-mean coefficients: the blocks of
+ * the averaged system become D_h = mean(B) - mean(X_lo) e^{-i t_h} -
+ * mean(X_hi) e^{i t_h} = D_0 + (1 - cos t_h) (mean X_lo + mean X_hi) +
+ * i sin t_h (mean X_lo - mean X_hi), the along-line blocks stay the means,
+ * and the right side is the Fourier coefficient mean(e^{-i t_h l} Res).
+ * Where the coefficients do not vary along the periodic axis this is exact
+ * for the harmonic.  The antisymmetric (convective, acoustic) part of the
+ * cross-axis blocks couples cos(t_h l) to sin(t_h l), so the pair is solved
+ * as one complex system.  The result is added to dU after the constant
+ * mode. */
+static void csolve4(double complex *M, double complex *B, int kc)
+{
+    for (int c = 0; c < 4; c++) {
+        int pr = c;
+        for (int r = c + 1; r < 4; r++)
+            if (cabs(M[r * 4 + c]) > cabs(M[pr * 4 + c])) pr = r;
+        if (pr != c) {
+            for (int q = 0; q < 4; q++) { double complex t = M[c * 4 + q]; M[c * 4 + q] = M[pr * 4 + q]; M[pr * 4 + q] = t; }
+            for (int q = 0; q < kc; q++) { double complex t = B[c * kc + q]; B[c * kc + q] = B[pr * kc + q]; B[pr * kc + q] = t; }
+        }
+        const double complex ip = 1.0 / M[c * 4 + c];
+        for (int r = c + 1; r < 4; r++) {
+            const double complex f = M[r * 4 + c] * ip;
+            for (int q = c; q < 4; q++) M[r * 4 + q] -= f * M[c * 4 + q];
+            for (int q = 0; q < kc; q++) B[r * kc + q] -= f * B[c * kc + q];
+        }
+    }
+    for (int c = 3; c >= 0; c--) {
+        const double complex ip = 1.0 / M[c * 4 + c];
+        for (int q = 0; q < kc; q++) {
+            double complex t = B[c * kc + q];
+            for (int r = c + 1; r < 4; r++) t -= M[c * 4 + r] * B[r * kc + q];
+            B[c * kc + q] = t * ip;
+        }
+    }
+}
+
+static int ns_line_harmonics(orc *o, int along_j, int n0, int n1, int k0, int k1)
+{
+    struct orc_ns *ns = o->ns;
+    const int nl = n1 - n0 + 1, nk = k1 - k0 + 1, H = o->gsis.line_mean - 1;
+    const double inl = 1.0 / nl;
+    /* per cell of the line axis: D_0 (the constant mode's diagonal), the
+     * lower and upper blocks, S = mean X_lo + mean X_hi, A = mean X_lo -
+     * mean X_hi */
+    double *D0 = calloc((size_t)nk * 16, sizeof(double)), *Lo = calloc((size_t)nk * 16, sizeof(double));
+    double *Up = calloc((size_t)nk * 16, sizeof(double)), *Sx = calloc((size_t)nk * 16, sizeof(double));
+    double *Ax = calloc((size_t)nk * 16, sizeof(double));
+    double complex *G = calloc((size_t)nk * 16, sizeof(double complex)), *g = calloc((size_t)nk * 4, sizeof(double complex));
+    double complex *rh = calloc((size_t)nk * 4, sizeof(double complex));
+    if (!D0 || !Lo || !Up || !Sx || !Ax || !G || !g || !rh) {
+        free(D0); free(Lo); free(Up); free(Sx); free(Ax); free(G); free(g); free(rh);
+        return HYB_ERR_NOMEM;
+    }
+    for (int k = k0; k <= k1; k++) {
+        const size_t o16 = (size_t)(k - k0) * 16;
+        double B[16];
+        const int wlo = o->gsis.wall_band && k == k0 && o->bc[along_j ? 1 : 0] == HYB_BC_WALL;
+        const int whi = o->gsis.wall_band && k == k1 && o->bc[along_j ? 3 : 2] == HYB_BC_WALL;
+        for (int ln = n0; ln <= n1; ln++) {
+            const int i = along_j ? ln : k, j = along_j ? k : ln;
+            const size_t c = C2(o, i, j);
+            const double alfa = o->vol[MI(o, i, j)] / ns->dt[c] + ns->Lci[c] + ns->Lcj[c] +
+                                2.0 * (ns->Lvi[c] + ns->Lvj[c]);
+            for (int q = 0; q < 4; q++) D0[o16 + q * 4 + q] += alfa * inl;
+            const int lo = ln > n0 ? ln - 1 : n1, hi = ln < n1 ? ln + 1 : n0;
+            const size_t clo = along_j ? C2(o, lo, j) : C2(o, i, lo), chi = along_j ? C2(o, hi, j) : C2(o, i, hi);
+            const double m1 = along_j ? o->ni1[MI(o, i, j)] : o->nj1[MI(o, i, j)];
+            const double m2 = along_j ? o->ni2[MI(o, i, j)] : o->nj2[MI(o, i, j)];
+            const double slo = along_j ? o->si[MI(o, i, j)] : o->sj[MI(o, i, j)];
+            const double shi = along_j ? o->si[MI(o, i + 1, j)] : o->sj[MI(o, i, j + 1)];
+            nb_block(o, clo, clo, along_j, m1, m2, slo, 0.5, B);
+            for (int q = 0; q < 16; q++) {
+                D0[o16 + q] -= B[q] * inl;
+                Sx[o16 + q] += B[q] * inl;
+                Ax[o16 + q] += B[q] * inl;
+            }
+            nb_block(o, chi, chi, along_j, m1, m2, shi, -0.5, B);
+            for (int q = 0; q < 16; q++) {
+                D0[o16 + q] -= B[q] * inl;
+                Sx[o16 + q] += B[q] * inl;
+                Ax[o16 + q] -= B[q] * inl;
+            }
+            const double n1f = along_j ? o->nj1[MI(o, i, j)] : o->ni1[MI(o, i, j)];
+            const double n2f = along_j ? o->nj2[MI(o, i, j)] : o->ni2[MI(o, i, j)];
+            if (k > k0 || wlo) {
+                const size_t cn = along_j ? C2(o, i, j - 1) : C2(o, i - 1, j);
+                const double sf = along_j ? o->sj[MI(o, i, j)] : o->si[MI(o, i, j)];
+                nb_block(o, cn, wlo ? c : cn, !along_j, n1f, n2f, sf, 0.5, B);
+                double *T = wlo ? D0 : Lo;
+                for (int q = 0; q < 16; q++) T[o16 + q] += B[q] * inl;
+            }
+            if (k < k1 || whi) {
+                const size_t cn = along_j ? C2(o, i, j + 1) : C2(o, i + 1, j);
+                const double sf = along_j ? o->sj[MI(o, i, j + 1)] : o->si[MI(o, i + 1, j)];
+                nb_block(o, cn, whi ? c : cn, !along_j, n1f, n2f, sf, -0.5, B);
+                double *T = whi ? D0 : Up;
+                for (int q = 0; q < 16; q++) T[o16 + q] += B[q] * inl;
+            }
+        }
+    }
+    for (int h = 1; h <= H && 2 * h < nl; h++) {
+        const double th = 2.0 * PI * h / nl, ct = 1.0 - cos(th), st = sin(th);
+        for (int k = k0; k <= k1; k++) {
+            double complex *r = rh + (size_t)(k - k0) * 4;
+            for (int m = 0; m < 4; m++) r[m] = 0.0;
+            for (int ln = n0; ln <= n1; ln++) {
+                const int i = along_j ? ln : k, j = along_j ? k : ln;
+                const double ph = th * (ln - n0);
+                const double complex e = cos(ph) - I * sin(ph);
+                for (int m = 0; m < 4; m++) r[m] += e * A4(ns->Res, m, C2(o, i, j)) * inl;
+            }
+        }
+        for (int k = k0; k <= k1; k++) {
+            const size_t o16 = (size_t)(k - k0) * 16;
+            double complex M[16], Bm[20];
+            for (int q = 0; q < 16; q++) M[q] = D0[o16 + q] + ct * Sx[o16 + q] + I * (st * Ax[o16 + q]);
+            for (int a = 0; a < 4; a++) {
+                for (int q = 0; q < 4; q++) Bm[a * 5 + q] = Up[o16 + a * 4 + q];
+                Bm[a * 5 + 4] = rh[(size_t)(k - k0) * 4 + a];
+            }
+            if (k > k0) {   /* M -= L G_{k-1}; r += L g_{k-1} */
+                const double complex *Gp = G + o16 - 16, *gp = g + (size_t)(k - 1 - k0) * 4;
+                for (int a = 0; a < 4; a++) {
+                    for (int q = 0; q < 4; q++) {
+                        double complex t = 0.0;
+                        for (int m = 0; m < 4; m++) t += Lo[o16 + a * 4 + m] * Gp[m * 4 + q];
+                        M[a * 4 + q] -= t;
+                    }
+                    double complex t = 0.0;
+                    for (int m = 0; m < 4; m++) t += Lo[o16 + a * 4 + m] * gp[m];
+                    Bm[a * 5 + 4] += t;
+                }
+            }
+            csolve4(M, Bm, 5);
+            for (int a = 0; a < 4; a++) {
+                for (int q = 0; q < 4; q++) G[o16 + a * 4 + q] = Bm[a * 5 + q];
+                g[(size_t)(k - k0) * 4 + a] = Bm[a * 5 + 4];
+            }
+        }
+        double complex nxt[4] = {0, 0, 0, 0};
+        for (int k = k1; k >= k0; k--) {
+            double complex d[4];
+            for (int a = 0; a < 4; a++) {
+                double complex t = g[(size_t)(k - k0) * 4 + a];
+                for (int q = 0; q < 4; q++) t += G[(size_t)(k - k0) * 16 + a * 4 + q] * nxt[q];
+                d[a] = t;
+            }
+            for (int ln = n0; ln <= n1; ln++) {
+                const int i = along_j ? ln : k, j = along_j ? k : ln;
+                const double ph = th * (ln - n0);
+                for (int a = 0; a < 4; a++)
+                    A4(ns->dU, a, C2(o, i, j)) += 2.0 * (cos(ph) * creal(d[a]) - sin(ph) * cimag(d[a]));
+            }
+            for (int a = 0; a < 4; a++) nxt[a] = d[a];
+        }
+    }
+    free(D0); free(Lo); free(Up); free(Sx); free(Ax); free(G); free(g); free(rh);
+    return HYB_OK;
+}
+
 static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
 {
     struct orc_ns *ns = o->ns;
@@ -868,7 +1032,13 @@ static int ns_lines(orc *o, int ilo, int ihi, int jlo, int jhi)
     double *G = malloc((size_t)nk * 16 * sizeof(double)), *gv = malloc((size_t)nk * 4 * sizeof(double));
     if (!G || !gv) { free(G); free(gv); return HYB_ERR_NOMEM; }
     memset(ns->dU, 0, 4 * ns->nc * sizeof(double));
-    if (o->gsis.line_mean && per) ns_line_mean(o, along_j, n0, n1, k0, k1, G, gv);
+    if (o->gsis.line_mean && per) {
+        ns_line_mean(o, along_j, n0, n1, k0, k1, G, gv);
+        if (o->gsis.line_mean > 1) {
+            const int rc = ns_line_harmonics(o, along_j, n0, n1, k0, k1);
+            if (rc) { free(G); free(gv); return rc; }
+        }
+    }
     /* red-black line Gauss-Seidel: colour 0 (even offsets from n0), 1 (odd),
      * 2 (the last line of an odd periodic count, which meets line n0 across
      * the seam), then colour 0 again; a line takes the current dU of its

@@ -117,7 +117,7 @@ def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
 
     monkeypatch.setattr(bench, "_ttr_run", fake)
     out = bench.time_to_residual_sine()
-    assert set(out["runs"]) == {"plain_mixed", "gsis_mixed_line_mean", "gsis_mixed_learned_line_mean",
-                                "gsis_mixed_without_line_mean"}
+    assert set(out["runs"]) == {"plain_mixed", "gsis_mixed_harmonics", "gsis_mixed_learned_harmonics",
+                                "gsis_mixed_line_mean", "gsis_mixed_without_line_mean"}
     assert all(c[1].startswith("couette-512x512") for c in calls)
-    assert [c[2] for c in calls] == [0, 1, 1, 0] and [c[3] for c in calls] == [False, False, True, False]
+    assert [c[2] for c in calls] == [0, 3, 3, 1, 0] and [c[3] for c in calls] == [False, False, True, False, False]

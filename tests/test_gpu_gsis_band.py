@@ -140,14 +140,21 @@ def _line_mean_case(cases_mod, kind, **kw):
     return cases_mod.couette_small(ncx=6, ncy=520, nvx=16, nvy=16, **kw)
 
 
-@pytest.mark.parametrize("kind", ["along_j", "along_i", "long"])
-def test_line_mean_matches_oracle(cases_mod, kind):
+@pytest.mark.parametrize("line_mean", [1, 3])
+@pytest.mark.parametrize("kind", ["along_j", "along_i", "long", "sine"])
+def test_line_mean_matches_oracle(cases_mod, kind, line_mean):
     """line_mean: before the colour passes of each inner iteration, the
     line system averaged over the lines is solved and copied to every line;
-    GPU (FP32 elimination, FP64 residual and update) against the oracle's
-    FP64 restatement after three outer iterations."""
-    c = _line_mean_case(cases_mod, kind, dt=1.0e6, sweep_order=1, mass_pin=1)
-    g, o = _pair(c, 0, wall_band=1, correct_f=1, ns_solver=2, line_mean=1, cfl=100.0, **FIXED)
+    line_mean 3 adds the first two harmonics across the periodic axis, each
+    a complex averaged system.  GPU (FP32 elimination, FP64 residual and
+    update) against the oracle's FP64 restatement after three outer
+    iterations."""
+    if kind == "sine":
+        c = _shape(cases_mod, "sine", dt=1.0e6, sweep_order=1, mass_pin=1)
+    else:
+        c = _line_mean_case(cases_mod, kind, dt=1.0e6, sweep_order=1, mass_pin=1)
+    cfl = 20.0 if kind == "sine" else 100.0      # at CFL 100 the sine case's NS state leaves the range
+    g, o = _pair(c, 0, wall_band=1, correct_f=1, ns_solver=2, line_mean=line_mean, cfl=cfl, **FIXED)
     for _ in range(3):
         g.step(1)
         o.step(1)
@@ -161,6 +168,9 @@ def test_line_mean_needs_the_line_solver(cases_mod):
     s = abi.Solver(c, precision=0)
     with pytest.raises(abi.HybError) as e:
         s.gsis(ns_solver=0, line_mean=1, **FIXED)
+    assert e.value.rc == T.HYB_ERR_INVALID
+    with pytest.raises(abi.HybError) as e:     # at most three harmonics
+        s.gsis(ns_solver=2, line_mean=5, **FIXED)
     assert e.value.rc == T.HYB_ERR_INVALID
     s.close()
 
