@@ -111,13 +111,74 @@ def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
     calls = []
 
     def fake(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
-             wall_s=None):
+             wall_s=None, handover_below=None):
         calls.append((name, case.name, (gsis or {}).get("line_mean", 0), learned, max_iters))
         return {"seconds": 1.0, "iterations": max_iters, "residual": 1e-3, "reached": False}, np.zeros(1)
 
     monkeypatch.setattr(bench, "_ttr_run", fake)
     out = bench.time_to_residual_sine()
     assert set(out["runs"]) == {"plain_mixed", "gsis_mixed_harmonics", "gsis_mixed_learned_harmonics",
-                                "gsis_mixed_line_mean", "gsis_mixed_without_line_mean"}
+                                "gsis_mixed_line_mean", "gsis_mixed_without_line_mean",
+                                "gsis_mixed_harmonics_to_fp64_then_plain"}
     assert all(c[1].startswith("couette-512x512") for c in calls)
-    assert [c[2] for c in calls] == [0, 3, 3, 1, 0] and [c[3] for c in calls] == [False, False, True, False, False]
+    assert [c[2] for c in calls] == [0, 3, 3, 1, 0, 3]
+    assert [c[3] for c in calls] == [False, False, True, False, False, False]
+
+
+class _FakeSolver:
+    """Stands in for abi.Solver in the time-to-residual runner: the residual
+    falls by 0.7 per outer iteration to a floor of 5e-8 while the synthetic
+    solve is on, and by 0.95 per iteration below it once it is off."""
+
+    def __init__(self, case, precision=0):
+        self.case, self.res, self.gsis_on, self.calls = case, 1.0, False, []
+
+    def init_maxwellian(self):
+        pass
+
+    def attach_mlp(self, m):
+        pass
+
+    def gsis(self, **kw):
+        self.gsis_on = kw.get("enable", 1) == 1
+        self.calls.append(("gsis", self.gsis_on))
+
+    def set_precision(self, p):
+        self.calls.append(("precision", p))
+
+    def step(self, n):
+        for _ in range(n):
+            self.res = max(5e-8, 0.7 * self.res) if self.gsis_on else 0.95 * self.res
+        return {"max_rms": self.res}
+
+    def moments(self):
+        import numpy as np
+        c = self.case
+        return np.zeros((c.ny + 7) * (c.nx + 7) * 11), None
+
+    def gsis_skipped(self):
+        return 0
+
+    def close(self):
+        pass
+
+
+def test_bench_hands_over_to_the_plain_iteration_at_the_synthetic_floor(cm, monkeypatch):
+    import bench
+    from hyb_gb300 import hyb_types as T
+    made = []
+
+    def make(case, precision=0):
+        made.append(_FakeSolver(case, precision))
+        return made[-1]
+
+    monkeypatch.setattr(bench.abi, "Solver", make)
+    c = cm.couette_small(dt=1.0e6, sweep_order=1, mass_pin=1)
+    g = dict(ns_solver=2, line_mean=3)
+    out, _ = bench._ttr_run("x", c, T.HYB_PREC_FP64, g, False, False, tol=1e-8, max_iters=2000, chunk=10,
+                            handover_below=1e-6)
+    assert out["reached"] and out["plain_from_iteration"] is not None
+    assert ("gsis", False) in made[-1].calls
+    # without the hand-over the run stays on the floor
+    out2, _ = bench._ttr_run("x", c, T.HYB_PREC_FP64, g, False, False, tol=1e-8, max_iters=300, chunk=10)
+    assert not out2["reached"] and "plain_from_iteration" not in out2
