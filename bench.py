@@ -265,19 +265,21 @@ def run_reference(args, world, rank):
 
 
 def _ttr_run(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
-             wall_s=None, handover_below=None):
+             wall_s=None, finish_below=None, finish_gsis=None):
     """One run to max RMS residual <= tol (DETFP_res): device-synchronised
     wall clock around the hyb_step calls, the residual read every `chunk`
     outer iterations.  promote: a mixed run continues in FP64 on the device
     (hyb_set_precision) once its FP32 residual stops falling.  An FP32 run
     without promotion that has not improved for 1000 iterations below 1e-4
     sits on its rounding floor and is stopped.  wall_s caps the wall time.
-    handover_below: a synthetic-solve run whose residual, below this value,
-    has fallen by less than 10 % over the last three checkpoints switches
-    the synthetic solve off (hyb_gsis_configure, enable 0) and finishes with
-    the plain kinetic iteration: the coupled iteration can settle on a fixed
-    point of its own a little off the kinetic one, where its residual stops
-    falling while the plain iteration's keeps falling."""
+    finish_below, finish_gsis: a synthetic-solve run whose residual, below
+    finish_below, has fallen by less than 10 % over the last three
+    checkpoints (and, with promote, after the promotion) is reconfigured
+    with finish_gsis (hyb_gsis_configure; {"enable": 0} for the plain
+    iteration).  The coupled iteration can settle on a fixed point of its
+    own a little off the kinetic one: with the distribution correction on,
+    its residual stops falling there, and it falls again once only the
+    moments are corrected."""
     from hyb_gb300 import closure, hyb_types as T
     s = abi.Solver(case, precision=prec)
     s.init_maxwellian()
@@ -286,7 +288,7 @@ def _ttr_run(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8
             s.attach_mlp(closure.load())
         s.gsis(**gsis)
     it, r, prev, promoted, best, best_it, stalled = 0, None, None, None, None, 0, False
-    handed = None
+    finished = None
     hist = []
     t0 = time.perf_counter()
     while it < max_iters:
@@ -306,10 +308,10 @@ def _ttr_run(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8
         if promote and promoted is None and prev is not None and res < 1e-3 and res > 0.9 * prev:
             s.set_precision(T.HYB_PREC_FP64)
             promoted = it
-        elif (handover_below is not None and gsis is not None and handed is None and res < handover_below
+        elif (finish_below is not None and gsis is not None and finished is None and res < finish_below
               and (promoted is not None or not promote) and len(hist) > 3 and res > 0.9 * hist[-4][1]):
-            s.gsis(enable=0)
-            handed = it
+            s.gsis(**finish_gsis)
+            finished = it
         prev = res
     el = time.perf_counter() - t0
     S = s.moments()[0].reshape(case.ny + 7, case.nx + 7, 11)[4:4 + case.ny - 1, 4:4 + case.nx - 1, :4]
@@ -318,8 +320,8 @@ def _ttr_run(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8
            "precision": "mixed" if prec == T.HYB_PREC_MIXED else "fp64", "history": hist}
     if promote:
         out["fp64_from_iteration"] = promoted
-    if handover_below is not None:
-        out["plain_from_iteration"] = handed
+    if finish_below is not None:
+        out["finish_from_iteration"] = finished
     if stalled:
         out["stalled_on_fp32_floor"] = True
     if gsis is not None:
@@ -407,9 +409,10 @@ def time_to_residual_sine():
     line-averaged correction and its first two harmonics, with and without
     the learned warm start, and with the constant mode only, for 400 outer
     iterations each; the synthetic solve without the correction for 150; and
-    the synthetic solve with the harmonics promoted to FP64 at its FP32
-    floor, handed over to the plain iteration at its own floor, to 1e-8
-    within 1000 outer iterations and 300 s.  The mixed runs stop on their
+    the synthetic solve with the harmonics and the unlimited NND stencil,
+    promoted to FP64 at its FP32 floor and reconfigured to correct the
+    moments only at its own floor, to 1e-8 within 1000 outer iterations and
+    300 s.  The mixed runs stop on their
     FP32 floor, so they report the residual each reaches and the cost of an
     iteration."""
     from hyb_gb300 import hyb_types as T
@@ -418,6 +421,9 @@ def time_to_residual_sine():
                relax_pct=70)
     glm = dict(gl2, line_mean=1)
     glh = dict(gl2, line_mean=3)
+    # the finishing run: the unlimited NND stencil in the synthetic equation,
+    # and the moments-only correction once the coupled iteration stalls
+    glf = dict(glh, ns_scheme=2)
     out = {}
     # (name, synthetic solve, learned, outer-iteration cap, chunk, promote to FP64 and hand over to the
     # plain iteration at its floor)
@@ -427,10 +433,11 @@ def time_to_residual_sine():
             ("gsis_mixed_learned_harmonics", dict(glh, mlp_warm_after=20, mlp_warm_inner=400), True, 400, 10, False),
             ("gsis_mixed_line_mean", glm, False, 400, 10, False),
             ("gsis_mixed_without_line_mean", gl2, False, 150, 10, False),
-            ("gsis_mixed_harmonics_to_fp64_then_plain", glh, False, 1000, 10, True)):
+            ("gsis_mixed_harmonics_to_fp64_then_moments_only", glf, False, 1000, 10, True)):
         c = cases.couette_sine(dt=1.0e6, sweep_order=1, mass_pin=1, precision=M)
         out[name], _ = _ttr_run(name, c, M, g, finish, learned, tol=1e-8, max_iters=cap, chunk=chunk,
-                                wall_s=300.0 if finish else None, handover_below=1e-6 if finish else None)
+                                wall_s=300.0 if finish else None, finish_below=1e-6 if finish else None,
+                                finish_gsis=dict(g, correct_f=0) if finish else None)
     return {"workload": "couette-512x512-nv48-kn0.005-sine, upwind order dt 1e6, mass pin", "runs": out}
 
 

@@ -111,7 +111,7 @@ def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
     calls = []
 
     def fake(name, case, prec, gsis=None, promote=False, learned=False, tol=1e-8, max_iters=8000, chunk=50,
-             wall_s=None, handover_below=None):
+             wall_s=None, finish_below=None, finish_gsis=None):
         calls.append((name, case.name, (gsis or {}).get("line_mean", 0), learned, max_iters))
         return {"seconds": 1.0, "iterations": max_iters, "residual": 1e-3, "reached": False}, np.zeros(1)
 
@@ -119,7 +119,7 @@ def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
     out = bench.time_to_residual_sine()
     assert set(out["runs"]) == {"plain_mixed", "gsis_mixed_harmonics", "gsis_mixed_learned_harmonics",
                                 "gsis_mixed_line_mean", "gsis_mixed_without_line_mean",
-                                "gsis_mixed_harmonics_to_fp64_then_plain"}
+                                "gsis_mixed_harmonics_to_fp64_then_moments_only"}
     assert all(c[1].startswith("couette-512x512") for c in calls)
     assert [c[2] for c in calls] == [0, 3, 3, 1, 0, 3]
     assert [c[3] for c in calls] == [False, False, True, False, False, False]
@@ -128,10 +128,11 @@ def test_bench_time_to_residual_sine_report_shape(cm, monkeypatch):
 class _FakeSolver:
     """Stands in for abi.Solver in the time-to-residual runner: the residual
     falls by 0.7 per outer iteration to a floor of 5e-8 while the synthetic
-    solve is on, and by 0.95 per iteration below it once it is off."""
+    solve corrects the distribution, and by 0.95 per iteration below it
+    once it corrects the moments only or is off."""
 
     def __init__(self, case, precision=0):
-        self.case, self.res, self.gsis_on, self.calls = case, 1.0, False, []
+        self.case, self.res, self.floored, self.calls = case, 1.0, False, []
 
     def init_maxwellian(self):
         pass
@@ -140,15 +141,15 @@ class _FakeSolver:
         pass
 
     def gsis(self, **kw):
-        self.gsis_on = kw.get("enable", 1) == 1
-        self.calls.append(("gsis", self.gsis_on))
+        self.floored = kw.get("enable", 1) == 1 and kw.get("correct_f", 0) == 1
+        self.calls.append(("gsis", kw.get("enable", 1), kw.get("correct_f", 0)))
 
     def set_precision(self, p):
         self.calls.append(("precision", p))
 
     def step(self, n):
         for _ in range(n):
-            self.res = max(5e-8, 0.7 * self.res) if self.gsis_on else 0.95 * self.res
+            self.res = max(5e-8, 0.7 * self.res) if self.floored else 0.95 * self.res
         return {"max_rms": self.res}
 
     def moments(self):
@@ -163,7 +164,7 @@ class _FakeSolver:
         pass
 
 
-def test_bench_hands_over_to_the_plain_iteration_at_the_synthetic_floor(cm, monkeypatch):
+def test_bench_finishes_with_the_moments_only_correction_at_the_synthetic_floor(cm, monkeypatch):
     import bench
     from hyb_gb300 import hyb_types as T
     made = []
@@ -174,11 +175,11 @@ def test_bench_hands_over_to_the_plain_iteration_at_the_synthetic_floor(cm, monk
 
     monkeypatch.setattr(bench.abi, "Solver", make)
     c = cm.couette_small(dt=1.0e6, sweep_order=1, mass_pin=1)
-    g = dict(ns_solver=2, line_mean=3)
+    g = dict(ns_solver=2, line_mean=3, ns_scheme=2, correct_f=1)
     out, _ = bench._ttr_run("x", c, T.HYB_PREC_FP64, g, False, False, tol=1e-8, max_iters=2000, chunk=10,
-                            handover_below=1e-6)
-    assert out["reached"] and out["plain_from_iteration"] is not None
-    assert ("gsis", False) in made[-1].calls
-    # without the hand-over the run stays on the floor
+                            finish_below=1e-6, finish_gsis=dict(g, correct_f=0))
+    assert out["reached"] and out["finish_from_iteration"] is not None
+    assert made[-1].calls == [("gsis", 1, 1), ("gsis", 1, 0)]
+    # without the finishing switch the run stays on the floor
     out2, _ = bench._ttr_run("x", c, T.HYB_PREC_FP64, g, False, False, tol=1e-8, max_iters=300, chunk=10)
-    assert not out2["reached"] and "plain_from_iteration" not in out2
+    assert not out2["reached"] and "finish_from_iteration" not in out2

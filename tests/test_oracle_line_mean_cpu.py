@@ -95,3 +95,25 @@ def test_the_limiter_sets_the_coarse_mesh_floor(pkg, ns_scheme, floor):
         assert r < 1e-9, r
     else:
         assert r > floor, r
+
+
+def test_moments_only_correction_finishes_the_sine_case(pkg):
+    """The sine-wall case at 64 x 64 (48^2 on [-5, 5], Kn 0.005): with the
+    harmonics and the unlimited NND stencil the coupled iteration settles
+    near 4e-8 with the distribution correction on; reconfigured to correct
+    the moments only it falls below 1e-8 within 20 more outer iterations
+    (4.9e-9 in the oracle)."""
+    from hyb_gb300 import cases
+    c = cases.couette_sine(ncx=64, ncy=64, dt=1.0e6, sweep_order=1, mass_pin=1, precision=0)
+    gk = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0, inner_rtol=1e-8,
+              relax_pct=70, line_mean=3, ns_scheme=2)
+    o = O.Oracle(c, threads=0)
+    o.init_maxwellian()
+    o.convert_ns()
+    o.gsis(**gk)
+    r50 = o.step(50)["max_rms"]
+    assert 1e-8 < r50 < 1e-6, r50
+    o.gsis(**dict(gk, correct_f=0))
+    r70 = o.step(20)["max_rms"]
+    assert r70 < 1e-8, r70
+    assert o.gsis_skipped() == 0
