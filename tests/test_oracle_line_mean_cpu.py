@@ -12,15 +12,20 @@ velocities on [-6, 6], plates +-0.5, walls 1 / 1.2, upwind order at dt 1e6,
 mass pin, band to the walls, line solver of 20 inner iterations at CFL 300),
 40 outer iterations take the residual to 1.9e-6 with it and 5.3e-3 without.
 """
+import os
+
 import pytest
 
 from oracle import oracle as O
+
+# every host core: an earlier test may have left the oracle at one thread
+THREADS = os.cpu_count() or 1
 
 
 def _run(cases, line_mean, nit):
     c = cases.Case(name="kn0.01-32x48", ncx=32, ncy=48, nvx=33, nvy=33, vmax=6.0, kn=0.01, uw=0.5, t_top=1.2,
                    dt=1.0e6, sweep_order=1, mass_pin=1)
-    o = O.Oracle(c, threads=0)
+    o = O.Oracle(c, threads=THREADS)
     o.init_maxwellian()
     o.convert_ns()
     o.gsis(wall_band=1, correct_f=1, ns_solver=2, line_mean=line_mean, cfl=300.0, max_inner=20, inner_tol=0.0,
@@ -45,7 +50,7 @@ def test_line_mean_is_ignored_without_the_line_solver_in_the_oracle(pkg, solver)
     c = cases.couette_small(ncx=8, ncy=16, nvx=17, nvy=17, dt=0.02)
     out = []
     for lm in (0, 1):
-        o = O.Oracle(c, threads=0)
+        o = O.Oracle(c, threads=THREADS)
         o.init_maxwellian()
         o.convert_ns()
         o.gsis(ns_solver=solver, line_mean=lm, max_inner=8, inner_tol=0.0, inner_rtol=0.0, cfl=20.0)
@@ -66,7 +71,7 @@ def test_harmonics_accelerate_the_sine_case(pkg):
     out = {}
     for lm in (1, 3):
         c = cases.couette_sine(ncx=64, ncy=64, dt=1.0e6, sweep_order=1, mass_pin=1, precision=0)
-        o = O.Oracle(c, threads=0)
+        o = O.Oracle(c, threads=THREADS)
         o.init_maxwellian()
         o.convert_ns()
         o.gsis(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0, inner_rtol=1e-8,
@@ -85,7 +90,7 @@ def test_the_limiter_sets_the_coarse_mesh_floor(pkg, ns_scheme, floor):
     from hyb_gb300 import cases
     c = cases.Case(name="kn0.01-4x32", ncx=4, ncy=32, nvx=48, nvy=48, vmax=6.0, kn=0.01, uw=0.5, t_top=1.2,
                    dt=1.0e6, sweep_order=1, mass_pin=1)
-    o = O.Oracle(c, threads=0)
+    o = O.Oracle(c, threads=THREADS)
     o.init_maxwellian()
     o.convert_ns()
     o.gsis(wall_band=1, correct_f=1, ns_solver=2, line_mean=1, cfl=300.0, max_inner=20, inner_tol=0.0,
@@ -107,7 +112,7 @@ def test_moments_only_correction_finishes_the_sine_case(pkg):
     c = cases.couette_sine(ncx=64, ncy=64, dt=1.0e6, sweep_order=1, mass_pin=1, precision=0)
     gk = dict(wall_band=1, correct_f=1, ns_solver=2, cfl=600.0, max_inner=16, inner_tol=0.0, inner_rtol=1e-8,
               relax_pct=70, line_mean=3, ns_scheme=2)
-    o = O.Oracle(c, threads=0)
+    o = O.Oracle(c, threads=THREADS)
     o.init_maxwellian()
     o.convert_ns()
     o.gsis(**gk)
