@@ -205,3 +205,24 @@ def test_line_mean_converges_to_the_oracle_fixed_point(cases_mod):
     for k in range(10):
         d = np.abs(Sg[..., k] - So[..., k]).max()
         assert d <= 1e-10 * max(np.abs(So[..., k]).max(), 1e-2), (k, d)
+
+
+def test_unlimited_nnd_stencil_matches_oracle(cases_mod):
+    """ns_scheme 2 (the NND stencil of the synthetic equation without its
+    limiter) with the line solver and two harmonics, then the moments-only
+    correction: the sine case's finishing configuration, on the 4 x 32
+    channel against the oracle after three outer iterations of each."""
+    c = _shape(cases_mod, "small", dt=1.0e6, sweep_order=1, mass_pin=1)
+    gk = dict(wall_band=1, correct_f=1, ns_solver=2, line_mean=3, ns_scheme=2, cfl=20.0, **FIXED)
+    g, o = _pair(c, 0, **gk)
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    _cmp_state(c, g, o, 1e-5)
+    g.gsis(**dict(gk, correct_f=0))
+    o.gsis(**dict(gk, correct_f=0))
+    for _ in range(3):
+        g.step(1)
+        o.step(1)
+    assert g.gsis_skipped() == o.gsis_skipped() == 0
+    _cmp_state(c, g, o, 1e-5)
